@@ -1,0 +1,749 @@
+// capi.cu -- the C ABI declared in include/neci_gpu.h.
+//
+// Host code only: argument checks, device allocation of the resident state,
+// host<->device copies and the launch sequence of one iteration (captured
+// once into a CUDA graph and replayed every step).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+using namespace neci;
+
+namespace {
+
+thread_local std::string g_last_error = "";
+
+int fail(int code, const std::string &msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t _e = (call);                                                              \
+        if (_e != cudaSuccess)                                                                \
+            return fail(NECI_GPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+template <typename T>
+int dalloc(Engine &e, T **p, size_t count) {
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t err = cudaMalloc((void **)p, count * sizeof(T));
+    if (err != cudaSuccess) return fail(NECI_GPU_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(err));
+    e.allocs.push_back((void *)*p);
+    err = cudaMemsetAsync(*p, 0, count * sizeof(T), e.stream);
+    if (err != cudaSuccess) return fail(NECI_GPU_ERR_CUDA, std::string("cudaMemset: ") + cudaGetErrorString(err));
+    return NECI_GPU_OK;
+}
+
+unsigned long long next_pow2(unsigned long long x) {
+    unsigned long long p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
+    d.tau = p.tau;
+    d.diag_sft[0] = p.diag_sft[0];
+    d.diag_sft[1] = p.diag_sft[1];
+    d.initiator_walk_no = p.initiator_walk_no;
+    d.occupied_thresh = p.occupied_thresh;
+    d.real_spawn_cutoff = p.real_spawn_cutoff;
+    d.av_mc_excits = p.av_mc_excits;
+    d.t_trunc_initiator = p.t_trunc_initiator;
+    d.t_init_coherent_rule = p.t_init_coherent_rule;
+    d.t_all_real_coeff = p.t_all_real_coeff;
+    d.t_real_spawn_cutoff = p.t_real_spawn_cutoff;
+    d.t_core_inits = p.t_core_inits;
+    d.precision = p.precision;
+    d.seed = p.seed;
+    d.iter = p.iter;
+}
+
+const char *kKernelNames[K_NUM] = {"rehash",      "begin",          "sweep",       "spawn",       "core",
+                                   "ann_probe",   "ann_compress",   "ann_insert",  "merge_stats", "final"};
+
+// Launch one kernel stage, bracketed by events when profiling.
+template <typename F>
+int stage(Engine &e, int id, F &&f) {
+    if (e.profiling) {
+        cudaEventRecord(e.ev[2 * id], e.stream);
+        f();
+        cudaEventRecord(e.ev[2 * id + 1], e.stream);
+        cudaEventSynchronize(e.ev[2 * id + 1]);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e.ev[2 * id], e.ev[2 * id + 1]);
+        e.kernel_ms[id] += ms;
+        e.kernel_launches[id] += 1;
+    } else {
+        f();
+    }
+    return NECI_GPU_OK;
+}
+
+// The launch sequence of one PerformFCIMCycPar step.
+void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
+    stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
+    stage(e, K_BEGIN, [&] { launch_begin(e, e.stream); });
+    stage(e, K_SWEEP, [&] { launch_sweep(e, e.stream); });
+    stage(e, K_SPAWN, [&] { launch_spawn(e, e.stream); });
+    if (e.st.n_core > 0) stage(e, K_CORE, [&] { launch_core(e, e.stream); });
+    stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
+    stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
+    stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream); });
+    stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, e.st.n_core > 0 ? 1 : 0); });
+    stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, advance); });
+}
+
+int ensure_graph(Engine &e) {
+    const bool core = e.st.n_core > 0;
+    if (e.graph && e.graph_core == core) return NECI_GPU_OK;
+    if (e.graph) {
+        cudaGraphExecDestroy(e.graph);
+        e.graph = nullptr;
+    }
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
+    step_sequence(e, e.d_stats + e.max_stats, 1);  // scratch record, copied out per step
+    CK(cudaStreamEndCapture(e.stream, &g));
+    CK(cudaGraphInstantiate(&e.graph, g, 0));
+    cudaGraphDestroy(g);
+    e.graph_core = core;
+    return NECI_GPU_OK;
+}
+
+template <typename T>
+int batch_io(Engine &e, const T *h, size_t n, T **d) {
+    CK(cudaMallocAsync((void **)d, std::max<size_t>(n, 1) * sizeof(T), e.stream));
+    if (h && n) CK(cudaMemcpyAsync(*d, h, n * sizeof(T), cudaMemcpyHostToDevice, e.stream));
+    return NECI_GPU_OK;
+}
+
+int check_ctx(neci_gpu_ctx *ctx) {
+    if (!ctx) return fail(NECI_GPU_ERR_INVALID, "null context");
+    return NECI_GPU_OK;
+}
+
+}  // namespace
+
+struct neci_gpu_ctx {
+    Engine e;
+};
+
+extern "C" {
+
+const char *neci_gpu_last_error(void) { return g_last_error.c_str(); }
+
+int32_t neci_gpu_num_kernels(void) { return K_NUM; }
+const char *neci_gpu_kernel_name(int32_t id) { return (id >= 0 && id < K_NUM) ? kKernelNames[id] : ""; }
+
+int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t device) {
+    if (!out || !sys) return fail(NECI_GPU_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (sys->nifd < 0 || sys->nifd + 1 > kMaxWords || sys->nbasis > 64 * (sys->nifd + 1) || sys->nbasis > 255)
+        return fail(NECI_GPU_ERR_UNSUPPORTED, "nBasis/NIfD outside the device layout (nBasis <= 255)");
+    if (sys->nel < 2 || sys->nel > kMaxNel) return fail(NECI_GPU_ERR_UNSUPPORTED, "nel outside 2..64");
+    if (sys->lenof_sign != 1 && sys->lenof_sign != 2) return fail(NECI_GPU_ERR_UNSUPPORTED, "lenof_sign must be 1 or 2");
+    if (sys->system == NECI_SYS_HUBBARD_REAL_SPACE) {
+        if (sys->excitgen != NECI_EXGEN_RS_HUBBARD) return fail(NECI_GPU_ERR_UNSUPPORTED, "lattice needs rs-hubbard generator");
+        if (sys->max_neighbours < 1 || sys->max_neighbours > kMaxNeigh) return fail(NECI_GPU_ERR_UNSUPPORTED, "max_neighbours");
+    } else if (sys->system == NECI_SYS_MOLECULAR) {
+        if (sys->excitgen != NECI_EXGEN_PCHB)
+            return fail(NECI_GPU_ERR_UNSUPPORTED, "molecular systems run the PCHB generator on the device");
+    } else {
+        return fail(NECI_GPU_ERR_UNSUPPORTED, "unknown system");
+    }
+    if (sys->max_walkers < 2 || sys->max_spawned < 1 || sys->max_walkers >= (1ll << 31) || sys->max_spawned >= (1ll << 31))
+        return fail(NECI_GPU_ERR_INVALID, "max_walkers / max_spawned out of range");
+    neci_gpu_ctx *ctx = new neci_gpu_ctx();
+    Engine &e = ctx->e;
+    e.desc = *sys;
+    e.device = device;
+    cudaError_t ce = cudaSetDevice(device);
+    if (ce != cudaSuccess) { delete ctx; return fail(NECI_GPU_ERR_CUDA, cudaGetErrorString(ce)); }
+    cudaDeviceGetAttribute(&e.num_sms, cudaDevAttrMultiProcessorCount, device);
+    ce = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { delete ctx; return fail(NECI_GPU_ERR_CUDA, cudaGetErrorString(ce)); }
+    DevSys &s = e.sys;
+    s.nel = sys->nel;
+    s.nbasis = sys->nbasis;
+    s.W = sys->nifd + 1;
+    s.L = sys->lenof_sign;
+    s.R = s.W + s.L + 1;
+    s.system = sys->system;
+    s.excitgen = sys->excitgen;
+    s.max_neigh = sys->max_neighbours;
+    s.uhub = sys->uhub;
+    s.bhub = sys->bhub;
+    s.ecore = sys->ecore;
+    s.p_singles = sys->p_singles;
+    s.p_parallel = sys->p_parallel;
+    s.nBI = sys->nbasis / 2;
+    DevState &st = e.st;
+    st.max_walkers = sys->max_walkers;
+    st.max_spawned = sys->max_spawned;
+    st.max_chunks = sys->max_walkers * s.L + sys->max_spawned + 1024;
+    st.hash_n = next_pow2(std::max<unsigned long long>((unsigned long long)sys->n_walker_hashes,
+                                                       2ull * (unsigned long long)sys->max_walkers));
+    st.spawn_hash_n = next_pow2(2ull * (unsigned long long)sys->max_spawned);
+    int rc = NECI_GPU_OK;
+#define A(p, n) if (rc == NECI_GPU_OK) rc = dalloc(e, &(p), (n))
+    int32_t *rh2 = nullptr;
+    A(rh2, (size_t)s.nbasis + 1);
+    s.random_hash2 = rh2;
+    A(st.dets, (size_t)st.max_walkers * s.R);
+    A(st.diagH, (size_t)st.max_walkers);
+    A(st.offdiagH, (size_t)st.max_walkers);
+    A(st.hash, (size_t)st.hash_n);
+    A(st.slot_bucket, (size_t)st.max_walkers);
+    A(st.free_list, (size_t)st.max_walkers + 1);
+    A(st.spawn, (size_t)st.max_spawned * s.R);
+    A(st.chunks, (size_t)st.max_chunks * 2);
+    A(st.acc, (size_t)st.max_walkers * s.L);
+    A(st.meta, (size_t)st.max_walkers * s.L);
+    A(st.cand, (size_t)st.max_spawned);
+    A(st.cand_h, (size_t)st.max_spawned);
+    A(st.spawn_hash, (size_t)st.spawn_hash_n);
+    A(st.reps, (size_t)st.max_spawned);
+    A(st.rep_bucket, (size_t)st.max_spawned);
+    A(st.rep_q, (size_t)st.max_spawned * s.L);
+    A(st.rep_cnt, (size_t)st.max_spawned * (s.L + 1));
+    A(st.ctl, 1);
+    A(e.d_params, 1);
+    e.max_stats = 4096;
+    A(e.d_stats, (size_t)e.max_stats + 1);
+#undef A
+    if (rc == NECI_GPU_OK) {
+        if (cudaMallocHost(&e.h_params, sizeof(IterParams)) != cudaSuccess ||
+            cudaMallocHost(&e.h_stats, sizeof(neci_gpu_iter_stats) * e.max_stats) != cudaSuccess)
+            rc = fail(NECI_GPU_ERR_CUDA, "cudaMallocHost failed");
+    }
+    if (rc == NECI_GPU_OK) {
+        std::memset(e.h_params, 0, sizeof(IterParams));
+        e.h_params->t_trunc_initiator = 1;  // CompressSpawnedList defaults for an initiator run
+        e.h_params->t_init_coherent_rule = 1;
+        for (int k = 0; k < 2 * K_NUM; ++k) cudaEventCreate(&e.ev[k]);
+        if (cudaStreamSynchronize(e.stream) != cudaSuccess) rc = fail(NECI_GPU_ERR_CUDA, "sync after init");
+    }
+    if (rc != NECI_GPU_OK) {
+        neci_gpu_free(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_free(neci_gpu_ctx *ctx) {
+    if (!ctx) return NECI_GPU_OK;
+    Engine &e = ctx->e;
+    cudaSetDevice(e.device);
+    if (e.stream) cudaStreamSynchronize(e.stream);
+    if (e.graph) cudaGraphExecDestroy(e.graph);
+    for (void *p : e.allocs) cudaFree(p);
+    if (e.h_params) cudaFreeHost(e.h_params);
+    if (e.h_stats) cudaFreeHost(e.h_stats);
+    for (int k = 0; k < 2 * K_NUM; ++k)
+        if (e.ev[k]) cudaEventDestroy(e.ev[k]);
+    if (e.stream) cudaStreamDestroy(e.stream);
+    delete ctx;
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_random_hash(neci_gpu_ctx *ctx, const int32_t *rh) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!rh) return fail(NECI_GPU_ERR_INVALID, "null RandomHash2");
+    Engine &e = ctx->e;
+    std::vector<int32_t> h(e.sys.nbasis + 1, 0);
+    for (int i = 1; i <= e.sys.nbasis; ++i) h[i] = rh[i - 1];
+    CK(cudaMemcpy((void *)e.sys.random_hash2, h.data(), h.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_tmat(neci_gpu_ctx *ctx, const double *t) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!t) return fail(NECI_GPU_ERR_INVALID, "null TMat2D");
+    Engine &e = ctx->e;
+    double *d = nullptr;
+    const size_t n = (size_t)e.sys.nbasis * e.sys.nbasis;
+    if (int r = dalloc(e, &d, n)) return r;
+    CK(cudaMemcpyAsync(d, t, n * sizeof(double), cudaMemcpyHostToDevice, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    e.sys.tmat = d;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *u, int64_t len) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!u || len <= 0) return fail(NECI_GPU_ERR_INVALID, "null UMAT");
+    Engine &e = ctx->e;
+    const long long P = (long long)e.sys.nBI * (e.sys.nBI + 1) / 2;
+    if (len < P * (P + 1) / 2) return fail(NECI_GPU_ERR_INVALID, "UMAT shorter than the 8-fold packed size");
+    double *d = nullptr;
+    if (int r = dalloc(e, &d, (size_t)len)) return r;
+    CK(cudaMemcpyAsync(d, u, (size_t)len * sizeof(double), cudaMemcpyHostToDevice, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    e.sys.umat = d;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_lattice(neci_gpu_ctx *ctx, const int32_t *nb, int32_t nsites) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!nb || nsites * 2 != e.sys.nbasis) return fail(NECI_GPU_ERR_INVALID, "lattice: nsites must be nBasis/2");
+    int32_t *d = nullptr;
+    const size_t n = (size_t)nsites * e.sys.max_neigh;
+    for (size_t i = 0; i < n; ++i)
+        if (nb[i] < 0 || nb[i] > nsites) return fail(NECI_GPU_ERR_INVALID, "lattice: neighbour index out of range");
+    if (int r = dalloc(e, &d, n)) return r;
+    CK(cudaMemcpyAsync(d, nb, n * sizeof(int32_t), cudaMemcpyHostToDevice, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    e.sys.neighbours = d;
+    e.sys.nsites = nsites;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!ref) return fail(NECI_GPU_ERR_INVALID, "null reference");
+    Engine &e = ctx->e;
+    int na = 0, nb = 0, ne = 0;
+    for (int w = 0; w < kMaxWords; ++w) e.sys.ilut_ref[w] = 0;
+    for (int w = 0; w < e.sys.W; ++w) {
+        const unsigned long long x = (unsigned long long)ref[w];
+        e.sys.ilut_ref[w] = x;
+        na += __builtin_popcountll(x & 0xAAAAAAAAAAAAAAAAull);
+        nb += __builtin_popcountll(x & 0x5555555555555555ull);
+    }
+    ne = na + nb;
+    if (ne != e.sys.nel) return fail(NECI_GPU_ERR_INVALID, "reference has the wrong electron count");
+    e.sys.nOccAlpha = na;
+    e.sys.nOccBeta = nb;
+    e.sys.hii = hii;
+    e.have_ref = true;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (e.sys.system != NECI_SYS_MOLECULAR || !e.sys.umat) return fail(NECI_GPU_ERR_INVALID, "PCHB needs a molecular system with UMAT");
+    DevSys &s = e.sys;
+    s.ijMax = (long long)s.nBI * (s.nBI + 1) / 2;
+    s.abMax = s.ijMax;
+    const size_t ntab = (size_t)s.ijMax * 3;
+    double *bias, *prob, *pexch;
+    int32_t *alias, *tgt;
+    uint8_t *present;
+    if (int r = dalloc(e, &bias, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &prob, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &alias, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &present, ntab)) return r;
+    if (int r = dalloc(e, &pexch, (size_t)s.ijMax)) return r;
+    if (int r = dalloc(e, &tgt, (size_t)s.abMax + 1)) return r;
+    std::vector<int32_t> tp(s.abMax + 1, 0);
+    for (int a = 1; a <= s.nBI; ++a)
+        for (int b = 1; b <= a; ++b) tp[(long long)b + (long long)a * (a - 1) / 2] = (b << 16) | a;
+    CK(cudaMemcpyAsync(tgt, tp.data(), tp.size() * sizeof(int32_t), cudaMemcpyHostToDevice, e.stream));
+    s.alias_bias = bias;
+    s.alias_prob = prob;
+    s.alias_alias = alias;
+    s.alias_present = present;
+    s.pexch = pexch;
+    s.tgt_pair = tgt;
+    launch_pchb_build(e);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e.stream));
+    e.have_pchb = true;
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_upload_walkers(neci_gpu_ctx *ctx, const int64_t *ilut, int64_t nrows, const double *dh,
+                                const double *odh) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!ilut && nrows > 0) return fail(NECI_GPU_ERR_INVALID, "null rows");
+    if (nrows < 0 || nrows >= e.st.max_walkers) return fail(NECI_GPU_ERR_LIST_FULL, "more rows than MaxWalkersPart - 1");
+    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
+    const int R = e.sys.R;
+    CK(cudaMemsetAsync(e.st.dets, 0, (size_t)e.st.max_walkers * R * 8, e.stream));
+    CK(cudaMemsetAsync(e.st.hash, 0, (size_t)e.st.hash_n * 4, e.stream));
+    CK(cudaMemsetAsync(e.st.acc, 0, (size_t)e.st.max_walkers * e.sys.L * 8, e.stream));
+    CK(cudaMemsetAsync(e.st.meta, 0, (size_t)e.st.max_walkers * e.sys.L * 4, e.stream));
+    if (nrows > 0) CK(cudaMemcpyAsync(e.st.dets, ilut, (size_t)nrows * R * 8, cudaMemcpyHostToDevice, e.stream));
+    const int compute = (dh && odh) ? 0 : 1;
+    if (!compute && nrows > 0) {
+        CK(cudaMemcpyAsync(e.st.diagH, dh, (size_t)nrows * 8, cudaMemcpyHostToDevice, e.stream));
+        CK(cudaMemcpyAsync(e.st.offdiagH, odh, (size_t)nrows * 8, cudaMemcpyHostToDevice, e.stream));
+    }
+    Control c{};
+    c.tot_walkers = (unsigned long long)nrows;
+    CK(cudaMemcpyAsync(e.st.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice, e.stream));
+    // the core space belongs to the previous list
+    e.st.n_core = 0;
+    if (nrows > 0) launch_upload_fix(e, nrows, compute);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e.stream));
+    int err = 0;
+    CK(cudaMemcpy(&err, &e.st.ctl->err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return fail(err, "upload: hash table full");
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_download_walkers(neci_gpu_ctx *ctx, int64_t *ilut, double *dh, double *odh, int64_t max_rows,
+                                  int64_t *nrows) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!ilut || !nrows) return fail(NECI_GPU_ERR_INVALID, "null output");
+    CK(cudaStreamSynchronize(e.stream));
+    unsigned long long tw = 0;
+    CK(cudaMemcpy(&tw, &e.st.ctl->tot_walkers, sizeof(tw), cudaMemcpyDeviceToHost));
+    tw = std::min<unsigned long long>(tw, (unsigned long long)e.st.max_walkers);
+    const int R = e.sys.R, W = e.sys.W, L = e.sys.L;
+    std::vector<long long> rows((size_t)tw * R);
+    std::vector<double> d1(tw), d2(tw);
+    if (tw) {
+        CK(cudaMemcpy(rows.data(), e.st.dets, (size_t)tw * R * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(d1.data(), e.st.diagH, (size_t)tw * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(d2.data(), e.st.offdiagH, (size_t)tw * 8, cudaMemcpyDeviceToHost));
+    }
+    long long n = 0;
+    for (unsigned long long j = 0; j < tw; ++j) {
+        const long long *r = &rows[j * R];
+        bool occ = e.st.n_core > 0 && ((r[W + L] >> NECI_FLAG_DETERMINISTIC_1) & 1);
+        for (int k = 0; k < L; ++k) {
+            double v;
+            std::memcpy(&v, &r[W + k], 8);
+            if (std::fabs(v) >= 1e-12) occ = true;
+        }
+        if (!occ) continue;
+        if (n >= max_rows) return fail(NECI_GPU_ERR_INVALID, "download: output too small");
+        std::memcpy(ilut + (size_t)n * R, r, (size_t)R * 8);
+        if (dh) dh[n] = d1[j];
+        if (odh) odh[n] = d2[j];
+        ++n;
+    }
+    *nrows = n;
+    return NECI_GPU_OK;
+}
+
+static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_gpu_iter_stats *stats,
+                     double *device_ms = nullptr) {
+    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
+    if (e.sys.system == NECI_SYS_MOLECULAR && !e.have_pchb) return fail(NECI_GPU_ERR_INVALID, "call neci_gpu_init_pchb first");
+    if (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours) return fail(NECI_GPU_ERR_INVALID, "set the lattice first");
+    if (!e.sys.tmat) return fail(NECI_GPU_ERR_INVALID, "set TMat2D first");
+    if (p->tau <= 0.0 || p->av_mc_excits <= 0.0) return fail(NECI_GPU_ERR_INVALID, "tau and AvMCExcits must be positive");
+    copy_params(*e.h_params, *p);
+    CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
+    int done = 0;
+    if (device_ms) *device_ms = 0.0;
+    if (!e.profiling)
+        if (int r = ensure_graph(e)) return r;
+    while (done < n_iter) {
+        const int batch = std::min(n_iter - done, e.max_stats);
+        if (device_ms) CK(cudaEventRecord(e.ev[0], e.stream));
+        if (e.profiling) {
+            for (int i = 0; i < batch; ++i) step_sequence(e, e.d_stats + i, 1);
+        } else {
+            for (int i = 0; i < batch; ++i) {
+                CK(cudaGraphLaunch(e.graph, e.stream));
+                CK(cudaMemcpyAsync(e.d_stats + i, e.d_stats + e.max_stats, sizeof(neci_gpu_iter_stats),
+                                   cudaMemcpyDeviceToDevice, e.stream));
+            }
+        }
+        if (device_ms) CK(cudaEventRecord(e.ev[1], e.stream));
+        CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats) * batch, cudaMemcpyDeviceToHost, e.stream));
+        CK(cudaStreamSynchronize(e.stream));
+        CK(cudaGetLastError());
+        if (device_ms) {
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, e.ev[0], e.ev[1]));
+            *device_ms += ms;
+        }
+        std::memcpy(stats + done, e.h_stats, sizeof(neci_gpu_iter_stats) * batch);
+        for (int i = 0; i < batch; ++i)
+            if (stats[done + i].err) {
+                done += i + 1;
+                return fail(stats[done - 1].err, "device reported an error in the step");
+            }
+        done += batch;
+    }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_iterate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, neci_gpu_iter_stats *stats) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!p || !stats) return fail(NECI_GPU_ERR_INVALID, "null argument");
+    return run_steps(ctx->e, p, 1, stats);
+}
+
+int32_t neci_gpu_iterate_n(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, int32_t n_iter, neci_gpu_iter_stats *stats) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!p || !stats || n_iter < 1) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    return run_steps(ctx->e, p, n_iter, stats);
+}
+
+int32_t neci_gpu_iterate_timed(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, int32_t n_iter,
+                               neci_gpu_iter_stats *stats, double *device_ms) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!p || !stats || n_iter < 1 || !device_ms) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    if (ctx->e.profiling) return fail(NECI_GPU_ERR_INVALID, "timed steps need profiling off");
+    return run_steps(ctx->e, p, n_iter, stats, device_ms);
+}
+
+static int upload_spawns(Engine &e, const int64_t *sp, int64_t n) {
+    if (n < 0 || n > e.st.max_spawned) return fail(NECI_GPU_ERR_SPAWN_FULL, "spawn list longer than MaxSpawned");
+    if (n > 0) CK(cudaMemcpyAsync(e.st.spawn, sp, (size_t)n * e.sys.R * 8, cudaMemcpyHostToDevice, e.stream));
+    launch_convert_spawns(e, n);
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_annihilate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, const int64_t *spawned, int64_t n,
+                            neci_gpu_iter_stats *stats) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!p || !stats || (!spawned && n > 0)) return fail(NECI_GPU_ERR_INVALID, "null argument");
+    copy_params(*e.h_params, *p);
+    CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
+    launch_rehash(e, e.stream);
+    launch_begin(e, e.stream);
+    launch_collect_holes(e);
+    if (int r = upload_spawns(e, spawned, n)) return r;
+    launch_ann_probe(e, e.stream);
+    launch_ann_compress(e, e.stream);
+    launch_ann_insert(e, e.stream);
+    launch_merge_stats(e, e.stream, 0);
+    launch_final(e, e.stream, e.d_stats, 0);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    *stats = e.h_stats[0];
+    stats->n_spawned = n;
+    if (stats->err) return fail(stats->err, "device reported an error in the annihilation");
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_compress_spawns(neci_gpu_ctx *ctx, const int64_t *spawned, int64_t n, int64_t *out, int64_t *n_out,
+                                 double *nannihil) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if ((!spawned && n > 0) || !out || !n_out) return fail(NECI_GPU_ERR_INVALID, "null argument");
+    const int R = e.sys.R, W = e.sys.W, L = e.sys.L;
+    launch_begin(e, e.stream);
+    if (int r = upload_spawns(e, spawned, n)) return r;
+    launch_all_cand(e);
+    launch_ann_compress(e, e.stream);
+    long long *d_out = nullptr;
+    unsigned long long *d_n = nullptr;
+    CK(cudaMallocAsync(&d_out, (size_t)std::max<int64_t>(n, 1) * R * 8, e.stream));
+    CK(cudaMallocAsync(&d_n, sizeof(unsigned long long), e.stream));
+    CK(cudaMemsetAsync(d_n, 0, sizeof(unsigned long long), e.stream));
+    launch_compress_out(e, d_out, d_n);
+    CK(cudaGetLastError());
+    unsigned long long hn = 0;
+    Control c{};
+    CK(cudaMemcpyAsync(&hn, d_n, sizeof(hn), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaMemcpyAsync(&c, e.st.ctl, sizeof(Control), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    std::vector<long long> rows((size_t)hn * R);
+    if (hn) CK(cudaMemcpyAsync(rows.data(), d_out, (size_t)hn * R * 8, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaFreeAsync(d_out, e.stream));
+    CK(cudaFreeAsync(d_n, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    if (c.err) return fail(c.err, "device reported an error in the compression");
+    // order of CompressSpawnedList's output: sorted by ilut_lt
+    std::vector<size_t> idx(hn);
+    for (size_t i = 0; i < hn; ++i) idx[i] = i;
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) {
+        for (int w = 0; w < W; ++w)
+            if (rows[a * R + w] != rows[b * R + w]) return rows[a * R + w] < rows[b * R + w];
+        return false;
+    });
+    for (size_t i = 0; i < hn; ++i) std::memcpy(out + i * R, &rows[idx[i] * R], (size_t)R * 8);
+    *n_out = (int64_t)hn;
+    if (nannihil)
+        for (int k = 0; k < L; ++k) nannihil[k] = (double)(long long)(c.abs_q[k] - c.abs_s[k]) * 0x1.0p-32;
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_find_walker_hash(neci_gpu_ctx *ctx, const int64_t *dets, int64_t n, int64_t len, int64_t *out) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (n < 0 || len < 1 || (n > 0 && (!dets || !out))) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    if (n == 0) return NECI_GPU_OK;
+    long long *dd, *dout;
+    if (int r = batch_io(e, (const long long *)dets, (size_t)n * e.sys.W, &dd)) return r;
+    if (int r = batch_io<long long>(e, nullptr, (size_t)n, &dout)) return r;
+    launch_util_hash(e, dd, n, (unsigned long long)len, dout);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, (size_t)n * 8, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaFreeAsync(dd, e.stream));
+    CK(cudaFreeAsync(dout, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_excit_level(neci_gpu_ctx *ctx, const int64_t *a, const int64_t *b, int64_t n, int32_t *out) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    if (n == 0) return NECI_GPU_OK;
+    long long *da, *db;
+    int *dout;
+    if (int r = batch_io(e, (const long long *)a, (size_t)n * e.sys.W, &da)) return r;
+    if (int r = batch_io(e, (const long long *)b, (size_t)n * e.sys.W, &db)) return r;
+    if (int r = batch_io<int>(e, nullptr, (size_t)n, &dout)) return r;
+    launch_util_excit_level(e, da, db, n, dout);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, (size_t)n * 4, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaFreeAsync(da, e.stream));
+    CK(cudaFreeAsync(db, e.stream));
+    CK(cudaFreeAsync(dout, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_helement(neci_gpu_ctx *ctx, const int64_t *a, const int64_t *b, int64_t n, double *out) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    if (!e.sys.tmat) return fail(NECI_GPU_ERR_INVALID, "set TMat2D first");
+    if (e.sys.system == NECI_SYS_MOLECULAR && !e.sys.umat) return fail(NECI_GPU_ERR_INVALID, "set UMAT first");
+    if (n == 0) return NECI_GPU_OK;
+    long long *da, *db;
+    double *dout;
+    if (int r = batch_io(e, (const long long *)a, (size_t)n * e.sys.W, &da)) return r;
+    if (int r = batch_io(e, (const long long *)b, (size_t)n * e.sys.W, &db)) return r;
+    if (int r = batch_io<double>(e, nullptr, (size_t)n, &dout)) return r;
+    launch_util_helement(e, da, db, n, dout);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, dout, (size_t)n * 8, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaFreeAsync(da, e.stream));
+    CK(cudaFreeAsync(db, e.stream));
+    CK(cudaFreeAsync(dout, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_gen_excit(neci_gpu_ctx *ctx, const int64_t *det, int64_t n, uint64_t seed, int64_t iter,
+                           int64_t *child, double *pgen, double *hel) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (n < 0 || !det || (n > 0 && (!child || !pgen || !hel))) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
+    if (e.sys.system == NECI_SYS_MOLECULAR && !e.have_pchb) return fail(NECI_GPU_ERR_INVALID, "call neci_gpu_init_pchb first");
+    if (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours) return fail(NECI_GPU_ERR_INVALID, "set the lattice first");
+    if (n == 0) return NECI_GPU_OK;
+    int nel = 0;
+    for (int w = 0; w < e.sys.W; ++w) nel += __builtin_popcountll((unsigned long long)det[w]);
+    if (nel != e.sys.nel) return fail(NECI_GPU_ERR_INVALID, "determinant has the wrong electron count");
+    long long *dd, *dc;
+    double *dp, *dh;
+    if (int r = batch_io(e, (const long long *)det, (size_t)e.sys.W, &dd)) return r;
+    if (int r = batch_io<long long>(e, nullptr, (size_t)n * e.sys.W, &dc)) return r;
+    if (int r = batch_io<double>(e, nullptr, (size_t)n, &dp)) return r;
+    if (int r = batch_io<double>(e, nullptr, (size_t)n, &dh)) return r;
+    launch_util_gen_excit(e, dd, n, seed, iter, dc, dp, dh);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(child, dc, (size_t)n * e.sys.W * 8, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaMemcpyAsync(pgen, dp, (size_t)n * 8, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaMemcpyAsync(hel, dh, (size_t)n * 8, cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaFreeAsync(dd, e.stream));
+    CK(cudaFreeAsync(dc, e.stream));
+    CK(cudaFreeAsync(dp, e.stream));
+    CK(cudaFreeAsync(dh, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core, int64_t n_core, int32_t precision) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    (void)precision;  // both value arrays are kept; the step's precision picks one
+    if (n_core < 1 || !core || n_core >= (1ll << 31)) return fail(NECI_GPU_ERR_INVALID, "bad core space");
+    DevState &st = e.st;
+    const int W = e.sys.W, L = e.sys.L;
+    if (!st.core_of_slot) {
+        if (int r = dalloc(e, &st.core_of_slot, (size_t)st.max_walkers)) return r;
+    }
+    CK(cudaMemsetAsync(st.core_of_slot, 0xFF, (size_t)st.max_walkers * 4, e.stream));
+    long long *dcore = nullptr, *counts = nullptr;
+    if (int r = dalloc(e, &dcore, (size_t)n_core * W)) return r;
+    CK(cudaMemcpyAsync(dcore, core, (size_t)n_core * W * 8, cudaMemcpyHostToDevice, e.stream));
+    if (int r = dalloc(e, &st.core_slot, (size_t)n_core)) return r;
+    if (int r = dalloc(e, &st.core_x, (size_t)n_core * L)) return r;
+    if (int r = dalloc(e, &st.core_y, (size_t)n_core * L)) return r;
+    if (int r = dalloc(e, &st.core_rowptr, (size_t)n_core + 1)) return r;
+    if (int r = dalloc(e, &counts, (size_t)n_core)) return r;
+    CK(cudaMemsetAsync(&st.ctl->err, 0, sizeof(int), e.stream));
+    launch_core_mark(e, dcore, n_core);
+    launch_core_count(e, dcore, n_core, counts);
+    CK(cudaGetLastError());
+    std::vector<long long> hc(n_core), rp(n_core + 1, 0);
+    CK(cudaMemcpyAsync(hc.data(), counts, (size_t)n_core * 8, cudaMemcpyDeviceToHost, e.stream));
+    int err = 0;
+    CK(cudaMemcpyAsync(&err, &st.ctl->err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    if (err) return fail(NECI_GPU_ERR_INVALID, "core determinant not in CurrentDets");
+    for (long long i = 0; i < n_core; ++i) rp[i + 1] = rp[i] + hc[i];
+    const long long nnz = rp[n_core];
+    CK(cudaMemcpyAsync(st.core_rowptr, rp.data(), (size_t)(n_core + 1) * 8, cudaMemcpyHostToDevice, e.stream));
+    if (int r = dalloc(e, &st.core_col, (size_t)nnz)) return r;
+    if (int r = dalloc(e, &st.core_val, (size_t)nnz)) return r;
+    if (int r = dalloc(e, &st.core_val32, (size_t)nnz)) return r;
+    st.n_core = n_core;
+    launch_core_fill(e, dcore, n_core);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e.stream));
+    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_core_nnz(neci_gpu_ctx *ctx, int64_t *nnz) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!nnz) return fail(NECI_GPU_ERR_INVALID, "null argument");
+    if (e.st.n_core == 0) { *nnz = 0; return NECI_GPU_OK; }
+    long long v = 0;
+    CK(cudaMemcpy(&v, e.st.core_rowptr + e.st.n_core, 8, cudaMemcpyDeviceToHost));
+    *nnz = v;
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_profiling(neci_gpu_ctx *ctx, int32_t on) {
+    if (int r = check_ctx(ctx)) return r;
+    ctx->e.profiling = on != 0;
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_kernel_times(neci_gpu_ctx *ctx, double *ms, int64_t *launches, int32_t n) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    for (int k = 0; k < n && k < K_NUM; ++k) {
+        if (ms) ms[k] = e.kernel_ms[k];
+        if (launches) launches[k] = e.kernel_launches[k];
+        e.kernel_ms[k] = 0.0;
+        e.kernel_launches[k] = 0;
+    }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_sync(neci_gpu_ctx *ctx) {
+    if (int r = check_ctx(ctx)) return r;
+    CK(cudaStreamSynchronize(ctx->e.stream));
+    return NECI_GPU_OK;
+}
+
+}  // extern "C"

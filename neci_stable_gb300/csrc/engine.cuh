@@ -1,0 +1,380 @@
+// engine.cuh -- device data layout and device functions of the FCIQMC engine.
+//
+// Walker rows are NECI CurrentDets rows (bit_rep_data.F90:10-17): W det
+// words, L signs (real(dp) bits), one flag word; R = W + L + 1 int64 words.
+// Spawn records carry the same words, except that the L sign words hold the
+// amplitude in 64-bit fixed point (NECI_SPAWN_FIXED_BITS fractional bits)
+// while spawns are being summed.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/neci_gpu.h"
+
+namespace neci {
+
+constexpr int kMaxWords = 4;      // nBasis <= 255 (NIfD <= 3)
+constexpr int kMaxNel = 64;
+constexpr int kMaxNeigh = 8;
+constexpr int kChunk = 16;        // spawn attempts per work item
+constexpr int kProbeLimit = 1 << 16;
+constexpr uint32_t kEmpty = 0u;
+constexpr uint32_t kTomb = 0xFFFFFFFFu;
+constexpr double kEps12 = 1e-12;
+
+enum Purpose : uint32_t { P_NSPAWN = 1, P_ATTEMPT = 2, P_DEATH = 3, P_ANN_ROUND = 4, P_STATS_ROUND = 5 };
+
+// Per-iteration counters and estimator sums (one instance in device memory).
+struct Control {
+    unsigned long long tot_walkers;     // slots in use (TotWalkers)
+    unsigned long long n_free;          // holes pushed this step
+    unsigned long long free_taken;      // holes reused by new determinants
+    unsigned long long n_chunks;        // spawn work items
+    unsigned long long n_spawned;       // spawn records
+    unsigned long long n_cand;          // spawns onto determinants not in the list
+    unsigned long long n_reps;          // unique new determinants
+    unsigned long long n_new;           // determinants inserted
+    unsigned long long n_attempts;      // spawn attempts
+    unsigned long long n_occupied;
+    unsigned long long n_holes;
+    unsigned long long n_tomb;          // hash tombstones
+    unsigned long long n_found;         // unique spawned determinants already present
+    unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
+    unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
+    int err;
+    int rehash;                         // rebuild the walker hash at the next step
+    double nborn[2], ndied[2], nannihil[2], naborted[2], nremoved[2];
+    double tot_parts[2], tot_parts_old[2], noat_hf[2], hf_cyc[2], enum_cyc[2], norm[2];
+};
+
+// System description as seen by the kernels (passed by value).
+struct DevSys {
+    int nel, nbasis, W, L, R, system, excitgen, max_neigh, nsites, nOccAlpha, nOccBeta, nBI;
+    double uhub, bhub, ecore, p_singles, p_parallel, hii;
+    long long ijMax, abMax;
+    unsigned long long ilut_ref[kMaxWords];
+    const int32_t *random_hash2;   // [nbasis + 1], 1-based
+    const double *tmat;            // TMat2D column-major
+    const double *umat;            // UMAT, UMatInd - 1
+    const int32_t *neighbours;     // [nsites * max_neigh], 1-based site, 0 = none
+    const double *pexch;           // [ijMax]
+    const double *alias_bias;      // [(ij-1)*3 + type-1][abMax]
+    const int32_t *alias_alias;
+    const double *alias_prob;
+    const uint8_t *alias_present;  // [(ij-1)*3 + type-1]
+    const int32_t *tgt_pair;       // [abMax+1]: (small << 16) | large
+};
+
+// Resident walker state (device pointers).
+struct DevState {
+    long long *dets;               // CurrentDets rows
+    double *diagH, *offdiagH;      // global_det_data diagH - Hii, offdiagH
+    uint32_t *hash;                // walker hash: slot+1, kEmpty, kTomb
+    unsigned long long hash_n;     // buckets (power of two)
+    uint32_t *slot_bucket;         // bucket holding each slot
+    int32_t *free_list;
+    long long max_walkers, max_spawned, max_chunks;
+    long long *spawn;              // spawn records
+    unsigned long long *chunks;    // pairs: slot | run << 32 | neg << 33 | n << 34, first attempt
+    long long *acc;                // per slot*L fixed-point spawn sums (found determinants)
+    uint32_t *meta;                // per slot*L spawn counts | initiator bit 31
+    uint32_t *cand;                // record index of spawns onto absent determinants
+    unsigned long long *cand_h;    // their 64-bit NECI hash
+    uint32_t *spawn_hash;          // compression table: candidate position + 1
+    unsigned long long spawn_hash_n;
+    uint32_t *reps;                // candidate position of each unique new determinant
+    uint32_t *rep_bucket;
+    long long *rep_q;              // per candidate*L fixed-point sums
+    uint32_t *rep_cnt;             // per candidate*L counts | initiator bit 31
+    // semistochastic core
+    long long n_core;
+    int32_t *core_of_slot;         // core index or -1
+    long long *core_slot;
+    double *core_x, *core_y;
+    long long *core_rowptr;
+    int32_t *core_col;
+    double *core_val;
+    float *core_val32;
+    Control *ctl;
+};
+
+struct IterParams {
+    double tau, diag_sft[2], initiator_walk_no, occupied_thresh, real_spawn_cutoff, av_mc_excits;
+    int t_trunc_initiator, t_init_coherent_rule, t_all_real_coeff, t_real_spawn_cutoff, t_core_inits, precision;
+    unsigned long long seed;
+    long long iter;
+};
+
+// ---------------------------------------------------------------------------
+// Philox-4x32-10 (Salmon et al., SC11) and the per-determinant stream.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline void philox_block(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const unsigned long long p0 = (unsigned long long)0xD2511F53u * c0;
+        const unsigned long long p1 = (unsigned long long)0xCD9E8D57u * c2;
+        const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+__host__ __device__ inline unsigned long long splitmix64(unsigned long long x) {
+    x += 0x9E3779B97F4A7C15ull;
+    unsigned long long z = x;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__host__ __device__ inline unsigned long long det_key(const unsigned long long *det, int W, unsigned long long seed) {
+    unsigned long long h = seed ^ 0x6A09E667F3BCC909ull;
+    for (int i = 0; i < W; ++i) h = splitmix64(h ^ det[i]);
+    return h;
+}
+
+struct Stream {
+    uint32_t key[2];
+    uint32_t ctr[4];
+    double buf[2];
+    int have;
+    __device__ inline Stream(unsigned long long dkey, long long iter, uint32_t purpose, uint32_t run, uint32_t attempt) {
+        key[0] = (uint32_t)dkey;
+        key[1] = (uint32_t)(dkey >> 32);
+        ctr[0] = attempt;
+        ctr[1] = 0;
+        ctr[2] = (uint32_t)iter;
+        ctr[3] = purpose | (run << 8) | ((uint32_t)((unsigned long long)iter >> 32) << 16);
+        have = 0;
+    }
+    __device__ inline double next() {
+        if (have == 0) {
+            uint32_t o[4];
+            philox_block(ctr, key, o);
+            ctr[1] += 1;
+            const unsigned long long a = ((unsigned long long)o[1] << 32) | o[0];
+            const unsigned long long b = ((unsigned long long)o[3] << 32) | o[2];
+            buf[0] = (double)(a >> 11) * 0x1.0p-53;
+            buf[1] = (double)(b >> 11) * 0x1.0p-53;
+            have = 2;
+        }
+        const double v = (have == 2) ? buf[0] : buf[1];
+        --have;
+        return v;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Fixed point and sign words.
+// ---------------------------------------------------------------------------
+__device__ inline long long to_fixed(double x, int *overflow) {
+    const double s = x * 4294967296.0;  // 2^NECI_SPAWN_FIXED_BITS
+    if (!(fabs(s) < 9.2e18)) { *overflow = 1; return 0; }
+    return __double2ll_rn(s);
+}
+__device__ inline double from_fixed(long long q) { return __ll2double_rn(q) * 0x1.0p-32; }
+__device__ inline double word_to_double(long long w) { return __longlong_as_double(w); }
+__device__ inline long long double_to_word(double d) { return __double_as_longlong(d); }
+__device__ inline double fsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+
+__device__ inline int init_flag_bit(int run) { return run == 0 ? NECI_FLAG_INITIATOR_1 : NECI_FLAG_INITIATOR_2; }
+__device__ inline bool test_bit(long long f, int b) { return ((unsigned long long)f >> b) & 1ull; }
+__device__ inline bool is_core_flags(long long f) { return test_bit(f, NECI_FLAG_DETERMINISTIC_1); }
+
+// ---------------------------------------------------------------------------
+// Bit strings.
+// ---------------------------------------------------------------------------
+__device__ inline int excit_level(const unsigned long long *a, const unsigned long long *b, int W) {
+    int ic = 0;
+    for (int i = 0; i < W; ++i) ic += __popcll(a[i] & ~b[i]);
+    return ic;
+}
+__device__ inline bool det_eq(const unsigned long long *a, const long long *b, int W) {
+    for (int i = 0; i < W; ++i)
+        if ((long long)a[i] != b[i]) return false;
+    return true;
+}
+__device__ inline bool orb_occ(const unsigned long long *d, int orb) {
+    return (d[(orb - 1) >> 6] >> ((orb - 1) & 63)) & 1ull;
+}
+__device__ inline void flip_orb(unsigned long long *d, int orb) { d[(orb - 1) >> 6] ^= 1ull << ((orb - 1) & 63); }
+// Occupied orbitals strictly between orbitals lo < hi.
+__device__ inline int occ_between(const unsigned long long *d, int W, int lo, int hi) {
+    int n = 0;
+    for (int w = 0; w < W; ++w) {
+        const int base = w * 64;  // orbital base+1 is bit 0
+        // bits for orbitals lo+1 .. hi-1 -> bit positions lo .. hi-2
+        const int b0 = lo - base, b1 = hi - 2 - base;  // inclusive range in this word
+        if (b1 < 0 || b0 > 63) continue;
+        const int s = b0 < 0 ? 0 : b0, e = b1 > 63 ? 63 : b1;
+        if (s > e) continue;
+        const unsigned long long mask = (e - s == 63) ? ~0ull : (((1ull << (e - s + 1)) - 1ull) << s);
+        n += __popcll(d[w] & mask);
+    }
+    return n;
+}
+// decode_bit_det: ascending occupied orbitals.
+__device__ inline int decode(const unsigned long long *d, int W, uint8_t *nI) {
+    int n = 0;
+    for (int w = 0; w < W; ++w) {
+        unsigned long long x = d[w];
+        while (x) {
+            const int b = __ffsll((long long)x) - 1;
+            nI[n++] = (uint8_t)(w * 64 + b + 1);
+            x &= x - 1;
+        }
+    }
+    return n;
+}
+
+// FindWalkerHash (hash.F90:23-38): full 64-bit value before the modulo.
+__device__ inline unsigned long long neci_hash(const unsigned long long *d, int W, const int32_t *rh2) {
+    unsigned long long hash = 0;
+    int i = 0;
+    for (int w = 0; w < W; ++w) {
+        unsigned long long x = d[w];
+        while (x) {
+            const int b = __ffsll((long long)x) - 1;
+            const int orb = w * 64 + b + 1;
+            ++i;
+            const long long term = (long long)(int32_t)(rh2[orb] * i);
+            hash = 1099511628211ull * hash + (unsigned long long)term;
+            x &= x - 1;
+        }
+    }
+    return hash;
+}
+// abs(mod(h, n)) with Fortran's sign-of-dividend mod, 0-based.
+__device__ inline unsigned long long hash_mod(unsigned long long hash, unsigned long long n) {
+    const long long h = (long long)hash;
+    const unsigned long long mag = h < 0 ? (0ull - (unsigned long long)h) : (unsigned long long)h;
+    return mag % n;
+}
+
+// ---------------------------------------------------------------------------
+// Integrals.
+// ---------------------------------------------------------------------------
+__device__ inline double tmat_el(const DevSys &s, int i, int j) {
+    return __ldg(&s.tmat[(size_t)(j - 1) * s.nbasis + (i - 1)]);
+}
+__device__ inline long long umat_ind(int I, int J, int K, int L) {
+    long long A, B;
+    if (I > K) A = (long long)I * (I - 1) / 2 + K; else A = (long long)K * (K - 1) / 2 + I;
+    if (J > L) B = (long long)J * (J - 1) / 2 + L; else B = (long long)L * (L - 1) / 2 + J;
+    return A > B ? A * (A - 1) / 2 + B : B * (B - 1) / 2 + A;
+}
+__device__ inline double umat_el(const DevSys &s, int i, int j, int k, int l) {
+    return __ldg(&s.umat[umat_ind(i, j, k, l) - 1]);
+}
+__device__ inline int spat(int orb) { return (orb + 1) >> 1; }
+__device__ inline bool beta(int orb) { return orb & 1; }
+
+// sltcnd_1_kernel (sltcnd.fpp:643-679): Coulomb terms over the occupied
+// list, then exchange terms, then the one-electron element.
+__device__ inline double sltcnd_1(const DevSys &s, const unsigned long long *d, int src, int tgt) {
+    double hel = 0.0;
+    const int id1 = spat(src), id2 = spat(tgt);
+    if (beta(src) == beta(tgt)) {
+        for (int w = 0; w < s.W; ++w) {
+            unsigned long long x = d[w];
+            while (x) {
+                const int o = w * 64 + __ffsll((long long)x);
+                x &= x - 1;
+                if (o != src) hel += umat_el(s, id1, spat(o), id2, spat(o));
+            }
+        }
+        for (int w = 0; w < s.W; ++w) {
+            unsigned long long x = d[w];
+            while (x) {
+                const int o = w * 64 + __ffsll((long long)x);
+                x &= x - 1;
+                if (o != src && beta(o) == beta(src)) hel -= umat_el(s, id1, spat(o), spat(o), id2);
+            }
+        }
+    }
+    hel += tmat_el(s, src, tgt);
+    return hel;
+}
+// sltcnd_2_kernel (sltcnd.fpp:690-711), ex sorted: i<j, a<b.
+__device__ inline double sltcnd_2(const DevSys &s, int i, int j, int a, int b) {
+    double hel = 0.0;
+    if (beta(i) == beta(a) && beta(j) == beta(b)) hel = umat_el(s, spat(i), spat(j), spat(a), spat(b));
+    if (beta(i) == beta(b) && beta(j) == beta(a)) hel -= umat_el(s, spat(i), spat(j), spat(b), spat(a));
+    return hel;
+}
+// sltcnd_0_base (sltcnd.fpp:585-622) + ECore, same summation order as NECI.
+__device__ inline double sltcnd_0(const DevSys &s, const uint8_t *nI, int nel) {
+    double hel_sing = 0.0;
+    for (int i = 0; i < nel; ++i) hel_sing += tmat_el(s, nI[i], nI[i]);
+    double hel_doub = 0.0;
+    for (int i = 0; i < nel - 1; ++i) {
+        double t = 0.0;
+        for (int j = i + 1; j < nel; ++j) t += umat_el(s, spat(nI[i]), spat(nI[j]), spat(nI[i]), spat(nI[j]));
+        hel_doub += t;
+    }
+    double hel_tmp = 0.0;
+    for (int i = 0; i < nel - 1; ++i)
+        for (int j = i + 1; j < nel; ++j)
+            if (beta(nI[i]) == beta(nI[j])) hel_tmp -= umat_el(s, spat(nI[i]), spat(nI[j]), spat(nI[j]), spat(nI[i]));
+    return hel_doub + hel_tmp + hel_sing;
+}
+
+__device__ inline double diag_helement(const DevSys &s, const unsigned long long *d) {
+    if (s.system == NECI_SYS_HUBBARD_REAL_SPACE) {
+        // U * number of doubly occupied sites: beta bit 2k and alpha bit 2k+1.
+        int n = 0;
+        for (int w = 0; w < s.W; ++w) n += __popcll(d[w] & (d[w] >> 1) & 0x5555555555555555ull);
+        return s.uhub * n;
+    }
+    uint8_t nI[kMaxNel];
+    const int nel = decode(d, s.W, nI);
+    return sltcnd_0(s, nI, nel) + s.ecore;
+}
+
+// <D_a|H|D_b> for a != b, given the excitation level.
+__device__ inline double offdiag_helement(const DevSys &s, const unsigned long long *a, const unsigned long long *b, int ic) {
+    if (ic == 1) {
+        int src = 0, tgt = 0;
+        for (int w = 0; w < s.W; ++w) {
+            const unsigned long long x = a[w] & ~b[w], y = b[w] & ~a[w];
+            if (x) src = w * 64 + __ffsll((long long)x);
+            if (y) tgt = w * 64 + __ffsll((long long)y);
+        }
+        const int lo = src < tgt ? src : tgt, hi = src < tgt ? tgt : src;
+        const bool par = occ_between(a, s.W, lo, hi) & 1;
+        double hel = (s.system == NECI_SYS_HUBBARD_REAL_SPACE) ? tmat_el(s, src, tgt) : sltcnd_1(s, a, src, tgt);
+        return par ? -hel : hel;
+    }
+    if (ic == 2 && s.system == NECI_SYS_MOLECULAR) {
+        int src[2], tgt[2], ns = 0, nt = 0;
+        for (int w = 0; w < s.W; ++w) {
+            unsigned long long x = a[w] & ~b[w], y = b[w] & ~a[w];
+            while (x) { src[ns++] = w * 64 + __ffsll((long long)x); x &= x - 1; }
+            while (y) { tgt[nt++] = w * 64 + __ffsll((long long)y); y &= y - 1; }
+        }
+        // parity of i->a then j->b (sorted pairing), as successive singles
+        unsigned long long t[kMaxWords];
+        for (int w = 0; w < s.W; ++w) t[w] = a[w];
+        int lo = min(src[0], tgt[0]), hi = max(src[0], tgt[0]);
+        int np = occ_between(t, s.W, lo, hi);
+        flip_orb(t, src[0]);
+        flip_orb(t, tgt[0]);
+        lo = min(src[1], tgt[1]);
+        hi = max(src[1], tgt[1]);
+        np += occ_between(t, s.W, lo, hi);
+        const double hel = sltcnd_2(s, src[0], src[1], tgt[0], tgt[1]);
+        return (np & 1) ? -hel : hel;
+    }
+    return 0.0;
+}
+
+}  // namespace neci

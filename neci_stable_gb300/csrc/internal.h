@@ -1,0 +1,80 @@
+// internal.h -- host-side engine object shared by the C ABI and the launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/neci_gpu.h"
+#include "engine.cuh"
+
+namespace neci {
+
+enum KernelId {
+    K_REHASH = 0,
+    K_BEGIN,
+    K_SWEEP,
+    K_SPAWN,
+    K_CORE,
+    K_ANN_PROBE,
+    K_ANN_COMPRESS,
+    K_ANN_INSERT,
+    K_MERGE_STATS,
+    K_FINAL,
+    K_NUM
+};
+
+struct Engine {
+    neci_gpu_system desc{};
+    DevSys sys{};
+    DevState st{};
+    int device = 0;
+    int num_sms = 152;
+    cudaStream_t stream = nullptr;
+    IterParams *d_params = nullptr;
+    IterParams *h_params = nullptr;          // pinned
+    neci_gpu_iter_stats *d_stats = nullptr;  // per-step records
+    neci_gpu_iter_stats *h_stats = nullptr;  // pinned
+    int max_stats = 0;
+    std::vector<void *> allocs;
+    bool have_ref = false, have_pchb = false;
+    // CUDA graph of one step (stats into d_stats[0])
+    cudaGraphExec_t graph = nullptr;
+    bool graph_core = false;
+    // profiling
+    bool profiling = false;
+    cudaEvent_t ev[2 * K_NUM] = {};
+    double kernel_ms[K_NUM] = {};
+    long long kernel_launches[K_NUM] = {};
+};
+
+// launchers (kernels.cu)
+void launch_begin(Engine &e, cudaStream_t s);
+void launch_rehash(Engine &e, cudaStream_t s);
+void launch_sweep(Engine &e, cudaStream_t s);
+void launch_spawn(Engine &e, cudaStream_t s);
+void launch_core(Engine &e, cudaStream_t s);
+void launch_ann_probe(Engine &e, cudaStream_t s);
+void launch_ann_compress(Engine &e, cudaStream_t s);
+void launch_ann_insert(Engine &e, cudaStream_t s);
+void launch_merge_stats(Engine &e, cudaStream_t s, int with_core);
+void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter);
+
+// utility launchers (util_kernels.cu)
+void launch_util_hash(Engine &e, const long long *dets, long long n, unsigned long long len, long long *out);
+void launch_util_excit_level(Engine &e, const long long *a, const long long *b, long long n, int *out);
+void launch_util_helement(Engine &e, const long long *a, const long long *b, long long n, double *out);
+void launch_util_gen_excit(Engine &e, const long long *det, long long n, unsigned long long seed, long long iter,
+                           long long *child, double *pgen, double *hel);
+void launch_upload_fix(Engine &e, long long nrows, int compute_diag);
+void launch_collect_holes(Engine &e);
+void launch_convert_spawns(Engine &e, long long n);
+void launch_all_cand(Engine &e);
+void launch_compress_out(Engine &e, long long *out, unsigned long long *n_out);
+void launch_core_mark(Engine &e, const long long *core_dets, long long n_core);
+void launch_core_count(Engine &e, const long long *core_dets, long long n_core, long long *counts);
+void launch_core_fill(Engine &e, const long long *core_dets, long long n_core);
+void launch_pchb_build(Engine &e);
+
+}  // namespace neci

@@ -1,0 +1,912 @@
+// kernels.cu -- the kernels of one FCIQMC iteration (PerformFCIMCycPar,
+// FciMCPar.F90:1177-1920) and the batch utility kernels of the C ABI.
+//
+// Iteration pipeline (all grid-stride, fixed grids, so one iteration is a
+// capturable CUDA graph; counts live in device memory):
+//   k_begin        reset per-step counters; rebuild the walker hash if its
+//                  tombstone load is high
+//   k_sweep        loop_over_determinants (:1294-1758) minus the spawn
+//                  attempts: free slots, initiator flags (CalcParentFlag),
+//                  E_proj sums (SumEContrib), number of spawns
+//                  (decide_num_to_spawn) emitted as work chunks, core
+//                  vector gather, and the death step
+//                  (perform_death_all_walkers / walker_death)
+//   k_spawn        the spawn attempts (generate_excitation, attempt_create,
+//                  create_particle): one thread per chunk of <= kChunk
+//                  attempts of one parent
+//   k_core         determ_projection_no_death (semi_stoch_procs.F90:290)
+//   k_ann_probe    annihilation pass 1: look every spawn up in the walker
+//                  hash (hash_table_lookup, hash.F90:294); spawns onto
+//                  present determinants are summed into per-slot fixed-
+//                  point accumulators, the rest become candidates
+//   k_ann_compress pass 2 (CompressSpawnedList, Annihilation.F90:249):
+//                  candidates are merged per determinant in a second
+//                  open-addressing table keyed on the spawn records
+//   k_ann_insert   pass 3 (AnnihilateSpawnedParts not-found branch,
+//                  :1191-1290): initiator abort, stochRoundSpawn,
+//                  diagonal elements, AddNewHashDet
+//   k_merge_stats  deterministic_annihilation + AnnihilateSpawnedParts
+//                  found branch + CalcHashTableStats (load_balancer.fpp:646)
+//                  in one sweep over the slots
+//   k_final        collect estimators into the step's stats record
+#include <cstdio>
+
+#include "engine.cuh"
+#include "excitgen.cuh"
+#include "internal.h"
+
+namespace neci {
+
+// ---------------------------------------------------------------------------
+// Reduction helpers.
+// ---------------------------------------------------------------------------
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ inline unsigned long long warp_sum_u(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide sum of NV doubles into global atomics (one atomic per value per block).
+template <int NV>
+__device__ inline void block_add(double (&v)[NV], double *const (&dst)[NV]) {
+    __shared__ double red[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const double s = warp_sum(v[k]);
+        if (lane == 0) red[k][wid] = s;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = lane < nw ? red[k][lane] : 0.0;
+            s = warp_sum(s);
+            if (lane == 0 && s != 0.0) atomicAdd(dst[k], s);
+        }
+    }
+    __syncthreads();
+}
+
+template <int NV>
+__device__ inline void block_add_u(unsigned long long (&v)[NV], unsigned long long *const (&dst)[NV]) {
+    __shared__ unsigned long long red[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const unsigned long long s = warp_sum_u(v[k]);
+        if (lane == 0) red[k][wid] = s;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            unsigned long long s = lane < nw ? red[k][lane] : 0ull;
+            s = warp_sum_u(s);
+            if (lane == 0 && s != 0ull) atomicAdd(dst[k], s);
+        }
+    }
+    __syncthreads();
+}
+
+// Warp-aggregated append of `want` items: returns this lane's first index.
+// Every lane of the warp must call it (all loops that use it run a
+// warp-uniform number of times).
+__device__ inline unsigned long long warp_append(unsigned long long *counter, unsigned int want) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned int incl = want;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const unsigned int total = __shfl_sync(0xffffffffu, incl, 31);
+    unsigned long long base = 0;
+    if (lane == 31 && total) base = atomicAdd(counter, (unsigned long long)total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + incl - want;
+}
+
+__device__ inline void set_err(Control *c, int code) { atomicCAS(&c->err, 0, code); }
+
+__device__ inline void load_rh2(const DevSys &s, int32_t *sh) {
+    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh[i] = s.random_hash2[i];
+    __syncthreads();
+}
+
+// Remove slot j from the walker hash (RemoveHashDet, load_balancer.fpp:631).
+__device__ inline void hash_remove(const DevState &st, long long j) {
+    const uint32_t b = st.slot_bucket[j];
+    st.hash[b] = kTomb;
+    atomicAdd(&st.ctl->n_tomb, 1ull);
+}
+
+// Look a determinant up: returns slot or -1.
+__device__ inline long long hash_find(const DevState &st, const unsigned long long *d, int W, int R,
+                                      unsigned long long h, Control *ctl) {
+    const unsigned long long mask = st.hash_n - 1;
+    unsigned long long b = hash_mod(h, st.hash_n);
+    for (int p = 0; p < kProbeLimit; ++p) {
+        const uint32_t e = st.hash[b];
+        if (e == kEmpty) return -1;
+        if (e != kTomb) {
+            const long long slot = (long long)e - 1;
+            if (det_eq(d, st.dets + slot * R, W)) return slot;
+        }
+        b = (b + 1) & mask;
+    }
+    set_err(ctl, NECI_GPU_ERR_HASH_FULL);
+    return -1;
+}
+
+// Insert a determinant known to be absent.
+__device__ inline void hash_insert(const DevState &st, long long slot, unsigned long long h, Control *ctl) {
+    const unsigned long long mask = st.hash_n - 1;
+    unsigned long long b = hash_mod(h, st.hash_n);
+    for (int p = 0; p < kProbeLimit; ++p) {
+        const uint32_t e = st.hash[b];
+        if (e == kEmpty || e == kTomb) {
+            if (atomicCAS(&st.hash[b], e, (uint32_t)(slot + 1)) == e) {
+                st.slot_bucket[slot] = (uint32_t)b;
+                if (e == kTomb) atomicAdd(&ctl->n_tomb, ~0ull);  // -1
+                return;
+            }
+            continue;  // lost the race for this bucket: look at it again
+        }
+        b = (b + 1) & mask;
+    }
+    set_err(ctl, NECI_GPU_ERR_HASH_FULL);
+}
+
+// TestInitiator_explicit (fcimc_helper.F90:1142-1240) without ADI, senior
+// initiators or an initiator space.
+__device__ inline bool test_initiator(const IterParams &p, bool was, double sgn, bool is_ref, bool core) {
+    const bool popInit = fabs(sgn) > p.initiator_walk_no;
+    if (!was) return popInit;
+    if (!is_ref && !(core && p.t_core_inits) && !popInit) return false;
+    return true;
+}
+
+// ===========================================================================
+// k_begin: per-step reset (single thread) and optional rehash.
+// ===========================================================================
+__global__ void k_begin(DevState st) {
+    Control *c = st.ctl;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        c->n_free = 0; c->free_taken = 0; c->n_chunks = 0; c->n_spawned = 0; c->n_cand = 0;
+        c->n_reps = 0; c->n_new = 0; c->n_attempts = 0; c->n_occupied = 0; c->n_holes = 0; c->n_found = 0;
+        for (int k = 0; k < 2; ++k) {
+            c->abs_q[k] = 0; c->abs_s[k] = 0;
+            c->nborn[k] = c->ndied[k] = c->nannihil[k] = c->naborted[k] = c->nremoved[k] = 0.0;
+            c->tot_parts[k] = c->tot_parts_old[k] = c->noat_hf[k] = c->hf_cyc[k] = c->enum_cyc[k] = c->norm[k] = 0.0;
+        }
+        c->err = 0;
+        c->rehash = 0;
+    }
+}
+
+// Rehash: clear every bucket, then reinsert live slots (run only when the
+// tombstone share is high; the flag is decided on the host from n_tomb).
+__global__ void k_hash_clear(DevState st) {
+    if (!st.ctl->rehash) return;
+    for (unsigned long long b = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; b < st.hash_n;
+         b += (unsigned long long)gridDim.x * blockDim.x)
+        st.hash[b] = kEmpty;
+    if (blockIdx.x == 0 && threadIdx.x == 0) st.ctl->n_tomb = 0;
+}
+__global__ void k_hash_fill(DevSys s, DevState st) {
+    if (!st.ctl->rehash) return;
+    extern __shared__ int32_t sh_rh2[];
+    load_rh2(s, sh_rh2);
+    const long long n = (long long)st.ctl->tot_walkers;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        const long long *r = st.dets + j * s.R;
+        bool occ = is_core_flags(r[s.W + s.L]);
+        for (int k = 0; k < s.L; ++k) occ = occ || fabs(word_to_double(r[s.W + k])) >= kEps12;
+        if (!occ) continue;
+        unsigned long long d[kMaxWords];
+        for (int w = 0; w < s.W; ++w) d[w] = (unsigned long long)r[w];
+        hash_insert(st, j, neci_hash(d, s.W, sh_rh2), st.ctl);
+    }
+}
+
+// ===========================================================================
+// k_sweep
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const IterParams *pp) {
+    const IterParams p = *pp;
+    Control *c = st.ctl;
+    const long long n = (long long)c->tot_walkers;
+    const int W = s.W, L = s.L, R = s.R;
+    double acc_old[2] = {0.0, 0.0}, acc_hf[2] = {0.0, 0.0}, acc_en[2] = {0.0, 0.0};
+    double acc_died[2] = {0.0, 0.0}, acc_born[2] = {0.0, 0.0}, acc_ab[2] = {0.0, 0.0};
+    unsigned long long acc_att = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;  // all lanes iterate together
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nround; j += stride) {
+        bool live = j < n;
+        long long *r = st.dets + (live ? j : 0) * R;
+        unsigned long long d[kMaxWords];
+        double C[2] = {0.0, 0.0};
+        long long flags = 0;
+        bool core = false, occ = false;
+        if (live) {
+            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
+            for (int k = 0; k < L; ++k) C[k] = word_to_double(r[W + k]);
+            flags = r[W + L];
+            core = st.n_core > 0 && is_core_flags(flags);
+            for (int k = 0; k < L; ++k) {
+                acc_old[k] += fabs(C[k]);
+                if (fabs(C[k]) >= kEps12) occ = true;
+            }
+            if (core) {
+                const int ci = st.core_of_slot[j];
+                for (int k = 0; k < L; ++k) st.core_x[(long long)ci * L + k] = C[k];
+            }
+        }
+        // holes go to the free list (FciMCPar.F90:1415-1427)
+        const bool hole = live && !occ && !core;
+        unsigned int nsp[2] = {0, 0};
+        bool neg[2] = {false, false};
+        if (live && occ) {
+            const int exl = excit_level(s.ilut_ref, d, W);
+            const bool is_ref = exl == 0;
+            if (p.t_trunc_initiator) {
+                long long nf = flags;
+                for (int k = 0; k < L; ++k) {
+                    const int b = init_flag_bit(k);
+                    const bool now = test_initiator(p, test_bit(flags, b), C[k], is_ref, core);
+                    if (now) nf |= (1ll << b); else nf &= ~(1ll << b);
+                }
+                if (nf != flags) { r[W + L] = nf; flags = nf; }
+            }
+            const double odh = st.offdiagH[j];
+            for (int k = 0; k < L; ++k) {
+                if (is_ref) acc_hf[k] += C[k];
+                acc_en[k] += odh * C[k];
+            }
+            const unsigned long long dkey = det_key(d, W, p.seed);
+            for (int k = 0; k < L; ++k) {
+                // decide_num_to_spawn (fcimc_helper.F90:2160-2174)
+                Stream rs(dkey, p.iter, P_NSPAWN, k, 0);
+                const double pa = C[k] * p.av_mc_excits;
+                int ns = abs((int)pa);
+                if (fabs(fabs(pa) - (double)ns) > kEps12) {
+                    const double pe = fabs(pa) - (double)ns;
+                    if (pe > rs.next()) ++ns;
+                }
+                nsp[k] = ns;
+                neg[k] = C[k] < 0.0;
+                acc_att += ns;
+            }
+            // walker_death + attempt_die_normal (fcimc_helper.F90:2279-2407,
+            // fcimc_pointed_fns.F90:573-705)
+            Stream rd(dkey, p.iter, P_DEATH, 0, 0);
+            const double Kii = st.diagH[j];
+            double cp[2] = {0.0, 0.0};
+            bool any = false;
+            for (int k = 0; k < L; ++k) {
+                const double fac = p.tau * (Kii - p.diag_sft[k]);
+                if (fac > 2.0) set_err(c, NECI_GPU_ERR_UNSTABLE);
+                double idie;
+                if (p.t_all_real_coeff) {
+                    idie = fac * fabs(C[k]);
+                } else {
+                    double rat = fac * fabs(C[k]);
+                    idie = trunc(rat);
+                    rat -= idie;
+                    if (fabs(rat) > rd.next()) idie += nearbyint(fsign(1.0, rat));
+                }
+                acc_died[k] += fmin(idie, fabs(C[k]));
+                acc_born[k] += fmax(idie - fabs(C[k]), 0.0);
+                cp[k] = C[k] - idie * fsign(1.0, C[k]);
+                if (fabs(cp[k]) > kEps12) any = true;
+            }
+            if (p.t_trunc_initiator && any) {
+                for (int k = 0; k < L; ++k)
+                    if ((cp[k] > 0.0) != (C[k] > 0.0)) { acc_ab[k] += fabs(cp[k]); cp[k] = 0.0; }
+                any = false;
+                for (int k = 0; k < L; ++k) if (fabs(cp[k]) > kEps12) any = true;
+            }
+            if (any || core) {
+                for (int k = 0; k < L; ++k) r[W + k] = double_to_word(cp[k]);
+            } else {
+                hash_remove(st, j);
+                r[W + L] = flags | 1ll;  // flag_removed
+                for (int k = 0; k < L; ++k) r[W + k] = double_to_word(0.0);
+            }
+        }
+        const bool freed = live && occ && !core && word_to_double(r[W]) == 0.0 &&
+                           (L == 1 || word_to_double(r[W + 1]) == 0.0);
+        // append free slots
+        {
+            const unsigned int want = (hole || freed) ? 1u : 0u;
+            const unsigned long long pos = warp_append(&c->n_free, want);
+            if (want) st.free_list[pos] = (int32_t)j;
+        }
+        // spawn work chunks
+        {
+            unsigned int nch = 0;
+            for (int k = 0; k < L; ++k) nch += (nsp[k] + kChunk - 1) / kChunk;
+            const unsigned long long base = warp_append(&c->n_chunks, nch);
+            if (nch) {
+                if (base + nch > (unsigned long long)st.max_chunks) {
+                    set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+                } else {
+                    unsigned long long q = base;
+                    for (int k = 0; k < L; ++k) {
+                        for (unsigned int k0 = 0; k0 < nsp[k]; k0 += kChunk) {
+                            const unsigned int cnt = min((unsigned int)kChunk, nsp[k] - k0);
+                            st.chunks[2 * q] = (unsigned long long)j | ((unsigned long long)k << 32) |
+                                               ((unsigned long long)neg[k] << 33) | ((unsigned long long)cnt << 34);
+                            st.chunks[2 * q + 1] = k0;
+                            ++q;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    double v[14] = {acc_old[0], acc_old[1], acc_hf[0], acc_hf[1], acc_en[0], acc_en[1], acc_died[0], acc_died[1],
+                    acc_born[0], acc_born[1], acc_ab[0], acc_ab[1], 0.0, 0.0};
+    double *const dst[14] = {&c->tot_parts_old[0], &c->tot_parts_old[1], &c->hf_cyc[0], &c->hf_cyc[1],
+                             &c->enum_cyc[0], &c->enum_cyc[1], &c->ndied[0], &c->ndied[1],
+                             &c->nborn[0], &c->nborn[1], &c->naborted[0], &c->naborted[1],
+                             &c->norm[0], &c->norm[1]};
+    block_add<14>(v, dst);
+    unsigned long long u[1] = {acc_att};
+    unsigned long long *const du[1] = {&c->n_attempts};
+    block_add_u<1>(u, du);
+}
+
+// ===========================================================================
+// k_spawn
+// ===========================================================================
+__global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const IterParams *pp) {
+    extern __shared__ int32_t sh[];
+    int32_t *sh_rh2 = sh;
+    int32_t *sh_neigh = sh + (s.nbasis + 1);
+    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
+    if (s.system == NECI_SYS_HUBBARD_REAL_SPACE)
+        for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
+    __syncthreads();
+    const IterParams p = *pp;
+    Control *c = st.ctl;
+    const long long nch = (long long)c->n_chunks;
+    const int W = s.W, L = s.L, R = s.R;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((nch + stride - 1) / stride) * stride;
+    int ovf = 0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
+        long long wout[kChunk];
+        int nout = 0;
+        unsigned long long kids[kChunk][kMaxWords];
+        int run = 0;
+        bool pinit = false;
+        if (q < nch) {
+            const unsigned long long w0 = st.chunks[2 * q];
+            const unsigned long long k0 = st.chunks[2 * q + 1];
+            const long long j = (long long)(w0 & 0xFFFFFFFFull);
+            run = (int)((w0 >> 32) & 1ull);
+            const bool neg = (w0 >> 33) & 1ull;
+            const int cnt = (int)(w0 >> 34);
+            const long long *r = st.dets + j * R;
+            unsigned long long d[kMaxWords];
+            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
+            const long long flags = r[W + L];
+            const bool core = st.n_core > 0 && is_core_flags(flags);
+            pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(run));
+            uint8_t nI[kMaxNel];
+            decode(d, W, nI);
+            const unsigned long long dkey = det_key(d, W, p.seed);
+            const double walkerweight = neg ? -1.0 : 1.0;
+            for (int a = 0; a < cnt; ++a) {
+                Stream rng(dkey, p.iter, P_ATTEMPT, run, (uint32_t)(k0 + a));
+                Excit e;
+                generate_excitation(s, d, nI, sh_neigh, rng, e);
+                if (!e.ok) continue;
+                if (core) {
+                    // is_core_state (semi_stoch_procs.F90:547): core -> core spawns
+                    // are done by the deterministic projection
+                    const long long hs = hash_find(st, e.child, W, R, neci_hash(e.child, W, sh_rh2), c);
+                    if (hs >= 0 && is_core_flags(st.dets[hs * R + W + L])) continue;
+                }
+                // attempt_create_normal (fcimc_pointed_fns.F90:178-494)
+                const double prob = e.pgen * p.av_mc_excits;
+                double nsp;
+                if (p.precision == NECI_PREC_MIXED) {
+                    const float t = (float)p.tau, h = (float)e.hel, ww = (float)walkerweight, pr = (float)prob;
+                    nsp = (double)(-t * h * ww / pr);
+                } else {
+                    nsp = -p.tau * e.hel * walkerweight / prob;
+                }
+                if (p.t_all_real_coeff) {
+                    if (p.t_real_spawn_cutoff && fabs(nsp) < p.real_spawn_cutoff) {
+                        const double x = nsp / p.real_spawn_cutoff;
+                        double i = trunc(x);
+                        const double res = x - i;
+                        if (fabs(res) >= kEps12)
+                            if (fabs(res) > rng.next()) i += nearbyint(fsign(1.0, x));
+                        nsp = p.real_spawn_cutoff * i;
+                    }
+                } else {
+                    double i = trunc(nsp);
+                    const double res = nsp - i;
+                    if (fabs(res) >= kEps12)
+                        if (fabs(res) > rng.next()) i += nearbyint(fsign(1.0, nsp));
+                    nsp = i;
+                }
+                if (fabs(nsp) < kEps12) continue;
+                wout[nout] = to_fixed(nsp, &ovf);
+                for (int w = 0; w < W; ++w) kids[nout][w] = e.child[w];
+                ++nout;
+            }
+        }
+        // create_particle (fcimc_helper.F90:152-308): append the records
+        const unsigned long long base = warp_append(&c->n_spawned, (unsigned int)nout);
+        for (int k = 0; k < nout; ++k) {
+            const unsigned long long pos = base + k;
+            if (pos >= (unsigned long long)st.max_spawned) { set_err(c, NECI_GPU_ERR_SPAWN_FULL); break; }
+            long long *o = st.spawn + pos * R;
+            for (int w = 0; w < W; ++w) o[w] = (long long)kids[k][w];
+            for (int k2 = 0; k2 < L; ++k2) o[W + k2] = (k2 == run) ? wout[k] : 0ll;
+            o[W + L] = pinit ? (1ll << init_flag_bit(run)) : 0ll;
+        }
+    }
+    if (ovf) set_err(c, NECI_GPU_ERR_OVERFLOW);
+}
+
+// ===========================================================================
+// k_core: y = -tau * H_offdiag x  (FP64, or FP32 values with compensated
+// FP32 hi/lo accumulation and an FP64 final sum)
+// ===========================================================================
+__global__ void k_core(DevSys s, DevState st, const IterParams *pp) {
+    const int L = s.L;
+    const double tau = pp->tau;
+    const bool mixed = pp->precision == NECI_PREC_MIXED;
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = warp; i < st.n_core; i += nwarps) {
+        const long long e0 = st.core_rowptr[i], e1 = st.core_rowptr[i + 1];
+        for (int k = 0; k < L; ++k) {
+            double acc = 0.0;
+            if (!mixed) {
+                for (long long e = e0 + lane; e < e1; e += 32)
+                    acc -= st.core_val[e] * st.core_x[(long long)st.core_col[e] * L + k];
+                acc = warp_sum(acc);
+            } else {
+                float hi = 0.0f, lo = 0.0f;  // Kahan-Babuska (TwoSum) accumulation
+                for (long long e = e0 + lane; e < e1; e += 32) {
+                    const float term = -(st.core_val32[e] * (float)st.core_x[(long long)st.core_col[e] * L + k]);
+                    const float t = hi + term;
+                    if (fabsf(hi) >= fabsf(term)) lo += (hi - t) + term; else lo += (term - t) + hi;
+                    hi = t;
+                }
+                acc = warp_sum((double)hi + (double)lo);
+            }
+            if (lane == 0) st.core_y[i * L + k] = acc * tau;
+        }
+    }
+}
+
+// ===========================================================================
+// Annihilation pass 1: probe the walker hash with every spawn record.
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
+    extern __shared__ int32_t sh_rh2[];
+    load_rh2(s, sh_rh2);
+    Control *c = st.ctl;
+    const long long n = (long long)min(c->n_spawned, (unsigned long long)st.max_spawned);
+    const int W = s.W, L = s.L, R = s.R;
+    unsigned long long aq[2] = {0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nround; i += stride) {
+        bool cand = false;
+        unsigned long long h = 0;
+        if (i < n) {
+            const long long *rec = st.spawn + i * R;
+            unsigned long long d[kMaxWords];
+            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)rec[w];
+            long long q[2] = {0, 0};
+            for (int k = 0; k < L; ++k) {
+                q[k] = rec[W + k];
+                aq[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
+            }
+            const long long fl = rec[W + L];
+            h = neci_hash(d, W, sh_rh2);
+            const long long slot = hash_find(st, d, W, R, h, c);
+            if (slot >= 0) {
+                for (int k = 0; k < L; ++k) {
+                    if (q[k] == 0) continue;
+                    atomicAdd((unsigned long long *)&st.acc[slot * L + k], (unsigned long long)q[k]);
+                    const uint32_t add = 1u;
+                    atomicAdd(&st.meta[slot * L + k], add);
+                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&st.meta[slot * L + k], 0x80000000u);
+                }
+            } else {
+                cand = true;
+            }
+        }
+        const unsigned long long pos = warp_append(&c->n_cand, cand ? 1u : 0u);
+        if (cand) {
+            st.cand[pos] = (uint32_t)i;
+            st.cand_h[pos] = h;
+        }
+    }
+    unsigned long long *const dst[2] = {&c->abs_q[0], &c->abs_q[1]};
+    block_add_u<2>(aq, dst);
+}
+
+// ===========================================================================
+// Annihilation pass 2: merge candidates per determinant.
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
+    Control *c = st.ctl;
+    const long long n = (long long)c->n_cand;
+    const int W = s.W, L = s.L, R = s.R;
+    const unsigned long long mask = st.spawn_hash_n - 1;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;
+    for (long long ci = blockIdx.x * (long long)blockDim.x + threadIdx.x; ci < nround; ci += stride) {
+        bool won = false;
+        uint32_t won_bucket = 0;
+        if (ci < n) {
+            const long long i = st.cand[ci];
+            const long long *rec = st.spawn + i * R;
+            unsigned long long d[kMaxWords];
+            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)rec[w];
+            unsigned long long b = splitmix64(st.cand_h[ci]) & mask;
+            long long owner = -1;
+            for (int p = 0; p < kProbeLimit; ++p) {
+                const uint32_t e = atomicCAS(&st.spawn_hash[b], kEmpty, (uint32_t)(ci + 1));
+                if (e == kEmpty) { owner = ci; won = true; won_bucket = (uint32_t)b; break; }
+                const long long other = (long long)e - 1;
+                if (det_eq(d, st.spawn + (long long)st.cand[other] * R, W)) { owner = other; break; }
+                b = (b + 1) & mask;
+            }
+            if (owner < 0) {
+                set_err(c, NECI_GPU_ERR_HASH_FULL);
+            } else {
+                const long long fl = rec[W + L];
+                atomicAdd(&st.rep_cnt[owner * (L + 1) + L], 1u);  // records in the block
+                for (int k = 0; k < L; ++k) {
+                    const long long q = rec[W + k];
+                    if (q == 0) continue;
+                    atomicAdd((unsigned long long *)&st.rep_q[owner * L + k], (unsigned long long)q);
+                    atomicAdd(&st.rep_cnt[owner * (L + 1) + k], 1u);
+                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&st.rep_cnt[owner * (L + 1) + k], 0x80000000u);
+                }
+            }
+        }
+        const unsigned long long pos = warp_append(&c->n_reps, won ? 1u : 0u);
+        if (won) {
+            st.reps[pos] = (uint32_t)ci;
+            st.rep_bucket[pos] = won_bucket;
+        }
+    }
+}
+
+// ===========================================================================
+// Annihilation pass 3: unique new determinants -> CurrentDets.
+// ===========================================================================
+__global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const IterParams *pp) {
+    const IterParams p = *pp;
+    Control *c = st.ctl;
+    const long long n = (long long)c->n_reps;
+    const int W = s.W, L = s.L, R = s.R;
+    double a_ab[2] = {0, 0}, a_rm[2] = {0, 0}, a_born[2] = {0, 0};
+    unsigned long long a_s[2] = {0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;
+    for (long long ri = blockIdx.x * (long long)blockDim.x + threadIdx.x; ri < nround; ri += stride) {
+        bool inserted = false;
+        if (ri < n) {
+            const long long ci = st.reps[ri];
+            st.spawn_hash[st.rep_bucket[ri]] = kEmpty;  // leave the table clean
+            const long long i = st.cand[ci];
+            const long long *rec = st.spawn + i * R;
+            unsigned long long d[kMaxWords];
+            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)rec[w];
+            long long q[2] = {0, 0};
+            uint32_t cnt[2] = {0, 0};
+            for (int k = 0; k < L; ++k) {
+                q[k] = st.rep_q[ci * L + k];
+                cnt[k] = st.rep_cnt[ci * (L + 1) + k];
+                st.rep_q[ci * L + k] = 0;
+                st.rep_cnt[ci * (L + 1) + k] = 0;
+            }
+            const uint32_t nrec = st.rep_cnt[ci * (L + 1) + L];
+            st.rep_cnt[ci * (L + 1) + L] = 0;
+            // compressed flags (CompressSpawnedList / FindResidualParticle)
+            long long flags;
+            if (nrec == 1) {
+                flags = rec[W + L];
+            } else {
+                flags = 0;
+                if (p.t_trunc_initiator)
+                    for (int k = 0; k < L; ++k) {
+                        const bool coh = p.t_init_coherent_rule && (cnt[k] & 0x7FFFFFFFu) >= 2u;
+                        if (coh || (cnt[k] & 0x80000000u)) flags |= 1ll << init_flag_bit(k);
+                    }
+            }
+            bool zero = true;
+            for (int k = 0; k < L; ++k) {
+                if (q[k] != 0) zero = false;
+                a_s[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
+            }
+            if (!zero) {
+                double ss[2] = {from_fixed(q[0]), from_fixed(q[1])};
+                if (p.t_trunc_initiator)
+                    for (int k = 0; k < L; ++k)
+                        if (!test_bit(flags, init_flag_bit(k))) { a_ab[k] += fabs(ss[k]); ss[k] = 0.0; }
+                bool unocc = true;
+                for (int k = 0; k < L; ++k) if (fabs(ss[k]) >= kEps12) unocc = false;
+                if (!unocc) {
+                    const unsigned long long dkey = det_key(d, W, p.seed);
+                    for (int k = 0; k < L; ++k) {
+                        // stochRoundSpawn (Annihilation.F90:1354-1418)
+                        const double a = fabs(ss[k]);
+                        if (a > kEps12 && a < p.occupied_thresh) {
+                            Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
+                            const double pRemove = 1.0 - a / p.occupied_thresh;
+                            if (pRemove > rng.next()) { a_rm[k] += a; ss[k] = 0.0; }
+                            else { a_born[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
+                        }
+                    }
+                    unocc = true;
+                    for (int k = 0; k < L; ++k) if (fabs(ss[k]) >= kEps12) unocc = false;
+                }
+                if (!unocc) {
+                    // AddNewHashDet (load_balancer.fpp:514-629)
+                    long long slot;
+                    const unsigned long long t = atomicAdd(&c->free_taken, 1ull);
+                    if (t < c->n_free) {
+                        slot = st.free_list[t];
+                    } else {
+                        slot = (long long)atomicAdd(&c->tot_walkers, 1ull);
+                    }
+                    if (slot + 1 >= st.max_walkers) {
+                        set_err(c, NECI_GPU_ERR_LIST_FULL);
+                    } else {
+                        long long *o = st.dets + slot * R;
+                        for (int w = 0; w < W; ++w) o[w] = (long long)d[w];
+                        for (int k = 0; k < L; ++k) o[W + k] = double_to_word(ss[k]);
+                        o[W + L] = flags & ~1ll;
+                        st.diagH[slot] = diag_helement(s, d) - s.hii;
+                        const int ic = excit_level(s.ilut_ref, d, W);
+                        st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
+                        if (st.n_core > 0) st.core_of_slot[slot] = -1;
+                        hash_insert(st, slot, st.cand_h[ci], c);
+                        inserted = true;
+                    }
+                }
+            }
+        }
+        const unsigned long long unused = warp_append(&c->n_new, inserted ? 1u : 0u);
+        (void)unused;
+    }
+    double v[6] = {a_ab[0], a_ab[1], a_rm[0], a_rm[1], a_born[0], a_born[1]};
+    double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
+                            &c->nborn[0], &c->nborn[1]};
+    block_add<6>(v, dst);
+    unsigned long long *const du[2] = {&c->abs_s[0], &c->abs_s[1]};
+    block_add_u<2>(a_s, du);
+}
+
+// ===========================================================================
+// k_merge_stats: deterministic annihilation, found-branch merge and
+// CalcHashTableStats in one sweep.
+// ===========================================================================
+__global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core) {
+    const IterParams p = *pp;
+    Control *c = st.ctl;
+    const long long n = (long long)min(c->tot_walkers, (unsigned long long)st.max_walkers);
+    const int W = s.W, L = s.L, R = s.R;
+    double a_born[2] = {0, 0}, a_ann[2] = {0, 0}, a_ab[2] = {0, 0}, a_rm[2] = {0, 0};
+    double a_tp[2] = {0, 0}, a_norm[2] = {0, 0};
+    unsigned long long a_s[2] = {0, 0}, a_occ = 0, a_holes = 0, a_found = 0;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        long long *r = st.dets + j * R;
+        const long long flags = r[W + L];
+        const bool core = st.n_core > 0 && is_core_flags(flags);
+        double C[2] = {0.0, 0.0};
+        for (int k = 0; k < L; ++k) C[k] = word_to_double(r[W + k]);
+        bool changed = false;
+        // deterministic_annihilation (Annihilation.F90:930-963)
+        if (core && with_core) {
+            const int ci = st.core_of_slot[j];
+            for (int k = 0; k < L; ++k) {
+                const double y = st.core_y[(long long)ci * L + k];
+                a_born[k] += fabs(y);
+                if (C[k] * y < 0.0) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(y));
+                C[k] = y + C[k];
+            }
+            changed = true;
+        }
+        // AnnihilateSpawnedParts, found branch (Annihilation.F90:1000-1140)
+        uint32_t m[2] = {0, 0};
+        bool has = false;
+        for (int k = 0; k < L; ++k) {
+            m[k] = st.meta[j * L + k];
+            if (m[k]) has = true;
+        }
+        if (has) {
+            ++a_found;
+            double S[2] = {0.0, 0.0};
+            for (int k = 0; k < L; ++k) {
+                const long long q = st.acc[j * L + k];
+                st.acc[j * L + k] = 0;
+                st.meta[j * L + k] = 0;
+                a_s[k] += (unsigned long long)(q < 0 ? -q : q);
+                S[k] = from_fixed(q);
+            }
+            for (int k = 0; k < L; ++k) {
+                if (fabs(C[k]) < kEps12 && p.t_trunc_initiator) {
+                    const bool sp_init = (m[k] & 0x80000000u) ||
+                                         (p.t_init_coherent_rule && (m[k] & 0x7FFFFFFFu) >= 2u);
+                    if (!sp_init && !core) { a_ab[k] += fabs(S[k]); S[k] = 0.0; }
+                }
+                if (C[k] * S[k] < 0.0) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(S[k]));
+            }
+            for (int k = 0; k < L; ++k) C[k] = S[k] + C[k];
+            changed = true;
+            if (!core) {
+                bool unocc = true;
+                for (int k = 0; k < L; ++k) if (fabs(C[k]) >= kEps12) unocc = false;
+                if (unocc) {
+                    hash_remove(st, j);
+                    r[W + L] = flags | 1ll;
+                }
+            }
+        }
+        // CalcHashTableStats (load_balancer.fpp:646-806)
+        bool occ = false;
+        for (int k = 0; k < L; ++k) if (fabs(C[k]) >= kEps12) occ = true;
+        if (!occ && !core) {
+            if (changed) for (int k = 0; k < L; ++k) r[W + k] = double_to_word(C[k]);
+            ++a_holes;
+            continue;
+        }
+        if (!core) {
+            for (int k = 0; k < L; ++k) {
+                const double a = fabs(C[k]);
+                if (a > kEps12 && a < p.occupied_thresh) {
+                    unsigned long long d[kMaxWords];
+                    for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
+                    Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
+                    const double pRemove = (p.occupied_thresh - a) / p.occupied_thresh;
+                    if (pRemove > rng.next()) {
+                        a_rm[k] += a;
+                        C[k] = 0.0;
+                        bool unocc = true;
+                        for (int k2 = 0; k2 < L; ++k2) if (fabs(C[k2]) >= kEps12) unocc = false;
+                        if (unocc) {
+                            hash_remove(st, j);
+                            r[W + L] = flags | 1ll;
+                        }
+                    } else {
+                        a_born[k] += p.occupied_thresh - a;
+                        C[k] = fsign(p.occupied_thresh, C[k]);
+                    }
+                    changed = true;
+                }
+            }
+        }
+        if (changed) for (int k = 0; k < L; ++k) r[W + k] = double_to_word(C[k]);
+        occ = false;
+        for (int k = 0; k < L; ++k) {
+            a_tp[k] += fabs(C[k]);
+            a_norm[k] += C[k] * C[k];
+            if (fabs(C[k]) >= kEps12) occ = true;
+        }
+        if (occ || core) {
+            ++a_occ;
+            bool is_ref = true;
+            for (int w = 0; w < W; ++w) if ((unsigned long long)r[w] != s.ilut_ref[w]) is_ref = false;
+            if (is_ref) for (int k = 0; k < L; ++k) c->noat_hf[k] = C[k];
+        } else {
+            ++a_holes;
+        }
+    }
+    double v[12] = {a_born[0], a_born[1], a_ann[0], a_ann[1], a_ab[0], a_ab[1], a_rm[0], a_rm[1],
+                    a_tp[0], a_tp[1], a_norm[0], a_norm[1]};
+    double *const dst[12] = {&c->nborn[0], &c->nborn[1], &c->nannihil[0], &c->nannihil[1],
+                             &c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
+                             &c->tot_parts[0], &c->tot_parts[1], &c->norm[0], &c->norm[1]};
+    block_add<12>(v, dst);
+    unsigned long long u[5] = {a_s[0], a_s[1], a_occ, a_holes, a_found};
+    unsigned long long *const du[5] = {&c->abs_s[0], &c->abs_s[1], &c->n_occupied, &c->n_holes, &c->n_found};
+    block_add_u<5>(u, du);
+}
+
+// ===========================================================================
+// k_final: write the step's stats record.
+// ===========================================================================
+__global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, int advance_iter, long long n_core) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    Control *c = st.ctl;
+    neci_gpu_iter_stats r;
+    for (int k = 0; k < 2; ++k) {
+        r.nborn[k] = c->nborn[k];
+        r.ndied[k] = c->ndied[k];
+        // compression annihilation: sum |q| - sum |sum q| over unique dets
+        const long long dq = (long long)(c->abs_q[k] - c->abs_s[k]);
+        r.nannihil[k] = c->nannihil[k] + (double)dq * 0x1.0p-32;
+        r.naborted[k] = c->naborted[k];
+        r.nremoved[k] = c->nremoved[k];
+        r.tot_parts[k] = c->tot_parts[k];
+        r.tot_parts_old[k] = c->tot_parts_old[k];
+        r.noat_hf[k] = c->noat_hf[k];
+        r.hf_cyc[k] = c->hf_cyc[k];
+        r.enum_cyc[k] = c->enum_cyc[k];
+        r.norm_psi_sq[k] = c->norm[k];
+    }
+    r.tot_walkers = (long long)c->tot_walkers;
+    r.n_occupied = (long long)c->n_occupied;
+    r.holes_in_list = (long long)c->n_holes;
+    r.n_attempts = (long long)c->n_attempts;
+    r.n_spawned = (long long)c->n_spawned;
+    r.n_unique = (long long)(c->n_reps + c->n_found);
+    r.n_new = (long long)c->n_new;
+    r.n_core = n_core;
+    r.err = c->err;
+    r.reserved = 0;
+    *out = r;
+    if (advance_iter) pp->iter += 1;
+    // rebuild the walker hash before the next step when live entries plus
+    // tombstones pass 70% of the buckets
+    c->rehash = (c->n_occupied + c->n_tomb) * 10ull > st.hash_n * 7ull ? 1 : 0;
+}
+
+// ===========================================================================
+// Host-side launch helpers (declared in internal.h).
+// ===========================================================================
+static int grid_for(const Engine &e, int threads) {
+    (void)threads;
+    return e.num_sms * 4;
+}
+
+void launch_begin(Engine &e, cudaStream_t s) { k_begin<<<1, 32, 0, s>>>(e.st); }
+
+void launch_rehash(Engine &e, cudaStream_t s) {
+    k_hash_clear<<<grid_for(e, 256), 256, 0, s>>>(e.st);
+    k_hash_fill<<<grid_for(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
+}
+
+void launch_sweep(Engine &e, cudaStream_t s) {
+    k_sweep<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
+}
+void launch_spawn(Engine &e, cudaStream_t s) {
+    const size_t shm = (size_t)(e.sys.nbasis + 1 + e.sys.nsites * e.sys.max_neigh) * sizeof(int32_t);
+    k_spawn<<<e.num_sms * 8, 128, shm, s>>>(e.sys, e.st, e.d_params);
+}
+void launch_core(Engine &e, cudaStream_t s) {
+    if (e.st.n_core > 0) k_core<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
+}
+void launch_ann_probe(Engine &e, cudaStream_t s) {
+    k_ann_probe<<<grid_for(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
+}
+void launch_ann_compress(Engine &e, cudaStream_t s) {
+    k_ann_compress<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st);
+}
+void launch_ann_insert(Engine &e, cudaStream_t s) {
+    k_ann_insert<<<e.num_sms * 8, 128, 0, s>>>(e.sys, e.st, e.d_params);
+}
+void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
+    k_merge_stats<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params, with_core);
+}
+void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter) {
+    k_final<<<1, 32, 0, s>>>(e.st, out, e.d_params, advance_iter, e.st.n_core);
+}
+
+}  // namespace neci

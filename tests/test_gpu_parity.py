@@ -1,0 +1,189 @@
+"""GPU parity tests: every kernel against the CPU oracle through the C ABI.
+
+Integer/bit work (hashes, excitation levels, excitation generation, spawn
+compression, annihilation, whole iterations) must be bit-exact; matrix
+elements within 1e-12 relative (they are in fact bit-exact: the FP64
+kernels are built with --fmad=false and sum in the oracle's order).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from neci_stable_gb300 import capi
+from neci_stable_gb300.engine import Engine
+from oracle.oracle import Oracle
+
+from helpers import (canonical, canonical_with, excite, hubbard10, hubbard_square, molecule, random_dets,
+                     random_spawns, random_walkers)
+
+pytestmark = pytest.mark.gpu
+
+SYSTEMS = {
+    "hub10": lambda: hubbard10(),
+    "hub10x2": lambda: hubbard10(lenof_sign=2),
+    "hub6x6": lambda: hubbard_square(6, 6, 36),
+    "mol12": lambda: molecule(12, 6),
+    "mol24": lambda: molecule(24, 10),
+    "mol40": lambda: molecule(40, 12),      # 80 spin orbitals: two det words
+    "mol64": lambda: molecule(64, 20),      # 128 spin orbitals: three det words
+}
+
+_cache = {}
+
+
+def pair(name, max_walkers=200_000, max_spawned=400_000):
+    key = (name, max_walkers, max_spawned)
+    if key not in _cache:
+        spec = SYSTEMS[name]()
+        eng = Engine(spec, max_walkers, max_spawned)
+        orc = Oracle(spec, max_walkers, max_spawned, hii=eng.hii)
+        _cache.clear()
+        _cache[key] = (spec, eng, orc)
+    return _cache[key]
+
+
+@pytest.mark.parametrize("name", ["hub10", "hub6x6", "mol24", "mol40", "mol64"])
+def test_find_walker_hash_and_excit_level(name):
+    spec, eng, orc = pair(name)
+    rng = np.random.default_rng(1)
+    dets = random_dets(spec, 4000, rng)
+    for length in (1, 7, 1000003, 1 << 20, (1 << 31) - 1):
+        assert np.array_equal(eng.find_walker_hash(dets, length), orc.find_walker_hash(dets, length))
+    other = random_dets(spec, 4000, rng)
+    assert np.array_equal(eng.excit_level(dets, other), orc.excit_level(dets, other))
+
+
+@pytest.mark.parametrize("name", ["hub10", "hub6x6", "mol12", "mol24", "mol40", "mol64"])
+def test_helement(name):
+    spec, eng, orc = pair(name)
+    rng = np.random.default_rng(2)
+    a = random_dets(spec, 600, rng)
+    b = np.array([excite(spec, d, lvl, rng) for d, lvl in zip(a, rng.integers(0, 4, size=a.shape[0]))])
+    b[:50] = a[:50]
+    g = eng.helement(a, b)
+    c = orc.helement(a, b)
+    np.testing.assert_allclose(g, c, rtol=1e-12, atol=1e-14)
+    assert np.array_equal(g, c), "FP64 matrix elements are expected bit-exact"
+
+
+@pytest.mark.parametrize("name", ["hub10", "hub6x6", "mol12", "mol24", "mol40", "mol64"])
+def test_gen_excit(name):
+    spec, eng, orc = pair(name)
+    rng = np.random.default_rng(3)
+    for det in random_dets(spec, 6, rng):
+        for seed, it in ((7, 1), (123456789, 99)):
+            cg, pg, hg = eng.gen_excit(det, 3000, seed, it)
+            cc, pc, hc = orc.gen_excit(det, 3000, seed, it)
+            assert np.array_equal(cg, cc)
+            assert np.array_equal(pg, pc)
+            assert np.array_equal(hg, hc)
+
+
+@pytest.mark.parametrize("name", ["hub10", "hub10x2", "mol24"])
+def test_compress_spawns(name):
+    spec, eng, orc = pair(name)
+    rng = np.random.default_rng(4)
+    walkers = random_walkers(spec, 500, rng)
+    for n in (0, 1, 17, 5000, 60000):
+        sp = random_spawns(spec, walkers, n, rng)
+        out_g, nann_g = eng.compress_spawns(sp)
+        out_c, nann_c = orc.compress_spawns(capi.default_params(), sp)
+        assert np.array_equal(out_g, out_c)
+        np.testing.assert_allclose(nann_g, nann_c, rtol=1e-12, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", ["hub10", "hub10x2", "mol24", "mol40"])
+@pytest.mark.parametrize("trunc", [1, 0])
+def test_annihilate_injected(name, trunc):
+    spec, eng, orc = pair(name)
+    rng = np.random.default_rng(5 + trunc)
+    W = spec.W
+    walkers = random_walkers(spec, 3000, rng)
+    # some holes in the list (zero signs) to exercise free-slot reuse
+    holes = rng.random(walkers.shape[0]) < 0.1
+    walkers[holes, W:W + spec.lenof_sign] = 0
+    eng.upload(walkers)
+    orc.upload(walkers)
+    p = capi.default_params(seed=99, iter=3, t_trunc_initiator=trunc, occupied_thresh=1.0)
+    sp = random_spawns(spec, walkers, 20000, rng)
+    sg = eng.annihilate(p, sp)
+    sc, rc = orc.annihilate(p, sp)
+    assert rc == 0 and sg.err == 0
+    rg, dg, og = eng.download()
+    rcpu, dc, oc = orc.download()
+    rg, (dg, og) = canonical_with(rg, [dg, og], W)
+    rcpu, (dc, oc) = canonical_with(rcpu, [dc, oc], W)
+    assert rg.shape == rcpu.shape
+    # flag_removed (bit 0) bookkeeping is slot-local; compare the rest
+    assert np.array_equal(rg[:, : W + spec.lenof_sign], rcpu[:, : W + spec.lenof_sign])
+    assert np.array_equal(rg[:, -1] & ~1, rcpu[:, -1] & ~1)
+    assert np.array_equal(dg, dc) and np.array_equal(og, oc)
+    for f in ("nborn", "nannihil", "naborted", "nremoved", "tot_parts", "norm_psi_sq", "tot_parts_old"):
+        np.testing.assert_allclose(getattr(sg, f)[:], getattr(sc, f)[:], rtol=1e-10, atol=1e-8, err_msg=f)
+    assert sg.n_new == sc.n_new and sg.n_occupied == sc.n_occupied
+
+
+def run_pair(name, iters, start_pop, tau, shift=0.0, seed=31, precision=capi.PREC_FP64, real=1):
+    spec, eng, orc = pair(name, 400_000, 800_000)
+    eng.start_from_reference(initial_part=start_pop)
+    rows, _, _ = eng.download()
+    orc.upload(rows)
+    W, L = spec.W, spec.lenof_sign
+    for it in range(1, iters + 1):
+        p = capi.default_params(tau=tau, diag_sft=[shift, shift], seed=seed, iter=it, precision=precision,
+                                t_all_real_coeff=real)
+        sg = eng.perform_fcimc_cyc_par(p)
+        sc, rc = orc.iterate(p)
+        assert rc == 0 and sg.err == 0, (it, rc, sg.err)
+        rg = canonical(eng.download()[0], W)
+        rcpu = canonical(orc.download()[0], W)
+        assert rg.shape == rcpu.shape, (it, rg.shape, rcpu.shape)
+        assert np.array_equal(rg[:, : W + L], rcpu[:, : W + L]), it
+        assert np.array_equal(rg[:, -1] & ~1, rcpu[:, -1] & ~1), it
+        for f in ("nborn", "ndied", "nannihil", "naborted", "nremoved", "tot_parts", "hf_cyc", "enum_cyc",
+                  "tot_parts_old"):
+            np.testing.assert_allclose(getattr(sg, f)[:], getattr(sc, f)[:], rtol=1e-9, atol=1e-7, err_msg=f"{f} it {it}")
+        assert sg.n_attempts == sc.n_attempts and sg.n_spawned == sc.n_spawned and sg.n_new == sc.n_new
+    return sg
+
+
+@pytest.mark.parametrize("name,iters,pop,tau", [("hub10", 40, 50.0, 0.02), ("hub10x2", 25, 20.0, 0.02),
+                                                ("hub6x6", 12, 30.0, 0.01), ("mol12", 30, 40.0, 0.02),
+                                                ("mol24", 20, 200.0, 0.005)])
+def test_iterations_bit_exact(name, iters, pop, tau):
+    st = run_pair(name, iters, pop, tau)
+    assert st.n_occupied > 1
+
+
+def test_iterations_integer_walkers_and_mixed():
+    run_pair("hub10", 20, 30.0, 0.02, real=0)
+    run_pair("mol12", 15, 40.0, 0.02, precision=capi.PREC_MIXED)
+
+
+def test_iterate_n_matches_single_steps():
+    spec, eng, orc = pair("hub10", 100_000, 200_000)
+    eng.start_from_reference(initial_part=10.0)
+    p = capi.default_params(tau=0.02, seed=5, iter=1)
+    a = [eng.perform_fcimc_cyc_par(capi.default_params(tau=0.02, seed=5, iter=i)) for i in range(1, 11)]
+    ra = canonical(eng.download()[0], spec.W)
+    eng.start_from_reference(initial_part=10.0)
+    b = eng.iterate_n(p, 10)
+    rb = canonical(eng.download()[0], spec.W)
+    assert np.array_equal(ra, rb)
+    assert [s.tot_parts[0] for s in a] == [s.tot_parts[0] for s in b]
+
+
+def test_errors_are_reported_not_faulted():
+    """Buffer overflows come back as NECI's err codes (no fault, context usable)."""
+    spec = hubbard10()
+    eng = Engine(spec, max_walkers=64, max_spawned=32)
+    eng.start_from_reference(initial_part=500.0)
+    with pytest.raises(capi.NeciGpuError) as ei:
+        for it in range(1, 20):
+            eng.perform_fcimc_cyc_par(capi.default_params(tau=0.05, seed=1, iter=it))
+    assert ei.value.code in (capi.ERR_SPAWN_FULL, capi.ERR_LIST_FULL)
+    # the context still works after the error
+    eng.start_from_reference(initial_part=1.0)
+    st = eng.perform_fcimc_cyc_par(capi.default_params(tau=0.001, seed=1, iter=1))
+    assert st.err == 0
