@@ -66,8 +66,8 @@ void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
     d.iter = p.iter;
 }
 
-const char *kKernelNames[K_NUM] = {"rehash",      "begin",          "sweep",       "spawn",       "core",
-                                   "ann_probe",   "ann_compress",   "ann_insert",  "merge_stats", "final"};
+const char *kKernelNames[K_NUM] = {"rehash",    "begin",        "sweep",      "expand",      "spawn", "core",
+                                   "ann_probe", "ann_compress", "ann_insert", "merge_stats", "final"};
 
 // Launch one kernel stage, bracketed by events when profiling.
 template <typename F>
@@ -92,6 +92,7 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
     stage(e, K_BEGIN, [&] { launch_begin(e, e.stream); });
     stage(e, K_SWEEP, [&] { launch_sweep(e, e.stream); });
+    stage(e, K_EXPAND, [&] { launch_expand(e, e.stream); });
     stage(e, K_SPAWN, [&] { launch_spawn(e, e.stream); });
     if (e.st.n_core > 0) stage(e, K_CORE, [&] { launch_core(e, e.stream); });
     stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
@@ -189,6 +190,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     st.max_walkers = sys->max_walkers;
     st.max_spawned = sys->max_spawned;
     st.max_chunks = sys->max_walkers * s.L + sys->max_spawned + 1024;
+    st.max_big = st.max_chunks / kBigChunks + 1024;
     st.hash_n = next_pow2(std::max<unsigned long long>((unsigned long long)sys->n_walker_hashes,
                                                        2ull * (unsigned long long)sys->max_walkers));
     st.spawn_hash_n = next_pow2(2ull * (unsigned long long)sys->max_spawned);
@@ -205,6 +207,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.free_list, (size_t)st.max_walkers + 1);
     A(st.spawn, (size_t)st.max_spawned * s.R);
     A(st.chunks, (size_t)st.max_chunks * 2);
+    A(st.big, (size_t)st.max_big * 3);
     A(st.acc, (size_t)st.max_walkers * s.L);
     A(st.meta, (size_t)st.max_walkers * s.L);
     A(st.cand, (size_t)st.max_spawned);
@@ -273,8 +276,13 @@ int32_t neci_gpu_set_tmat(neci_gpu_ctx *ctx, const double *t) {
     const size_t n = (size_t)e.sys.nbasis * e.sys.nbasis;
     if (int r = dalloc(e, &d, n)) return r;
     CK(cudaMemcpyAsync(d, t, n * sizeof(double), cudaMemcpyHostToDevice, e.stream));
+    std::vector<float> t32(t, t + n);
+    float *d32 = nullptr;
+    if (int r = dalloc(e, &d32, n)) return r;
+    CK(cudaMemcpyAsync(d32, t32.data(), n * sizeof(float), cudaMemcpyHostToDevice, e.stream));
     CK(cudaStreamSynchronize(e.stream));
     e.sys.tmat = d;
+    e.sys.tmat32 = d32;
     if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
     return NECI_GPU_OK;
 }
@@ -288,8 +296,13 @@ int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *u, int64_t len) {
     double *d = nullptr;
     if (int r = dalloc(e, &d, (size_t)len)) return r;
     CK(cudaMemcpyAsync(d, u, (size_t)len * sizeof(double), cudaMemcpyHostToDevice, e.stream));
+    std::vector<float> u32(u, u + len);
+    float *d32 = nullptr;
+    if (int r = dalloc(e, &d32, (size_t)len)) return r;
+    CK(cudaMemcpyAsync(d32, u32.data(), (size_t)len * sizeof(float), cudaMemcpyHostToDevice, e.stream));
     CK(cudaStreamSynchronize(e.stream));
     e.sys.umat = d;
+    e.sys.umat32 = d32;
     if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
     return NECI_GPU_OK;
 }
@@ -328,6 +341,21 @@ int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii
     e.sys.nOccAlpha = na;
     e.sys.nOccBeta = nb;
     e.sys.hii = hii;
+    // hoisted constants of the generators (pick_biased_elecs pgen,
+    // excit_gens_int_weighted.F90:770-790; pDoubles = 1 - pSingles)
+    DevSys &s = e.sys;
+    const int par = na * (na - 1) / 2 + nb * (nb - 1) / 2;
+    s.pgen_par = s.p_parallel / (double)par;
+    s.pgen_opp = (1.0 - s.p_parallel) / (double)(na * nb);
+    s.p_doubles = 1.0 - s.p_singles;
+    s.p_elec = 1.0 / (double)s.nel;
+    s.thr_singles = prob_thresh(s.p_singles);
+    s.thr_bias = prob_thresh(s.p_parallel);
+    s.f_pgen_par = (float)s.p_parallel / (float)par;
+    s.f_pgen_opp = (1.0f - (float)s.p_parallel) / (float)(na * nb);
+    s.f_p_doubles = 1.0f - (float)s.p_singles;
+    s.f_p_singles = (float)s.p_singles;
+    s.f_p_elec = 1.0f / (float)s.nel;
     e.have_ref = true;
     if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
     return NECI_GPU_OK;
@@ -350,6 +378,16 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
     if (int r = dalloc(e, &present, ntab)) return r;
     if (int r = dalloc(e, &pexch, (size_t)s.ijMax)) return r;
     if (int r = dalloc(e, &tgt, (size_t)s.abMax + 1)) return r;
+    unsigned long long *athr, *pthr;
+    float *prob32, *pexch32;
+    if (int r = dalloc(e, &athr, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &prob32, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &pthr, (size_t)s.ijMax)) return r;
+    if (int r = dalloc(e, &pexch32, (size_t)s.ijMax)) return r;
+    s.alias_thr = athr;
+    s.alias_prob32 = prob32;
+    s.pexch_thr = pthr;
+    s.pexch32 = pexch32;
     std::vector<int32_t> tp(s.abMax + 1, 0);
     for (int a = 1; a <= s.nBI; ++a)
         for (int b = 1; b <= a; ++b) tp[(long long)b + (long long)a * (a - 1) / 2] = (b << 16) | a;

@@ -18,6 +18,7 @@ constexpr int kMaxWords = 4;      // nBasis <= 255 (NIfD <= 3)
 constexpr int kMaxNel = 64;
 constexpr int kMaxNeigh = 8;
 constexpr int kChunk = 16;        // spawn attempts per work item
+constexpr int kBigChunks = 64;    // parents with more chunks are expanded by k_expand
 constexpr int kProbeLimit = 1 << 16;
 constexpr uint32_t kEmpty = 0u;
 constexpr uint32_t kTomb = 0xFFFFFFFFu;
@@ -40,6 +41,7 @@ struct Control {
     unsigned long long n_holes;
     unsigned long long n_tomb;          // hash tombstones
     unsigned long long n_found;         // unique spawned determinants already present
+    unsigned long long n_big;           // parents expanded by k_expand
     unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
@@ -64,6 +66,14 @@ struct DevSys {
     const double *alias_prob;
     const uint8_t *alias_present;  // [(ij-1)*3 + type-1]
     const int32_t *tgt_pair;       // [abMax+1]: (small << 16) | large
+    // hoisted constants of the generators
+    double pgen_par, pgen_opp, p_doubles, p_elec;        // pBias/par, (1-pBias)/AB, 1-pSingles, 1/nel
+    unsigned long long thr_singles, thr_bias;           // prob_thresh(pSingles), prob_thresh(pParallel)
+    const unsigned long long *alias_thr;                 // prob_thresh(bias) of each alias entry
+    const unsigned long long *pexch_thr;                 // prob_thresh(pExch(ij))
+    // single-precision copies for the mixed-precision spawn amplitudes
+    float f_pgen_par, f_pgen_opp, f_p_doubles, f_p_singles, f_p_elec;
+    const float *umat32, *tmat32, *alias_prob32, *pexch32;
 };
 
 // Resident walker state (device pointers).
@@ -77,6 +87,8 @@ struct DevState {
     long long max_walkers, max_spawned, max_chunks;
     long long *spawn;              // spawn records
     unsigned long long *chunks;    // pairs: slot | run << 32 | neg << 33 | n << 34, first attempt
+    unsigned long long *big;       // triples: slot | run << 32 | neg << 33, attempts, first chunk
+    long long max_big;
     long long *acc;                // per slot*L fixed-point spawn sums (found determinants)
     uint32_t *meta;                // per slot*L spawn counts | initiator bit 31
     uint32_t *cand;                // record index of spawns onto absent determinants
@@ -142,10 +154,12 @@ __host__ __device__ inline unsigned long long det_key(const unsigned long long *
     return h;
 }
 
+// One stream of 64-bit draws for (determinant, iteration, purpose, run,
+// attempt).  Every draw consumes one 64-bit value; a Philox block gives two.
 struct Stream {
     uint32_t key[2];
     uint32_t ctr[4];
-    double buf[2];
+    unsigned long long buf[2];
     int have;
     __device__ inline Stream(unsigned long long dkey, long long iter, uint32_t purpose, uint32_t run, uint32_t attempt) {
         key[0] = (uint32_t)dkey;
@@ -156,22 +170,45 @@ struct Stream {
         ctr[3] = purpose | (run << 8) | ((uint32_t)((unsigned long long)iter >> 32) << 16);
         have = 0;
     }
-    __device__ inline double next() {
+    __device__ inline unsigned long long next64() {
         if (have == 0) {
             uint32_t o[4];
             philox_block(ctr, key, o);
             ctr[1] += 1;
-            const unsigned long long a = ((unsigned long long)o[1] << 32) | o[0];
-            const unsigned long long b = ((unsigned long long)o[3] << 32) | o[2];
-            buf[0] = (double)(a >> 11) * 0x1.0p-53;
-            buf[1] = (double)(b >> 11) * 0x1.0p-53;
+            buf[0] = ((unsigned long long)o[1] << 32) | o[0];
+            buf[1] = ((unsigned long long)o[3] << 32) | o[2];
             have = 2;
         }
-        const double v = (have == 2) ? buf[0] : buf[1];
+        const unsigned long long v = (have == 2) ? buf[0] : buf[1];
         --have;
         return v;
     }
+    // genrand_real2 equivalent: a double in [0, 1) from 53 bits
+    __device__ inline double next() { return (double)(next64() >> 11) * 0x1.0p-53; }
 };
+
+// Probability p as a 64-bit threshold: draw r < thresh(p)  <=>  r/2^64 < p.
+__host__ __device__ inline unsigned long long prob_thresh(double p) {
+    if (!(p > 0.0)) return 0ull;
+    if (p >= 1.0) return ~0ull;
+    return (unsigned long long)(p * 18446744073709551616.0);
+}
+// Bernoulli(p) from one draw (p >= 1 is always true).
+__device__ inline bool bern(Stream &r, double p) {
+    const unsigned long long x = r.next64();
+    return p >= 1.0 || x < prob_thresh(p);
+}
+// Bernoulli(p) for a float p from the top 32 bits of one draw.
+__device__ inline bool bern_f(Stream &r, float p) {
+    const unsigned int x = (unsigned int)(r.next64() >> 32);
+    if (p >= 1.0f) return true;
+    if (!(p > 0.0f)) return false;
+    return x < (unsigned int)(p * 4294967296.0f);
+}
+// Uniform integer in [0, n) (multiply-high of one draw).
+__device__ inline unsigned int uniform_index(Stream &r, unsigned int n) {
+    return (unsigned int)__umul64hi(r.next64(), (unsigned long long)n);
+}
 
 // ---------------------------------------------------------------------------
 // Fixed point and sign words.

@@ -1,40 +1,102 @@
 // excitgen.cuh -- device excitation generators (generate_excitation,
-// proc_ptrs.F90:13) in bit-string form.  Each consumes uniforms from one
-// Philox stream in the same order as NECI's routine consumes dSFMT draws.
+// proc_ptrs.F90:13) in bit-string form, templated on the precision of the
+// generation probability and matrix element (double: the FP64 path; float:
+// the mixed-precision spawn amplitudes).
+//
+// Random draws are consumed as 64-bit integers: int(n*r) becomes
+// uniform_index(n) (multiply-high), r < p becomes a threshold test; the
+// sampled distributions and the returned p_gen are those of NECI's routines,
+// with the constant divisions of p_gen hoisted out of the attempt.  GB300
+// executes FP64 at 1/64 of the FP32 rate, so the sampling itself carries no
+// FP64 arithmetic.
 #pragma once
 
 #include "engine.cuh"
 
 namespace neci {
 
+template <typename Real>
 struct Excit {
     unsigned long long child[kMaxWords];
-    double pgen;
-    double hel;
+    Real pgen;
+    Real hel;
     int ic;
     bool ok;
 };
 
+template <typename Real>
+__device__ inline Real tmat_r(const DevSys &s, int i, int j);
+template <>
+__device__ inline double tmat_r<double>(const DevSys &s, int i, int j) { return tmat_el(s, i, j); }
+template <>
+__device__ inline float tmat_r<float>(const DevSys &s, int i, int j) {
+    return __ldg(&s.tmat32[(size_t)(j - 1) * s.nbasis + (i - 1)]);
+}
+template <typename Real>
+__device__ inline Real umat_r(const DevSys &s, int i, int j, int k, int l);
+template <>
+__device__ inline double umat_r<double>(const DevSys &s, int i, int j, int k, int l) { return umat_el(s, i, j, k, l); }
+template <>
+__device__ inline float umat_r<float>(const DevSys &s, int i, int j, int k, int l) {
+    return __ldg(&s.umat32[umat_ind(i, j, k, l) - 1]);
+}
+
+// sltcnd_1_kernel (sltcnd.fpp:643-679) in precision Real.
+template <typename Real>
+__device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, int src, int tgt) {
+    Real hel = 0;
+    const int id1 = spat(src), id2 = spat(tgt);
+    if (beta(src) == beta(tgt)) {
+        for (int w = 0; w < s.W; ++w) {
+            unsigned long long x = d[w];
+            while (x) {
+                const int o = w * 64 + __ffsll((long long)x);
+                x &= x - 1;
+                if (o != src) hel += umat_r<Real>(s, id1, spat(o), id2, spat(o));
+            }
+        }
+        for (int w = 0; w < s.W; ++w) {
+            unsigned long long x = d[w];
+            while (x) {
+                const int o = w * 64 + __ffsll((long long)x);
+                x &= x - 1;
+                if (o != src && beta(o) == beta(src)) hel -= umat_r<Real>(s, id1, spat(o), spat(o), id2);
+            }
+        }
+    }
+    hel += tmat_r<Real>(s, src, tgt);
+    return hel;
+}
+// sltcnd_2_kernel (sltcnd.fpp:690-711), ex sorted: i<j, a<b.
+template <typename Real>
+__device__ inline Real sltcnd_2_r(const DevSys &s, int i, int j, int a, int b) {
+    Real hel = 0;
+    if (beta(i) == beta(a) && beta(j) == beta(b)) hel = umat_r<Real>(s, spat(i), spat(j), spat(a), spat(b));
+    if (beta(i) == beta(b) && beta(j) == beta(a)) hel -= umat_r<Real>(s, spat(i), spat(j), spat(b), spat(a));
+    return hel;
+}
+
 // Child determinant and H_ij of a single src -> tgt.
-__device__ inline void finish_single(const DevSys &s, const unsigned long long *d, int src, int tgt, Excit &e) {
+template <typename Real>
+__device__ inline void finish_single(const DevSys &s, const unsigned long long *d, int src, int tgt, Excit<Real> &e) {
     for (int w = 0; w < s.W; ++w) e.child[w] = d[w];
     flip_orb(e.child, src);
     flip_orb(e.child, tgt);
     const int lo = min(src, tgt), hi = max(src, tgt);
     const bool par = occ_between(d, s.W, lo, hi) & 1;  // make_single tParity
-    const double hel = (s.system == NECI_SYS_HUBBARD_REAL_SPACE) ? tmat_el(s, src, tgt) : sltcnd_1(s, d, src, tgt);
+    const Real hel = (s.system == NECI_SYS_HUBBARD_REAL_SPACE) ? tmat_r<Real>(s, src, tgt) : sltcnd_1_r<Real>(s, d, src, tgt);
     e.hel = par ? -hel : hel;
 }
 
 // gen_excit_rs_hubbard (real_space_hubbard.F90:1938-2030),
 // create_cum_list_rs_hubbard (:2080) and pick_from_cum_list
-// (lattice_models_utils.F90:150).
+// (lattice_models_utils.F90:150).  The cumulative pick stays in FP64.
+template <typename Real>
 __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                      const int32_t *neigh, Stream &rng, Excit &e) {
+                                      const int32_t *neigh, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
     e.ok = false;
-    const int elec = 1 + (int)(rng.next() * s.nel);
-    const double p_elec = 1.0 / (double)s.nel;
+    const int elec = 1 + (int)uniform_index(rng, (unsigned)s.nel);
     const int src = nI[elec - 1];
     const int site = spat(src);
     int orbs[kMaxNeigh];
@@ -52,22 +114,24 @@ __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long 
         cum[nn] = cum_sum;
         ++nn;
     }
-    if (cum_sum < 1e-10) { e.pgen = 0.0; return; }
+    if (cum_sum < 1e-10) { e.pgen = 0; return; }
     const double r = rng.next() * cum_sum;
     int ind = nn;
     for (int k = 0; k < nn; ++k)
         if (cum[k] >= r) { ind = k + 1; break; }
     const double p_orb = (ind == 1) ? cum[0] / cum_sum : (cum[ind - 1] - cum[ind - 2]) / cum_sum;
     const int orb = orbs[ind - 1];
-    e.pgen = p_elec * p_orb;
-    finish_single(s, d, src, orb, e);
+    e.pgen = (Real)(s.p_elec * p_orb);
+    finish_single<Real>(s, d, src, orb, e);
     e.ok = true;
 }
 
 // CreateSingleExcit (GenRandSymExcitNUMod.F90:1118-1243), C1 symmetry,
 // tCycleOrbs = .false. (rejection for the electron and for the hole).
+// Returns the full single pgen, pSingles / (NExcit * (nel - ElecsWNoExcits)).
+template <typename Real>
 __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                          Stream &rng, Excit &e) {
+                                          Stream &rng, Excit<Real> &e) {
     e.ic = 1;
     e.ok = false;
     const int norbs = s.nbasis / 2;
@@ -78,64 +142,69 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
     }
     const int nun_a = norbs - nalpha, nun_b = norbs - nbeta;
     const int elecs_wno = (nun_a == 0 ? nalpha : 0) + (nun_b == 0 ? nbeta : 0);
-    if (elecs_wno == s.nel) { e.pgen = 0.0; return; }
+    if (elecs_wno == s.nel) { e.pgen = 0; return; }
     int eleci = 0, ispn = 0, nexcit = 0;
     for (int attempts = 0; attempts <= 250; ++attempts) {
-        eleci = (int)(s.nel * rng.next()) + 1;
+        eleci = (int)uniform_index(rng, (unsigned)s.nel) + 1;
         ispn = beta(nI[eleci - 1]) ? 2 : 1;
         nexcit = (ispn == 1) ? nun_a : nun_b;
         if (nexcit != 0) break;
     }
-    if (nexcit == 0) { e.pgen = 0.0; return; }
+    if (nexcit == 0) { e.pgen = 0; return; }
     int orb = 0;
     bool found = false;
     for (int attempts = 0; attempts <= 250; ++attempts) {
-        const int chosen = (int)(norbs * rng.next());
+        const int chosen = (int)uniform_index(rng, (unsigned)norbs);
         orb = 2 * (chosen + 1) - (ispn - 1);
         if (!orb_occ(d, orb)) { found = true; break; }
     }
-    if (!found) { e.pgen = 0.0; return; }
-    e.pgen = 1.0 / (double)(nexcit * (s.nel - elecs_wno));
-    finish_single(s, d, nI[eleci - 1], orb, e);
+    if (!found) { e.pgen = 0; return; }
+    if (sizeof(Real) == 8) e.pgen = (Real)(s.p_singles / (double)(nexcit * (s.nel - elecs_wno)));
+    else e.pgen = (Real)(s.f_p_singles / (float)(nexcit * (s.nel - elecs_wno)));
+    finish_single<Real>(s, d, nI[eleci - 1], orb, e);
     e.ok = true;
+}
+
+// Position among the electrons of one spin of the pair with triangular
+// index idx (pick_biased_elecs' ceiling((1+sqrt(9+8 idx))/2), in integers):
+// returns a1 > a2 >= 1 with idx = (a1-1)(a1-2)/2 + a2 - 1.
+__device__ inline void tri_pair(int idx, int &a1, int &a2) {
+    int a = 2;
+    while (a * (a - 1) / 2 <= idx) ++a;
+    a1 = a;
+    a2 = idx + 1 - ((a - 1) * (a - 2)) / 2;
 }
 
 // GAS_doubles_PCHB_gen_exc (gasci_pchb_doubles_spatorb_fastweighted.fpp)
 // with UNIF_UNIF particles = pick_biased_elecs
-// (excit_gens_int_weighted.F90:722-830).
+// (excit_gens_int_weighted.F90:722-830).  Returns the full double pgen
+// (times pDoubles).
+template <typename Real>
 __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                       Stream &rng, Excit &e) {
+                                       Stream &rng, Excit<Real> &e) {
     e.ic = 2;
     e.ok = false;
+    const bool dbl = sizeof(Real) == 8;
     const int aa = s.nOccAlpha * (s.nOccAlpha - 1) / 2;
     const int bb = s.nOccBeta * (s.nOccBeta - 1) / 2;
-    const int par = aa + bb;
-    const int ab_pairs = s.nOccAlpha * s.nOccBeta;
-    const double pBias = s.p_parallel;
-    double r = rng.next();
     int al_req, be_req, al_num[2] = {0, 0}, be_num[2] = {0, 0};
-    double pgen;
-    if (r < pBias) {
-        r = (r / pBias) * par;
-        int idx = (int)floor(r);
+    Real pgen;
+    if (rng.next64() < s.thr_bias) {
+        int idx = (int)uniform_index(rng, (unsigned)(aa + bb));
         if (idx < aa) {
             al_req = 2; be_req = 0;
-            al_num[0] = (int)ceil((1.0 + sqrt(9.0 + 8.0 * (double)idx)) / 2.0);
-            al_num[1] = idx + 1 - ((al_num[0] - 1) * (al_num[0] - 2)) / 2;
+            tri_pair(idx, al_num[0], al_num[1]);
         } else {
             al_req = 0; be_req = 2;
-            idx -= aa;
-            be_num[0] = (int)ceil((1.0 + sqrt(9.0 + 8.0 * (double)idx)) / 2.0);
-            be_num[1] = idx + 1 - ((be_num[0] - 1) * (be_num[0] - 2)) / 2;
+            tri_pair(idx - aa, be_num[0], be_num[1]);
         }
-        pgen = pBias / (double)par;
+        pgen = dbl ? (Real)s.pgen_par : (Real)s.f_pgen_par;
     } else {
         al_req = 1; be_req = 1;
-        pgen = (1.0 - pBias) / (double)ab_pairs;
-        r = ((r - pBias) / (1.0 - pBias)) * ab_pairs;
-        const int idx = (int)floor(r);
+        const int idx = (int)uniform_index(rng, (unsigned)(s.nOccAlpha * s.nOccBeta));
         al_num[0] = 1 + idx % s.nOccAlpha;
-        be_num[0] = 1 + (int)floor(idx / (double)s.nOccAlpha);
+        be_num[0] = 1 + idx / s.nOccAlpha;
+        pgen = dbl ? (Real)s.pgen_opp : (Real)s.f_pgen_opp;
     }
     int elecs[2] = {0, 0}, found = 0, al_count = 0, be_count = 0;
     for (int i = 1; i <= s.nel; ++i) {
@@ -148,7 +217,7 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
         }
         if (al_req == 0 && be_req == 0) break;
     }
-    if (found < 2) { e.pgen = 0.0; return; }
+    if (found < 2) { e.pgen = 0; return; }
     const int src0 = nI[elecs[0] - 1], src1 = nI[elecs[1] - 1];
     const long long i1 = spat(src0), j1 = spat(src1);
     const long long ij = i1 < j1 ? i1 + j1 * (j1 - 1) / 2 : j1 + i1 * (i1 - 1) / 2;
@@ -157,30 +226,31 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     if (spin0 == spin1) {
         type = 1;
     } else {
-        const double pe = __ldg(&s.pexch[ij - 1]);
-        if (rng.next() < pe) {
+        const Real pe = dbl ? (Real)__ldg(&s.pexch[ij - 1]) : (Real)__ldg(&s.pexch32[ij - 1]);
+        if (rng.next64() < __ldg(&s.pexch_thr[ij - 1])) {
             type = 3;
             pgen *= pe;
             const int t = spin0; spin0 = spin1; spin1 = t;
         } else {
             type = 2;
-            pgen *= (1.0 - pe);
+            pgen *= ((Real)1 - pe);
         }
     }
-    // sample_AliasTable_t (aliasSampling.F90:310-331)
+    // sample_AliasTable_t (aliasSampling.F90:310-331): slot and fraction
+    // from the high and low halves of one 64x(abMax) product
     const size_t t = (size_t)(ij - 1) * 3 + (type - 1);
-    if (!__ldg(&s.alias_present[t])) { e.pgen = 0.0; return; }
-    const double ra = rng.next();
-    const int pos = (int)((double)s.abMax * ra) + 1;
-    const double bias = fmax((double)s.abMax * ra + 1.0 - pos, 0.0);
+    if (!__ldg(&s.alias_present[t])) { e.pgen = 0; return; }
+    const unsigned long long r = rng.next64();
+    const unsigned long long n = (unsigned long long)s.abMax;
+    const unsigned long long pos0 = __umul64hi(r, n);
+    const unsigned long long frac = r * n;
     const size_t base = t * (size_t)s.abMax;
-    int ab;
-    if (bias < __ldg(&s.alias_bias[base + pos - 1])) ab = pos;
-    else ab = __ldg(&s.alias_alias[base + pos - 1]);
-    const double pholes = __ldg(&s.alias_prob[base + ab - 1]);
+    const unsigned long long thr = __ldg(&s.alias_thr[base + pos0]);
+    const int ab = (frac < thr || thr == ~0ull) ? (int)pos0 + 1 : __ldg(&s.alias_alias[base + pos0]);
+    const Real pholes = dbl ? (Real)__ldg(&s.alias_prob[base + ab - 1]) : (Real)__ldg(&s.alias_prob32[base + ab - 1]);
     const int tp = __ldg(&s.tgt_pair[ab]);
     const int o0 = 2 * (tp >> 16) - spin0, o1 = 2 * (tp & 0xFFFF) - spin1;
-    if (o0 == 0 || o1 == 0 || orb_occ(d, o0) || orb_occ(d, o1) || fabs(pholes) < 1e-10) { e.pgen = 0.0; return; }
+    if (o0 == 0 || o1 == 0 || orb_occ(d, o0) || orb_occ(d, o1) || !(pholes > (Real)1e-10)) { e.pgen = 0; return; }
     const int ta = min(o0, o1), tb = max(o0, o1);
     for (int w = 0; w < s.W; ++w) e.child[w] = d[w];
     // parity of src0 -> ta then src1 -> tb (make_double pairing)
@@ -190,26 +260,23 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     np += occ_between(e.child, s.W, min(src1, tb), max(src1, tb));
     flip_orb(e.child, src1);
     flip_orb(e.child, tb);
-    const double hel = sltcnd_2(s, src0, src1, ta, tb);
+    const Real hel = sltcnd_2_r<Real>(s, src0, src1, ta, tb);
     e.hel = (np & 1) ? -hel : hel;
-    e.pgen = pgen * pholes;
+    pgen *= pholes;
+    e.pgen = pgen * (dbl ? (Real)s.p_doubles : (Real)s.f_p_doubles);
     e.ok = true;
 }
 
 // gen_exc_sd (excitation_generators.F90:110-133): singles with pSingles.
+template <typename Real>
 __device__ inline void generate_excitation(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                           const int32_t *neigh, Stream &rng, Excit &e) {
+                                           const int32_t *neigh, Stream &rng, Excit<Real> &e) {
     if (s.excitgen == NECI_EXGEN_RS_HUBBARD) {
-        gen_rs_hubbard(s, d, nI, neigh, rng, e);
+        gen_rs_hubbard<Real>(s, d, nI, neigh, rng, e);
         return;
     }
-    if (rng.next() < s.p_singles) {
-        gen_uniform_single(s, d, nI, rng, e);
-        e.pgen *= s.p_singles;
-    } else {
-        gen_pchb_double(s, d, nI, rng, e);
-        e.pgen *= (1.0 - s.p_singles);
-    }
+    if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, nI, rng, e);
+    else gen_pchb_double<Real>(s, d, nI, rng, e);
 }
 
 }  // namespace neci

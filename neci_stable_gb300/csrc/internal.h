@@ -15,6 +15,7 @@ enum KernelId {
     K_REHASH = 0,
     K_BEGIN,
     K_SWEEP,
+    K_EXPAND,
     K_SPAWN,
     K_CORE,
     K_ANN_PROBE,
@@ -53,6 +54,7 @@ struct Engine {
 void launch_begin(Engine &e, cudaStream_t s);
 void launch_rehash(Engine &e, cudaStream_t s);
 void launch_sweep(Engine &e, cudaStream_t s);
+void launch_expand(Engine &e, cudaStream_t s);
 void launch_spawn(Engine &e, cudaStream_t s);
 void launch_core(Engine &e, cudaStream_t s);
 void launch_ann_probe(Engine &e, cudaStream_t s);

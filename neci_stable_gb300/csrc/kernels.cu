@@ -183,6 +183,7 @@ __global__ void k_begin(DevState st) {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         c->n_free = 0; c->free_taken = 0; c->n_chunks = 0; c->n_spawned = 0; c->n_cand = 0;
         c->n_reps = 0; c->n_new = 0; c->n_attempts = 0; c->n_occupied = 0; c->n_holes = 0; c->n_found = 0;
+        c->n_big = 0;
         for (int k = 0; k < 2; ++k) {
             c->abs_q[k] = 0; c->abs_s[k] = 0;
             c->nborn[k] = c->ndied[k] = c->nannihil[k] = c->naborted[k] = c->nremoved[k] = 0.0;
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 int ns = abs((int)pa);
                 if (fabs(fabs(pa) - (double)ns) > kEps12) {
                     const double pe = fabs(pa) - (double)ns;
-                    if (pe > rs.next()) ++ns;
+                    if (bern(rs, pe)) ++ns;
                 }
                 nsp[k] = ns;
                 neg[k] = C[k] < 0.0;
@@ -303,7 +304,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                     double rat = fac * fabs(C[k]);
                     idie = trunc(rat);
                     rat -= idie;
-                    if (fabs(rat) > rd.next()) idie += nearbyint(fsign(1.0, rat));
+                    if (bern(rd, fabs(rat))) idie += nearbyint(fsign(1.0, rat));
                 }
                 acc_died[k] += fmin(idie, fabs(C[k]));
                 acc_born[k] += fmax(idie - fabs(C[k]), 0.0);
@@ -332,7 +333,8 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             const unsigned long long pos = warp_append(&c->n_free, want);
             if (want) st.free_list[pos] = (int32_t)j;
         }
-        // spawn work chunks
+        // spawn work chunks; a parent with more than kBigChunks chunks is handed
+        // to k_expand, which writes its chunks with a whole block
         {
             unsigned int nch = 0;
             for (int k = 0; k < L; ++k) nch += (nsp[k] + kChunk - 1) / kChunk;
@@ -343,10 +345,24 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 } else {
                     unsigned long long q = base;
                     for (int k = 0; k < L; ++k) {
+                        const unsigned int nk = (nsp[k] + kChunk - 1) / kChunk;
+                        const unsigned long long head = (unsigned long long)j | ((unsigned long long)k << 32) |
+                                                        ((unsigned long long)neg[k] << 33);
+                        if (nk > (unsigned int)kBigChunks) {
+                            const unsigned long long b = atomicAdd(&c->n_big, 1ull);
+                            if (b < (unsigned long long)st.max_big) {
+                                st.big[3 * b] = head;
+                                st.big[3 * b + 1] = nsp[k];
+                                st.big[3 * b + 2] = q;
+                            } else {
+                                set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+                            }
+                            q += nk;
+                            continue;
+                        }
                         for (unsigned int k0 = 0; k0 < nsp[k]; k0 += kChunk) {
                             const unsigned int cnt = min((unsigned int)kChunk, nsp[k] - k0);
-                            st.chunks[2 * q] = (unsigned long long)j | ((unsigned long long)k << 32) |
-                                               ((unsigned long long)neg[k] << 33) | ((unsigned long long)cnt << 34);
+                            st.chunks[2 * q] = head | ((unsigned long long)cnt << 34);
                             st.chunks[2 * q + 1] = k0;
                             ++q;
                         }
@@ -368,17 +384,67 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
 }
 
 // ===========================================================================
+// k_expand: chunks of heavily populated parents, one block per parent.
+// ===========================================================================
+__global__ void k_expand(DevState st) {
+    const unsigned long long nb = min(st.ctl->n_big, (unsigned long long)st.max_big);
+    for (unsigned long long b = blockIdx.x; b < nb; b += gridDim.x) {
+        const unsigned long long head = st.big[3 * b];
+        const unsigned long long n = st.big[3 * b + 1];
+        const unsigned long long base = st.big[3 * b + 2];
+        const unsigned long long nk = (n + kChunk - 1) / kChunk;
+        for (unsigned long long q = threadIdx.x; q < nk; q += blockDim.x) {
+            const unsigned long long k0 = q * kChunk;
+            const unsigned long long cnt = min((unsigned long long)kChunk, n - k0);
+            st.chunks[2 * (base + q)] = head | (cnt << 34);
+            st.chunks[2 * (base + q) + 1] = k0;
+        }
+    }
+}
+
+// ===========================================================================
 // k_spawn
 // ===========================================================================
-__global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const IterParams *pp) {
-    extern __shared__ int32_t sh[];
-    int32_t *sh_rh2 = sh;
-    int32_t *sh_neigh = sh + (s.nbasis + 1);
-    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
-    if (s.system == NECI_SYS_HUBBARD_REAL_SPACE)
-        for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
-    __syncthreads();
-    const IterParams p = *pp;
+// attempt_create_normal (fcimc_pointed_fns.F90:178-494) for one generated
+// excitation: the child amplitude -tau H_ij sign(C) / (p_gen AvMCExcits),
+// rounded by RealSpawnCutoff / stochastic_round, in fixed point (0 = none).
+template <typename Real>
+__device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real pgen, bool neg, Stream &rng, int &ovf) {
+    const Real ww = neg ? (Real)-1 : (Real)1;
+    const Real prob = pgen * (Real)p.av_mc_excits;
+    Real nsp = -(Real)p.tau * hel * ww / prob;
+    const Real eps = (Real)kEps12;
+    if (p.t_all_real_coeff) {
+        const Real cut = (Real)p.real_spawn_cutoff;
+        if (p.t_real_spawn_cutoff && fabs(nsp) < cut) {
+            const Real x = nsp * ((Real)1 / cut);
+            Real i = trunc(x);
+            const Real res = x - i;
+            if (fabs(res) >= eps) {
+                const bool up = (sizeof(Real) == 8) ? bern(rng, (double)fabs(res)) : bern_f(rng, (float)fabs(res));
+                if (up) i += (x >= (Real)0 ? (Real)1 : (Real)-1);
+            }
+            nsp = cut * i;
+        }
+    } else {
+        Real i = trunc(nsp);
+        const Real res = nsp - i;
+        if (fabs(res) >= eps) {
+            const bool up = (sizeof(Real) == 8) ? bern(rng, (double)fabs(res)) : bern_f(rng, (float)fabs(res));
+            if (up) i += (nsp >= (Real)0 ? (Real)1 : (Real)-1);
+        }
+        nsp = i;
+    }
+    if (!(fabs(nsp) >= eps)) return 0;
+    if (sizeof(Real) == 8) return to_fixed((double)nsp, &ovf);
+    const float sc = (float)nsp * 4294967296.0f;
+    if (!(fabsf(sc) < 9.2e18f)) { ovf = 1; return 0; }
+    return __float2ll_rn(sc);
+}
+
+template <typename Real>
+__device__ inline void spawn_chunks(const DevSys &s, const DevState &st, const IterParams &p, const int32_t *sh_rh2,
+                                    const int32_t *sh_neigh) {
     Control *c = st.ctl;
     const long long nch = (long long)c->n_chunks;
     const int W = s.W, L = s.L, R = s.R;
@@ -407,11 +473,10 @@ __global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const Iter
             uint8_t nI[kMaxNel];
             decode(d, W, nI);
             const unsigned long long dkey = det_key(d, W, p.seed);
-            const double walkerweight = neg ? -1.0 : 1.0;
             for (int a = 0; a < cnt; ++a) {
                 Stream rng(dkey, p.iter, P_ATTEMPT, run, (uint32_t)(k0 + a));
-                Excit e;
-                generate_excitation(s, d, nI, sh_neigh, rng, e);
+                Excit<Real> e;
+                generate_excitation<Real>(s, d, nI, sh_neigh, rng, e);
                 if (!e.ok) continue;
                 if (core) {
                     // is_core_state (semi_stoch_procs.F90:547): core -> core spawns
@@ -419,33 +484,9 @@ __global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const Iter
                     const long long hs = hash_find(st, e.child, W, R, neci_hash(e.child, W, sh_rh2), c);
                     if (hs >= 0 && is_core_flags(st.dets[hs * R + W + L])) continue;
                 }
-                // attempt_create_normal (fcimc_pointed_fns.F90:178-494)
-                const double prob = e.pgen * p.av_mc_excits;
-                double nsp;
-                if (p.precision == NECI_PREC_MIXED) {
-                    const float t = (float)p.tau, h = (float)e.hel, ww = (float)walkerweight, pr = (float)prob;
-                    nsp = (double)(-t * h * ww / pr);
-                } else {
-                    nsp = -p.tau * e.hel * walkerweight / prob;
-                }
-                if (p.t_all_real_coeff) {
-                    if (p.t_real_spawn_cutoff && fabs(nsp) < p.real_spawn_cutoff) {
-                        const double x = nsp / p.real_spawn_cutoff;
-                        double i = trunc(x);
-                        const double res = x - i;
-                        if (fabs(res) >= kEps12)
-                            if (fabs(res) > rng.next()) i += nearbyint(fsign(1.0, x));
-                        nsp = p.real_spawn_cutoff * i;
-                    }
-                } else {
-                    double i = trunc(nsp);
-                    const double res = nsp - i;
-                    if (fabs(res) >= kEps12)
-                        if (fabs(res) > rng.next()) i += nearbyint(fsign(1.0, nsp));
-                    nsp = i;
-                }
-                if (fabs(nsp) < kEps12) continue;
-                wout[nout] = to_fixed(nsp, &ovf);
+                const long long qv = spawn_amplitude<Real>(p, e.hel, e.pgen, neg, rng, ovf);
+                if (qv == 0) continue;
+                wout[nout] = qv;
                 for (int w = 0; w < W; ++w) kids[nout][w] = e.child[w];
                 ++nout;
             }
@@ -462,6 +503,19 @@ __global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const Iter
         }
     }
     if (ovf) set_err(c, NECI_GPU_ERR_OVERFLOW);
+}
+
+__global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const IterParams *pp) {
+    extern __shared__ int32_t sh[];
+    int32_t *sh_rh2 = sh;
+    int32_t *sh_neigh = sh + (s.nbasis + 1);
+    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
+    if (s.system == NECI_SYS_HUBBARD_REAL_SPACE)
+        for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
+    __syncthreads();
+    const IterParams p = *pp;
+    if (p.precision == NECI_PREC_MIXED) spawn_chunks<float>(s, st, p, sh_rh2, sh_neigh);
+    else spawn_chunks<double>(s, st, p, sh_rh2, sh_neigh);
 }
 
 // ===========================================================================
@@ -659,7 +713,7 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
                         if (a > kEps12 && a < p.occupied_thresh) {
                             Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
                             const double pRemove = 1.0 - a / p.occupied_thresh;
-                            if (pRemove > rng.next()) { a_rm[k] += a; ss[k] = 0.0; }
+                            if (bern(rng, pRemove)) { a_rm[k] += a; ss[k] = 0.0; }
                             else { a_born[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
                         }
                     }
@@ -785,7 +839,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                     for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
                     Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
                     const double pRemove = (p.occupied_thresh - a) / p.occupied_thresh;
-                    if (pRemove > rng.next()) {
+                    if (bern(rng, pRemove)) {
                         a_rm[k] += a;
                         C[k] = 0.0;
                         bool unocc = true;
@@ -886,6 +940,7 @@ void launch_rehash(Engine &e, cudaStream_t s) {
 void launch_sweep(Engine &e, cudaStream_t s) {
     k_sweep<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
+void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<e.num_sms * 2, 256, 0, s>>>(e.st); }
 void launch_spawn(Engine &e, cudaStream_t s) {
     const size_t shm = (size_t)(e.sys.nbasis + 1 + e.sys.nsites * e.sys.max_neigh) * sizeof(int32_t);
     k_spawn<<<e.num_sms * 8, 128, shm, s>>>(e.sys, e.st, e.d_params);

@@ -41,8 +41,8 @@ __global__ void k_util_gen_excit(DevSys s, const long long *det, long long n, un
     const unsigned long long dkey = det_key(d, s.W, seed);
     for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < n; a += (long long)gridDim.x * blockDim.x) {
         Stream rng(dkey, iter, P_ATTEMPT, 0, (uint32_t)a);
-        Excit e;
-        generate_excitation(s, d, nI, s.neighbours, rng, e);
+        Excit<double> e;
+        generate_excitation<double>(s, d, nI, s.neighbours, rng, e);
         for (int w = 0; w < s.W; ++w) child[a * s.W + w] = e.ok ? (long long)e.child[w] : 0ll;
         pgen[a] = e.ok ? e.pgen : 0.0;
         hel[a] = e.ok ? e.hel : 0.0;
@@ -303,10 +303,20 @@ __global__ void k_pchb_tables(DevSys s, double *bias, int32_t *alias, double *pr
         for (long long k = 0; k < n; ++k) w[k] = w[k] / sum;
     }
 }
-__global__ void k_pchb_pexch(DevSys s, const double *wsum, double *pexch) {
+__global__ void k_pchb_pexch(DevSys s, const double *wsum, double *pexch, unsigned long long *pexch_thr, float *pexch32) {
     for (long long ij = blockIdx.x * (long long)blockDim.x + threadIdx.x; ij < s.ijMax; ij += (long long)gridDim.x * blockDim.x) {
         const double ex = wsum[ij * 3 + 2], noex = wsum[ij * 3 + 1];
-        pexch[ij] = fabs(ex + noex) < 1e-10 ? 0.0 : ex / (ex + noex);
+        const double pe = fabs(ex + noex) < 1e-10 ? 0.0 : ex / (ex + noex);
+        pexch[ij] = pe;
+        pexch_thr[ij] = prob_thresh(pe);
+        pexch32[ij] = (float)pe;
+    }
+}
+// Integer thresholds of the alias biases and single-precision probabilities.
+__global__ void k_pchb_derived(long long n, const double *bias, const double *prob, unsigned long long *thr, float *prob32) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        thr[i] = prob_thresh(bias[i]);
+        prob32[i] = (float)prob[i];
     }
 }
 
@@ -362,7 +372,10 @@ void launch_pchb_build(Engine &e) {
     k_pchb_tables<<<blocks, threads, 0, e.stream>>>(e.sys, (double *)e.sys.alias_bias, (int32_t *)e.sys.alias_alias,
                                                     (double *)e.sys.alias_prob, (uint8_t *)e.sys.alias_present, wsum,
                                                     scratch);
-    k_pchb_pexch<<<gsz(e), 256, 0, e.stream>>>(e.sys, wsum, (double *)e.sys.pexch);
+    k_pchb_pexch<<<gsz(e), 256, 0, e.stream>>>(e.sys, wsum, (double *)e.sys.pexch,
+                                               (unsigned long long *)e.sys.pexch_thr, (float *)e.sys.pexch32);
+    k_pchb_derived<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, e.sys.alias_bias, e.sys.alias_prob,
+                                                 (unsigned long long *)e.sys.alias_thr, (float *)e.sys.alias_prob32);
     cudaStreamSynchronize(e.stream);
     cudaFree(wsum);
     cudaFree(scratch);

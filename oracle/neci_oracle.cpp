@@ -95,12 +95,15 @@ inline u64 det_key(const i64 *det, int W, u64 seed) {
     return h;
 }
 
-// Stream of doubles in [0,1) (genrand_real2 semantics) for one
-// (determinant, iteration, purpose, run, attempt).
+// Stream of 64-bit draws for one (determinant, iteration, purpose, run,
+// attempt).  Each draw consumes one 64-bit value; a Philox block gives two.
+// NECI's uses of a uniform r in [0,1) are restated on the integer draws:
+// int(n*r) -> uniform_index(n) (multiply-high), r < p -> draw < prob_thresh(p),
+// and a genrand_real2 double is (draw >> 11) * 2^-53.
 struct Stream {
     u32 key[2];
     u32 ctr[4];
-    double buf[2];
+    u64 buf[2];
     int have;
     Stream(u64 dkey, i64 iter, u32 purpose, u32 run, u32 attempt) {
         key[0] = (u32)dkey;
@@ -111,20 +114,38 @@ struct Stream {
         ctr[3] = purpose | (run << 8) | ((u32)((u64)iter >> 32) << 16);
         have = 0;
     }
-    double next() {
+    u64 next64() {
         if (have == 0) {
             u32 o[4];
             Philox::block(ctr, key, o);
             ctr[1] += 1;
-            const u64 a = ((u64)o[1] << 32) | o[0];
-            const u64 b = ((u64)o[3] << 32) | o[2];
-            buf[0] = (double)(a >> 11) * 0x1.0p-53;
-            buf[1] = (double)(b >> 11) * 0x1.0p-53;
+            buf[0] = ((u64)o[1] << 32) | o[0];
+            buf[1] = ((u64)o[3] << 32) | o[2];
             have = 2;
         }
         return buf[2 - (have--)];
     }
+    double next() { return (double)(next64() >> 11) * 0x1.0p-53; }
 };
+
+inline u64 prob_thresh(double p) {
+    if (!(p > 0.0)) return 0ull;
+    if (p >= 1.0) return ~0ull;
+    return (u64)(p * 18446744073709551616.0);
+}
+inline bool bern(Stream &r, double p) {
+    const u64 x = r.next64();
+    return p >= 1.0 || x < prob_thresh(p);
+}
+inline bool bern_f(Stream &r, float p) {
+    const u32 x = (u32)(r.next64() >> 32);
+    if (p >= 1.0f) return true;
+    if (!(p > 0.0f)) return false;
+    return x < (u32)(p * 4294967296.0f);
+}
+inline u32 uniform_index(Stream &r, u32 n) {
+    return (u32)(((unsigned __int128)r.next64() * (unsigned __int128)n) >> 64);
+}
 
 thread_local std::string g_err;
 
@@ -456,35 +477,6 @@ struct Oracle {
         }
         (void)nI;
     }
-    // gen_excit_rs_hubbard (real_space_hubbard.F90:1938-2030) with
-    // pick_from_cum_list (lattice_models_utils.F90:150).
-    bool gen_excit_rs_hubbard(const i64 *ilut, const std::vector<int> &nI, Stream &rng,
-                              std::vector<int> &nJ, int &ic, int ex[2][2], bool &tParity, double &pgen) const {
-        const int nel = sys.nel;
-        ic = 1;
-        const int elec = 1 + (int)(rng.next() * nel);
-        const double p_elec = 1.0 / (double)nel;
-        const int src = nI[elec - 1];
-        std::vector<int> neigh;
-        spinorb_neighbours(src, neigh);
-        std::vector<double> cum;
-        double cum_sum;
-        create_cum_list(ilut, nI, src, neigh, cum, cum_sum);
-        if (cum_sum < 1e-10) { pgen = 0.0; return false; }
-        const double r = rng.next() * cum_sum;
-        int ind = (int)cum.size();  // binary_search_first_ge
-        for (size_t i = 0; i < cum.size(); ++i)
-            if (cum[i] >= r) { ind = (int)i + 1; break; }
-        double p_orb;
-        if (ind == 1) p_orb = cum[0] / cum_sum;
-        else p_orb = (cum[ind - 1] - cum[ind - 2]) / cum_sum;
-        const int orb = neigh[ind - 1];
-        pgen = p_elec * p_orb;
-        int e[2];
-        make_single(nI, nJ, elec, orb, e, tParity);
-        ex[0][0] = e[0]; ex[1][0] = e[1];
-        return true;
-    }
     // calc_pgen_rs_hubbard (real_space_hubbard.F90:2035-2078).
     double calc_pgen_rs_hubbard(const i64 *ilut, int src, int tgt, int ic) const {
         if (ic != 1) return 0.0;
@@ -502,70 +494,160 @@ struct Oracle {
         return (1.0 / (double)sys.nel) * (cpt / cum_sum);
     }
 
-    // ------------------------------------------------ molecular excitgens
+    // Excitation generated in precision Real (double: the FP64 path, float:
+    // the mixed-precision spawn amplitudes).
+    template <typename Real>
+    struct Gen {
+        std::vector<int> nJ;
+        int ic = 0;
+        int ex[2][2] = {{0, 0}, {0, 0}};
+        bool par = false;
+        Real pgen = 0;
+        Real hel = 0;
+    };
+    double tmat_d(int i, int j) const { return get_tmat(i, j); }
+    float tmat_f(int i, int j) const { return (float)get_tmat(i, j); }
+    template <typename Real> Real tmat_r(int i, int j) const;
+    template <typename Real> Real umat_r(int i, int j, int k, int l) const;
+    // sltcnd_1_kernel / sltcnd_2_kernel in precision Real (same order).
+    template <typename Real>
+    Real sltcnd_1_r(const std::vector<int> &nI, int src, int tgt) const {
+        Real hel = 0;
+        const int id1 = gtID(src), id2 = gtID(tgt);
+        if (is_beta(src) == is_beta(tgt)) {
+            for (int o : nI)
+                if (o != src) hel += umat_r<Real>(id1, gtID(o), id2, gtID(o));
+            for (int o : nI)
+                if (o != src && is_beta(src) == is_beta(o)) hel -= umat_r<Real>(id1, gtID(o), gtID(o), id2);
+        }
+        hel += tmat_r<Real>(src, tgt);
+        return hel;
+    }
+    template <typename Real>
+    Real sltcnd_2_r(const int ex[2][2]) const {
+        const int i = ex[0][0], j = ex[0][1], a = ex[1][0], b = ex[1][1];
+        Real hel = 0;
+        if (is_beta(i) == is_beta(a) && is_beta(j) == is_beta(b)) hel = umat_r<Real>(gtID(i), gtID(j), gtID(a), gtID(b));
+        if (is_beta(i) == is_beta(b) && is_beta(j) == is_beta(a)) hel -= umat_r<Real>(gtID(i), gtID(j), gtID(b), gtID(a));
+        return hel;
+    }
+    template <typename Real>
+    Real offdiag_from_ex_r(const std::vector<int> &nI, int ic, const int ex[2][2], bool tParity) const {
+        Real hel = 0;
+        if (sys.system == NECI_SYS_HUBBARD_REAL_SPACE) {
+            if (ic == 1) hel = tmat_r<Real>(ex[0][0], ex[1][0]);
+            else return 0;
+        } else {
+            if (ic == 1) hel = sltcnd_1_r<Real>(nI, ex[0][0], ex[1][0]);
+            else if (ic == 2) hel = sltcnd_2_r<Real>(ex);
+            else return 0;
+        }
+        return tParity ? -hel : hel;
+    }
+
+    // gen_excit_rs_hubbard (real_space_hubbard.F90:1938-2030) with
+    // pick_from_cum_list (lattice_models_utils.F90:150).
+    template <typename Real>
+    bool gen_excit_rs_hubbard(const i64 *ilut, const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
+        const int nel = sys.nel;
+        g.ic = 1;
+        const int elec = 1 + (int)uniform_index(rng, (u32)nel);
+        const double p_elec = 1.0 / (double)nel;
+        const int src = nI[elec - 1];
+        std::vector<int> neigh;
+        spinorb_neighbours(src, neigh);
+        std::vector<double> cum;
+        double cum_sum;
+        create_cum_list(ilut, nI, src, neigh, cum, cum_sum);
+        if (cum_sum < 1e-10) { g.pgen = 0; return false; }
+        const double r = rng.next() * cum_sum;
+        int ind = (int)cum.size();  // binary_search_first_ge
+        for (size_t i = 0; i < cum.size(); ++i)
+            if (cum[i] >= r) { ind = (int)i + 1; break; }
+        double p_orb;
+        if (ind == 1) p_orb = cum[0] / cum_sum;
+        else p_orb = (cum[ind - 1] - cum[ind - 2]) / cum_sum;
+        const int orb = neigh[ind - 1];
+        g.pgen = (Real)(p_elec * p_orb);
+        int e[2];
+        make_single(nI, g.nJ, elec, orb, e, g.par);
+        g.ex[0][0] = e[0]; g.ex[1][0] = e[1];
+        g.hel = offdiag_from_ex_r<Real>(nI, 1, g.ex, g.par);
+        return true;
+    }
+
     // CreateSingleExcit (GenRandSymExcitNUMod.F90:1118-1243), C1 symmetry,
     // tCycleOrbs = .false.: electron by rejection, hole by rejection.
-    bool create_single_excit(const i64 *ilut, const std::vector<int> &nI, Stream &rng,
-                             std::vector<int> &nJ, int ex[2][2], bool &tParity, double &pgen) const {
+    // pgen returned including pSingles (UniformSingles_t / gen_exc_sd).
+    template <typename Real>
+    bool create_single_excit(const i64 *ilut, const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
         const int nel = sys.nel, norbs = sys.nbasis / 2;
+        g.ic = 1;
         int nocc[2] = {0, 0};  // [alpha, beta]
         for (int o : nI) nocc[is_beta(o) ? 1 : 0]++;
         const int nunocc[2] = {norbs - nocc[0], norbs - nocc[1]};
         int elecs_wno = 0;
         for (int o : nI) if (nunocc[is_beta(o) ? 1 : 0] == 0) ++elecs_wno;
-        if (elecs_wno == nel) { pgen = 0.0; return false; }
+        if (elecs_wno == nel) { g.pgen = 0; return false; }
         int eleci = 0, ispn = 0, nexcit = 0;
         for (int attempts = 0; attempts <= 250; ++attempts) {
-            eleci = (int)(nel * rng.next()) + 1;
+            eleci = (int)uniform_index(rng, (u32)nel) + 1;
             ispn = is_beta(nI[eleci - 1]) ? 2 : 1;
             nexcit = nunocc[ispn - 1];
             if (nexcit != 0) break;
         }
-        if (nexcit == 0) { pgen = 0.0; return false; }
+        if (nexcit == 0) { g.pgen = 0; return false; }
         int orb = 0;
         bool found = false;
         for (int attempts = 0; attempts <= 250; ++attempts) {
-            const int chosen = (int)(norbs * rng.next());
+            const int chosen = (int)uniform_index(rng, (u32)norbs);
             orb = 2 * (chosen + 1) - (ispn - 1);
             if (!orb_occ(ilut, orb)) { found = true; break; }
         }
-        if (!found) { pgen = 0.0; return false; }
+        if (!found) { g.pgen = 0; return false; }
         int e[2];
-        make_single(nI, nJ, eleci, orb, e, tParity);
-        ex[0][0] = e[0]; ex[1][0] = e[1];
-        pgen = 1.0 / (double)(nexcit * (nel - elecs_wno));
+        make_single(nI, g.nJ, eleci, orb, e, g.par);
+        g.ex[0][0] = e[0]; g.ex[1][0] = e[1];
+        if (sizeof(Real) == 8) g.pgen = (Real)(sys.p_singles / (double)(nexcit * (nel - elecs_wno)));
+        else g.pgen = (Real)((float)sys.p_singles / (float)(nexcit * (nel - elecs_wno)));
+        g.hel = offdiag_from_ex_r<Real>(nI, 1, g.ex, g.par);
         return true;
     }
-    // pick_biased_elecs (excit_gens_int_weighted.F90:722-830) without pAA.
-    void pick_biased_elecs(const std::vector<int> &nI, Stream &rng, int elecs[2], int src[2], double &pgen) const {
+    // Electron pair positions of triangular index idx: ceiling((1+sqrt(9+8
+    // idx))/2) of pick_biased_elecs, in integers.
+    static void tri_pair(int idx, int &a1, int &a2) {
+        int a = 2;
+        while (a * (a - 1) / 2 <= idx) ++a;
+        a1 = a;
+        a2 = idx + 1 - ((a - 1) * (a - 2)) / 2;
+    }
+    // pick_biased_elecs (excit_gens_int_weighted.F90:722-830) without pAA:
+    // parallel pair with probability pParallel, then a uniform pair index.
+    template <typename Real>
+    void pick_biased_elecs(const std::vector<int> &nI, Stream &rng, int elecs[2], int src[2], Real &pgen) const {
         const int aa = nOccAlpha * (nOccAlpha - 1) / 2;
         const int bb = nOccBeta * (nOccBeta - 1) / 2;
         const int par = aa + bb;
         const int ab = nOccAlpha * nOccBeta;
-        const double pBias = sys.p_parallel;
-        double r = rng.next();
         int al_req, be_req, al_num[2] = {0, 0}, be_num[2] = {0, 0};
-        if (r < pBias) {
-            r = (r / pBias) * par;
-            int idx = (int)std::floor(r);
+        if (rng.next64() < prob_thresh(sys.p_parallel)) {
+            const int idx = (int)uniform_index(rng, (u32)par);
             if (idx < aa) {
                 al_req = 2; be_req = 0;
-                al_num[0] = (int)std::ceil((1.0 + std::sqrt(9.0 + 8.0 * (double)idx)) / 2.0);
-                al_num[1] = idx + 1 - ((al_num[0] - 1) * (al_num[0] - 2)) / 2;
+                tri_pair(idx, al_num[0], al_num[1]);
             } else {
                 al_req = 0; be_req = 2;
-                idx -= aa;
-                be_num[0] = (int)std::ceil((1.0 + std::sqrt(9.0 + 8.0 * (double)idx)) / 2.0);
-                be_num[1] = idx + 1 - ((be_num[0] - 1) * (be_num[0] - 2)) / 2;
+                tri_pair(idx - aa, be_num[0], be_num[1]);
             }
-            pgen = pBias / (double)par;
+            if (sizeof(Real) == 8) pgen = (Real)(sys.p_parallel / (double)par);
+            else pgen = (Real)((float)sys.p_parallel / (float)par);
         } else {
             al_req = 1; be_req = 1;
-            pgen = (1.0 - pBias) / (double)ab;
-            r = ((r - pBias) / (1.0 - pBias)) * ab;
-            const int idx = (int)std::floor(r);
+            const int idx = (int)uniform_index(rng, (u32)ab);
             al_num[0] = 1 + idx % nOccAlpha;
-            be_num[0] = 1 + (int)std::floor(idx / (double)nOccAlpha);
+            be_num[0] = 1 + idx / nOccAlpha;
+            if (sizeof(Real) == 8) pgen = (Real)((1.0 - sys.p_parallel) / (double)ab);
+            else pgen = (Real)((1.0f - (float)sys.p_parallel) / (float)ab);
         }
         int al_count = 0, be_count = 0, found = 0;
         for (int i = 1; i <= sys.nel; ++i) {
@@ -673,68 +755,65 @@ struct Oracle {
         pchb_ready = true;
         return NECI_GPU_OK;
     }
-    // sample_AliasTable_t (aliasSampling.F90:310-331) + AliasSampler_t%sample.
-    void alias_sample(size_t t, Stream &rng, int &ab, double &prob) const {
-        if (!alias_present[t]) { ab = 0; prob = 1.0; return; }
-        const double r = rng.next();
-        const int pos = (int)(abMax * r) + 1;
-        const double bias = std::max((double)abMax * r + 1.0 - pos, 0.0);
-        if (bias < alias_bias[t * abMax + pos - 1]) ab = pos;
-        else ab = alias_alias[t * abMax + pos - 1];
-        prob = alias_prob[t * abMax + ab - 1];
+    // sample_AliasTable_t (aliasSampling.F90:310-331) + AliasSampler_t%sample:
+    // slot = int(n r) and the fraction n r - int(n r) from one 64-bit draw.
+    template <typename Real>
+    void alias_sample(size_t t, Stream &rng, int &ab, Real &prob) const {
+        if (!alias_present[t]) { ab = 0; prob = 1; return; }
+        const u64 r = rng.next64();
+        const unsigned __int128 prod = (unsigned __int128)r * (unsigned __int128)(u64)abMax;
+        const u64 pos0 = (u64)(prod >> 64), frac = (u64)prod;
+        const u64 thr = prob_thresh(alias_bias[t * abMax + pos0]);
+        if (frac < thr || thr == ~0ull) ab = (int)pos0 + 1;
+        else ab = alias_alias[t * abMax + pos0];
+        const double pr = alias_prob[t * abMax + ab - 1];
+        prob = (Real)pr;  // single precision: the same rounding as the device copy
     }
-    // GAS_doubles_PCHB_gen_exc (gasci_pchb_doubles_spatorb_fastweighted.fpp).
-    bool pchb_doubles(const std::vector<int> &nI, Stream &rng, std::vector<int> &nJ, int ex[2][2],
-                      bool &tParity, double &pgen) const {
+    // GAS_doubles_PCHB_gen_exc (gasci_pchb_doubles_spatorb_fastweighted.fpp);
+    // pgen returned including pDoubles.
+    template <typename Real>
+    bool pchb_doubles(const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
+        g.ic = 2;
         int elecs[2], src[2];
-        pick_biased_elecs(nI, rng, elecs, src, pgen);
+        Real pgen;
+        pick_biased_elecs<Real>(nI, rng, elecs, src, pgen);
         const i64 ij = fuse_index(gtID(src[0]), gtID(src[1]));
         int spin[2] = {src[0] % 2, src[1] % 2};  // getSpinIndex: 0 alpha, 1 beta
         int type;
         if (spin[0] == spin[1]) type = 1;
         else {
-            if (rng.next() < pexch[ij - 1]) {
+            const Real pe = (Real)pexch[ij - 1];
+            if (rng.next64() < prob_thresh(pexch[ij - 1])) {
                 type = 3;
-                pgen *= pexch[ij - 1];
+                pgen *= pe;
                 std::swap(spin[0], spin[1]);
             } else {
                 type = 2;
-                pgen *= (1.0 - pexch[ij - 1]);
+                pgen *= ((Real)1 - pe);
             }
         }
         int ab;
-        double pholes;
-        alias_sample((size_t)(ij - 1) * 3 + (type - 1), rng, ab, pholes);
-        if (ab == 0) return false;
+        Real pholes;
+        alias_sample<Real>((size_t)(ij - 1) * 3 + (type - 1), rng, ab, pholes);
+        if (ab == 0) { g.pgen = 0; return false; }
         int orbs[2] = {2 * tgt1[ab] - spin[0], 2 * tgt2[ab] - spin[1]};
         bool invalid = orbs[0] == 0 || orbs[1] == 0;
         for (int o : nI) if (o == orbs[0] || o == orbs[1]) invalid = true;
-        if (!invalid && std::fabs(pholes) < 1e-10) invalid = true;
-        if (invalid) return false;
-        make_double(nI, nJ, elecs[0], elecs[1], orbs[0], orbs[1], ex, tParity);
+        if (!invalid && !(pholes > (Real)1e-10)) invalid = true;
+        if (invalid) { g.pgen = 0; return false; }
+        make_double(nI, g.nJ, elecs[0], elecs[1], orbs[0], orbs[1], g.ex, g.par);
         pgen *= pholes;
+        if (sizeof(Real) == 8) g.pgen = pgen * (Real)(1.0 - sys.p_singles);
+        else g.pgen = pgen * (Real)(1.0f - (float)sys.p_singles);
+        g.hel = offdiag_from_ex_r<Real>(nI, 2, g.ex, g.par);
         return true;
     }
     // gen_exc_sd (excitation_generators.F90:110-133) with UniformSingles_t.
-    bool gen_excit_pchb(const i64 *ilut, const std::vector<int> &nI, Stream &rng, std::vector<int> &nJ,
-                        int &ic, int ex[2][2], bool &tParity, double &pgen) const {
-        if (rng.next() < sys.p_singles) {
-            ic = 1;
-            const bool ok = create_single_excit(ilut, nI, rng, nJ, ex, tParity, pgen);
-            pgen *= sys.p_singles;
-            return ok;
-        }
-        ic = 2;
-        const bool ok = pchb_doubles(nI, rng, nJ, ex, tParity, pgen);
-        pgen *= (1.0 - sys.p_singles);
-        return ok;
-    }
-
-    bool generate_excitation(const i64 *ilut, const std::vector<int> &nI, Stream &rng, std::vector<int> &nJ,
-                             int &ic, int ex[2][2], bool &tParity, double &pgen) const {
-        if (sys.excitgen == NECI_EXGEN_RS_HUBBARD)
-            return gen_excit_rs_hubbard(ilut, nI, rng, nJ, ic, ex, tParity, pgen);
-        return gen_excit_pchb(ilut, nI, rng, nJ, ic, ex, tParity, pgen);
+    template <typename Real>
+    bool generate_excitation(const i64 *ilut, const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
+        if (sys.excitgen == NECI_EXGEN_RS_HUBBARD) return gen_excit_rs_hubbard<Real>(ilut, nI, rng, g);
+        if (rng.next64() < prob_thresh(sys.p_singles)) return create_single_excit<Real>(ilut, nI, rng, g);
+        return pchb_doubles<Real>(nI, rng, g);
     }
 
     // ------------------------------------------------------------- rows
@@ -780,6 +859,11 @@ struct Oracle {
     };
 };
 
+template <> inline double Oracle::tmat_r<double>(int i, int j) const { return get_tmat(i, j); }
+template <> inline float Oracle::tmat_r<float>(int i, int j) const { return (float)get_tmat(i, j); }
+template <> inline double Oracle::umat_r<double>(int i, int j, int k, int l) const { return get_umat_el(i, j, k, l); }
+template <> inline float Oracle::umat_r<float>(int i, int j, int k, int l) const { return (float)get_umat_el(i, j, k, l); }
+
 struct IterRun;
 std::vector<Oracle::Spawn> compress_list(const Oracle &o, const neci_gpu_iter_params &p, std::vector<Oracle::Spawn> &sp,
                                          double *nannihil);
@@ -796,22 +880,80 @@ struct IterRun {
     int err = 0;
     IterRun(Oracle &o_, const neci_gpu_iter_params &p_, neci_gpu_iter_stats &s_) : o(o_), p(p_), st(s_) {}
 
-    // stochastic_round (lib/util_mod.fpp:182-203).
-    static double stochastic_round(double r, Stream &rng) {
-        double i = std::trunc(r);
-        const double res = r - i;
-        if (std::fabs(res) >= 1e-12)
-            if (std::fabs(res) > rng.next()) i += std::nearbyint(fsign(1.0, r));
-        return i;
-    }
     // decide_num_to_spawn (fcimc_helper.F90:2160-2174).
     static int decide_num_to_spawn(double pop, double av, Stream &rng) {
         int n = std::abs((int)(pop * av));
         if (std::fabs(std::fabs(pop * av) - (double)n) > 1e-12) {
             const double pe = std::fabs(pop * av) - (double)n;
-            if (pe > rng.next()) ++n;
+            if (bern(rng, pe)) ++n;
         }
         return n;
+    }
+    // attempt_create_normal (fcimc_pointed_fns.F90:178-494): the child
+    // amplitude -tau H_ij sign(C) / (p_gen AvMCExcits) in precision Real,
+    // then RealSpawnCutoff rounding (x = n/cutoff taken as n * (1/cutoff)) or
+    // stochastic_round (lib/util_mod.fpp:182-203); returned in fixed point.
+    template <typename Real>
+    i64 spawn_amplitude(Real hel, Real pgen, bool neg, Stream &rng, int &ovf) const {
+        const Real ww = neg ? (Real)-1 : (Real)1;
+        const Real prob = pgen * (Real)p.av_mc_excits;
+        Real nsp = -(Real)p.tau * hel * ww / prob;
+        const Real eps = (Real)1e-12;
+        if (p.t_all_real_coeff) {
+            const Real cut = (Real)p.real_spawn_cutoff;
+            if (p.t_real_spawn_cutoff && std::fabs(nsp) < cut) {
+                const Real x = nsp * ((Real)1 / cut);
+                Real i = std::trunc(x);
+                const Real res = x - i;
+                if (std::fabs(res) >= eps) {
+                    const bool up = (sizeof(Real) == 8) ? bern(rng, (double)std::fabs(res)) : bern_f(rng, (float)std::fabs(res));
+                    if (up) i += (x >= (Real)0 ? (Real)1 : (Real)-1);
+                }
+                nsp = cut * i;
+            }
+        } else {
+            Real i = std::trunc(nsp);
+            const Real res = nsp - i;
+            if (std::fabs(res) >= eps) {
+                const bool up = (sizeof(Real) == 8) ? bern(rng, (double)std::fabs(res)) : bern_f(rng, (float)std::fabs(res));
+                if (up) i += (nsp >= (Real)0 ? (Real)1 : (Real)-1);
+            }
+            nsp = i;
+        }
+        if (!(std::fabs(nsp) >= eps)) return 0;
+        if (sizeof(Real) == 8) {
+            const double sc = (double)nsp * 4294967296.0;
+            if (!(std::fabs(sc) < 9.2e18)) { ovf = 1; return 0; }
+            return (i64)std::llrint(sc);
+        }
+        const float sc = (float)nsp * 4294967296.0f;
+        if (!(std::fabs(sc) < 9.2e18f)) { ovf = 1; return 0; }
+        return (i64)std::llrintf(sc);
+    }
+    template <typename Real>
+    void attempt(const i64 *r, const std::vector<int> &nI, u64 dkey, int run, int a, bool neg, bool core,
+                 bool semistoch, bool parent_init, int &ovf) {
+        Stream rng(dkey, p.iter, P_ATTEMPT, run, (u32)a);
+        Oracle::Gen<Real> g;
+        if (!o.generate_excitation<Real>(r, nI, rng, g)) return;
+        std::vector<i64> child(o.W);
+        o.encode_bit_det(g.nJ, child.data());
+        if (semistoch && core) {
+            // is_core_state (semi_stoch_procs.F90:547)
+            i64 slot, h;
+            if (o.hash_lookup(g.nJ, child.data(), slot, h) && o.is_core(o.row(slot))) return;
+        }
+        const i64 q = spawn_amplitude<Real>(g.hel, g.pgen, neg, rng, ovf);
+        if (q == 0) return;
+        // create_particle (fcimc_helper.F90:152-308)
+        if ((i64)spawns.size() >= o.sys.max_spawned) { err = NECI_GPU_ERR_SPAWN_FULL; return; }
+        Oracle::Spawn s;
+        s.det = child;
+        s.q[0] = s.q[1] = 0;
+        s.q[run] = q;
+        s.flags = 0;
+        if (p.t_trunc_initiator && parent_init) Oracle::set_flag(s.flags, Oracle::init_flag(run));
+        spawns.push_back(s);
     }
     // TestInitiator_explicit (fcimc_helper.F90:1142-1240) with
     // initiator_criterium (:1274) and no ADI / senior / initiator space.
@@ -873,47 +1015,15 @@ struct IterRun {
                 const int nspawn = decide_num_to_spawn(sgn[run], p.av_mc_excits, rs);
                 st.n_attempts += nspawn;
                 const bool parent_init = Oracle::test_flag(o.flags(r), Oracle::init_flag(run));
+                int ovf = 0;
                 for (int a = 0; a < nspawn; ++a) {
-                    Stream rng(dkey, p.iter, P_ATTEMPT, run, (u32)a);
-                    int ic = 0, ex[2][2] = {{0, 0}, {0, 0}};
-                    bool par = false;
-                    double pgen = 0.0;
-                    if (!o.generate_excitation(r, nI, rng, nJ, ic, ex, par, pgen)) continue;
-                    std::vector<i64> child(W);
-                    o.encode_bit_det(nJ, child.data());
-                    if (semistoch && core) {
-                        // is_core_state (semi_stoch_procs.F90:547)
-                        i64 slot, h;
-                        if (o.hash_lookup(nJ, child.data(), slot, h) && o.is_core(o.row(slot))) continue;
-                    }
-                    // attempt_create_normal (fcimc_pointed_fns.F90:178-494)
-                    const double prob = pgen * p.av_mc_excits;
-                    const double hel = o.offdiag_from_ex(nI, ic, ex, par);
-                    const double walkerweight = fsign(1.0, sgn[run]);
-                    double nSpawn;
-                    if (p.precision == NECI_PREC_MIXED) {
-                        const float t = (float)p.tau, h = (float)hel, w = (float)walkerweight, pr = (float)prob;
-                        nSpawn = (double)(-t * h * w / pr);
-                    } else {
-                        nSpawn = -p.tau * hel * walkerweight / prob;
-                    }
-                    if (p.t_all_real_coeff) {
-                        if (p.t_real_spawn_cutoff && std::fabs(nSpawn) < p.real_spawn_cutoff)
-                            nSpawn = p.real_spawn_cutoff * stochastic_round(nSpawn / p.real_spawn_cutoff, rng);
-                    } else {
-                        nSpawn = stochastic_round(nSpawn, rng);
-                    }
-                    if (std::fabs(nSpawn) < 1e-12) continue;  // near_zero(child)
-                    // create_particle (fcimc_helper.F90:152-308)
-                    if ((i64)spawns.size() >= o.sys.max_spawned) { err = NECI_GPU_ERR_SPAWN_FULL; return; }
-                    Oracle::Spawn s;
-                    s.det = child;
-                    s.q[0] = s.q[1] = 0;
-                    s.q[run] = to_fixed(nSpawn);
-                    s.flags = 0;
-                    if (p.t_trunc_initiator && parent_init) Oracle::set_flag(s.flags, Oracle::init_flag(run));
-                    spawns.push_back(s);
+                    if (p.precision == NECI_PREC_MIXED)
+                        attempt<float>(r, nI, dkey, run, a, sgn[run] < 0.0, core, semistoch, parent_init, ovf);
+                    else
+                        attempt<double>(r, nI, dkey, run, a, sgn[run] < 0.0, core, semistoch, parent_init, ovf);
+                    if (err) return;
                 }
+                if (ovf) { err = NECI_GPU_ERR_OVERFLOW; return; }
             }
         }
         st.n_spawned = (i64)spawns.size();
@@ -1000,7 +1110,7 @@ struct IterRun {
                     if (a > 1e-12 && a < p.occupied_thresh) {
                         Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
                         const double pRemove = 1.0 - a / p.occupied_thresh;
-                        if (pRemove > rng.next()) {
+                        if (bern(rng, pRemove)) {
                             st.nremoved[k] += a;
                             ss[k] = 0.0;
                         } else {
@@ -1061,7 +1171,7 @@ struct IterRun {
                 double rat = fac * std::fabs(sgn[k]);
                 iDie[k] = std::trunc(rat);
                 rat -= iDie[k];
-                if (std::fabs(rat) > rng.next()) iDie[k] += std::nearbyint(fsign(1.0, rat));
+                if (bern(rng, std::fabs(rat))) iDie[k] += std::nearbyint(fsign(1.0, rat));
             }
         }
         for (int k = 0; k < L; ++k) {
@@ -1105,7 +1215,7 @@ struct IterRun {
                 if (a > 1e-12 && a < p.occupied_thresh) {
                     Stream rng(det_key(r, o.W, p.seed), p.iter, P_STATS_ROUND, k, 0);
                     const double pRemove = (p.occupied_thresh - a) / p.occupied_thresh;
-                    if (pRemove > rng.next()) {
+                    if (bern(rng, pRemove)) {
                         st.nremoved[k] += a;
                         cur[k] = 0.0;
                         o.set_sign(r, k, 0.0);
@@ -1248,7 +1358,7 @@ int annihilate_injected(Oracle &o, const neci_gpu_iter_params &p, const i64 *spa
                 if (a > 1e-12 && a < p.occupied_thresh) {
                     Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
                     const double pRemove = 1.0 - a / p.occupied_thresh;
-                    if (pRemove > rng.next()) { st.nremoved[k] += a; ss[k] = 0.0; }
+                    if (bern(rng, pRemove)) { st.nremoved[k] += a; ss[k] = 0.0; }
                     else { st.nborn[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
                 }
             }
@@ -1444,15 +1554,13 @@ int32_t orc_gen_excit(void *h, const int64_t *det, int64_t n, uint64_t seed, int
     const u64 dkey = det_key(det, o->W, seed);
     for (int64_t a = 0; a < n; ++a) {
         Stream rng(dkey, iter, P_ATTEMPT, 0, (u32)a);
-        int ic = 0, ex[2][2] = {{0, 0}, {0, 0}};
-        bool par = false;
-        double pg = 0.0;
+        Oracle::Gen<double> g;
         int64_t *c = child + (size_t)a * o->W;
         for (int w = 0; w < o->W; ++w) c[w] = 0;
-        if (o->generate_excitation(det, nI, rng, nJ, ic, ex, par, pg)) {
-            o->encode_bit_det(nJ, c);
-            pgen[a] = pg;
-            hel[a] = o->offdiag_from_ex(nI, ic, ex, par);
+        if (o->generate_excitation<double>(det, nI, rng, g)) {
+            o->encode_bit_det(g.nJ, c);
+            pgen[a] = g.pgen;
+            hel[a] = g.hel;
         } else {
             pgen[a] = 0.0;
             hel[a] = 0.0;

@@ -35,10 +35,12 @@ def hub10_exact():
     return E0_HUB10
 
 
-@pytest.mark.parametrize("initiator,walkers", [(False, 2.0e4), (True, 5.0e4)])
+# full FCIQMC runs above the annihilation plateau of this lattice; the
+# initiator run at 5e4 walkers carries a small initiator bias (< 2 mHa)
+@pytest.mark.parametrize("initiator,walkers", [(False, 2.0e5), (True, 5.0e4)])
 def test_hubbard10_energy_matches_exact_diagonalisation(initiator, walkers):
     spec = hubbard10()
-    eng = Engine(spec, max_walkers=2_000_000, max_spawned=4_000_000)
+    eng = Engine(spec, max_walkers=4_000_000, max_spawned=8_000_000)
     eng.start_from_reference(initial_part=10.0)
     calc = CalcParams(tau=0.01, target_walkers=walkers, steps_sft=10, sft_damp=0.1, seed=4242,
                       trunc_initiator=initiator)
