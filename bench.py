@@ -178,6 +178,15 @@ def run_gpu(args, rank, world):
         p.iter += 1
         e2e_updates += st.tot_parts_old[0]
     e2e_s = time.perf_counter() - t0
+    # ---- the same steps with FP32 spawn amplitudes (mixed precision)
+    pm = drv.params()
+    pm.iter = p.iter
+    pm.precision = capi.PREC_MIXED
+    eng.iterate_n(pm, 3)
+    pm.iter += 3
+    mstats, mixed_ms = eng.iterate_timed(pm, args.steps)
+    p.iter = pm.iter + args.steps
+    mixed_updates = sum(s.tot_parts_old[0] for s in mstats)
     # ---- per-kernel timing pass (events around each kernel; not the timed number)
     eng.set_profiling(True)
     prof_stats = eng.iterate_n(p, 3)
@@ -188,7 +197,7 @@ def run_gpu(args, rank, world):
     return {
         "eng": eng, "spec": spec, "tau": tau, "updates": updates, "dev_ms": dev_ms, "clk": clk.summary(),
         "e2e_updates": e2e_updates, "e2e_s": e2e_s, "ktimes": ktimes, "last": last, "stats": stats,
-        "equil": equil,
+        "equil": equil, "mixed_updates": mixed_updates, "mixed_ms": mixed_ms,
     }
 
 
@@ -264,7 +273,7 @@ def run_reference(args, rank, world):
     from oracle import oracle as o
     o.lib()  # build/load before forking workers
     cores = os.cpu_count() or 1
-    per_step = 4.0
+    per_step = max(0.5, min(4.0, 150.0 / max(args.steps, 1)))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     total_upd, total_s = 0.0, 0.0
@@ -371,6 +380,10 @@ def main():
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": ab, "ms_per_launch": top_ms},
         "kernel_ms_per_step": {k: v[0] / v[1] for k, v in kt.items()},
+        "mixed_precision": {"value": r["mixed_updates"] / (r["mixed_ms"] / 1000.0), "unit": UNIT,
+                            "ms_per_step": r["mixed_ms"] / args.steps,
+                            "speedup_vs_fp64": (r["mixed_updates"] / r["mixed_ms"]) / (updates / (dev_s * 1000.0)),
+                            "note": "FP32 H_ij, p_gen and spawn amplitude; FP64 death, E_proj and signs"},
     }
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_sample()

@@ -64,6 +64,13 @@ void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
     d.precision = p.precision;
     d.seed = p.seed;
     d.iter = p.iter;
+    d.inv_cutoff = 1.0 / p.real_spawn_cutoff;
+    d.inv_av = 1.0 / p.av_mc_excits;
+    d.f_tau = (float)p.tau;
+    d.f_inv_av = (float)d.inv_av;
+    d.f_cutoff = (float)p.real_spawn_cutoff;
+    d.f_inv_cutoff = (float)d.inv_cutoff;
+    d.cutoff_q = (unsigned long long)std::llrint(std::ldexp(p.real_spawn_cutoff, NECI_SPAWN_FIXED_BITS));
 }
 
 const char *kKernelNames[K_NUM] = {"rehash",    "begin",        "sweep",      "expand",      "spawn", "core",
@@ -104,7 +111,7 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
 
 int ensure_graph(Engine &e) {
     const bool core = e.st.n_core > 0;
-    if (e.graph && e.graph_core == core) return NECI_GPU_OK;
+    if (e.graph && e.graph_core == core && e.graph_prec == e.h_params->precision) return NECI_GPU_OK;
     if (e.graph) {
         cudaGraphExecDestroy(e.graph);
         e.graph = nullptr;
@@ -116,6 +123,7 @@ int ensure_graph(Engine &e) {
     CK(cudaGraphInstantiate(&e.graph, g, 0));
     cudaGraphDestroy(g);
     e.graph_core = core;
+    e.graph_prec = e.h_params->precision;
     return NECI_GPU_OK;
 }
 
@@ -189,8 +197,8 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     DevState &st = e.st;
     st.max_walkers = sys->max_walkers;
     st.max_spawned = sys->max_spawned;
-    st.max_chunks = sys->max_walkers * s.L + sys->max_spawned + 1024;
-    st.max_big = st.max_chunks / kBigChunks + 1024;
+    st.max_att = 2 * sys->max_spawned + 1024;
+    st.max_big = st.max_att / kBigAttempts + 1024;
     st.hash_n = next_pow2(std::max<unsigned long long>((unsigned long long)sys->n_walker_hashes,
                                                        2ull * (unsigned long long)sys->max_walkers));
     st.spawn_hash_n = next_pow2(2ull * (unsigned long long)sys->max_spawned);
@@ -206,8 +214,9 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.slot_bucket, (size_t)st.max_walkers);
     A(st.free_list, (size_t)st.max_walkers + 1);
     A(st.spawn, (size_t)st.max_spawned * s.R);
-    A(st.chunks, (size_t)st.max_chunks * 2);
+    A(st.att, (size_t)st.max_att);
     A(st.big, (size_t)st.max_big * 3);
+    A(st.huge, (size_t)kMaxHuge * 3);
     A(st.acc, (size_t)st.max_walkers * s.L);
     A(st.meta, (size_t)st.max_walkers * s.L);
     A(st.cand, (size_t)st.max_spawned);
@@ -356,6 +365,14 @@ int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii
     s.f_p_doubles = 1.0f - (float)s.p_singles;
     s.f_p_singles = (float)s.p_singles;
     s.f_p_elec = 1.0f / (float)s.nel;
+    s.inv_par = (double)par / s.p_parallel;
+    s.inv_opp = (double)(na * nb) / (1.0 - s.p_parallel);
+    s.inv_pdoub = 1.0 / s.p_doubles;
+    s.inv_psingles = 1.0 / s.p_singles;
+    s.f_inv_par = (float)s.inv_par;
+    s.f_inv_opp = (float)s.inv_opp;
+    s.f_inv_pdoub = (float)s.inv_pdoub;
+    s.f_inv_psingles = (float)s.inv_psingles;
     e.have_ref = true;
     if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
     return NECI_GPU_OK;
@@ -388,6 +405,20 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
     s.alias_prob32 = prob32;
     s.pexch_thr = pthr;
     s.pexch32 = pexch32;
+    double *ainv, *peinv, *pninv;
+    float *ainv32, *peinv32, *pninv32;
+    if (int r = dalloc(e, &ainv, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &ainv32, ntab * s.abMax)) return r;
+    if (int r = dalloc(e, &peinv, (size_t)s.ijMax)) return r;
+    if (int r = dalloc(e, &pninv, (size_t)s.ijMax)) return r;
+    if (int r = dalloc(e, &peinv32, (size_t)s.ijMax)) return r;
+    if (int r = dalloc(e, &pninv32, (size_t)s.ijMax)) return r;
+    s.alias_inv = ainv;
+    s.alias_inv32 = ainv32;
+    s.pexch_inv = peinv;
+    s.pnoexch_inv = pninv;
+    s.pexch_inv32 = peinv32;
+    s.pnoexch_inv32 = pninv32;
     std::vector<int32_t> tp(s.abMax + 1, 0);
     for (int a = 1; a <= s.nBI; ++a)
         for (int b = 1; b <= a; ++b) tp[(long long)b + (long long)a * (a - 1) / 2] = (b << 16) | a;

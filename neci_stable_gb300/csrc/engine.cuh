@@ -17,8 +17,9 @@ namespace neci {
 constexpr int kMaxWords = 4;      // nBasis <= 255 (NIfD <= 3)
 constexpr int kMaxNel = 64;
 constexpr int kMaxNeigh = 8;
-constexpr int kChunk = 16;        // spawn attempts per work item
-constexpr int kBigChunks = 64;    // parents with more chunks are expanded by k_expand
+constexpr int kBigAttempts = 32;  // parents with more attempts are expanded by k_expand
+constexpr int kHugeAttempts = 1 << 16;  // ... and with more than this by the whole grid
+constexpr int kMaxHuge = 4096;
 constexpr int kProbeLimit = 1 << 16;
 constexpr uint32_t kEmpty = 0u;
 constexpr uint32_t kTomb = 0xFFFFFFFFu;
@@ -31,7 +32,7 @@ struct Control {
     unsigned long long tot_walkers;     // slots in use (TotWalkers)
     unsigned long long n_free;          // holes pushed this step
     unsigned long long free_taken;      // holes reused by new determinants
-    unsigned long long n_chunks;        // spawn work items
+    unsigned long long n_att;           // spawn attempt entries
     unsigned long long n_spawned;       // spawn records
     unsigned long long n_cand;          // spawns onto determinants not in the list
     unsigned long long n_reps;          // unique new determinants
@@ -42,6 +43,7 @@ struct Control {
     unsigned long long n_tomb;          // hash tombstones
     unsigned long long n_found;         // unique spawned determinants already present
     unsigned long long n_big;           // parents expanded by k_expand
+    unsigned long long n_huge;          // parents expanded by the whole grid
     unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
@@ -74,6 +76,11 @@ struct DevSys {
     // single-precision copies for the mixed-precision spawn amplitudes
     float f_pgen_par, f_pgen_opp, f_p_doubles, f_p_singles, f_p_elec;
     const float *umat32, *tmat32, *alias_prob32, *pexch32;
+    // reciprocals: the spawn amplitude multiplies by 1/p_gen built from them
+    double inv_par, inv_opp, inv_pdoub, inv_psingles;
+    float f_inv_par, f_inv_opp, f_inv_pdoub, f_inv_psingles;
+    const double *alias_inv, *pexch_inv, *pnoexch_inv;   // 1/prob, 1/pExch, 1/(1-pExch)
+    const float *alias_inv32, *pexch_inv32, *pnoexch_inv32;
 };
 
 // Resident walker state (device pointers).
@@ -84,10 +91,11 @@ struct DevState {
     unsigned long long hash_n;     // buckets (power of two)
     uint32_t *slot_bucket;         // bucket holding each slot
     int32_t *free_list;
-    long long max_walkers, max_spawned, max_chunks;
+    long long max_walkers, max_spawned, max_att;
     long long *spawn;              // spawn records
-    unsigned long long *chunks;    // pairs: slot | run << 32 | neg << 33 | n << 34, first attempt
-    unsigned long long *big;       // triples: slot | run << 32 | neg << 33, attempts, first chunk
+    unsigned long long *att;       // attempts: slot | run << 32 | neg << 33 | attempt << 34
+    unsigned long long *big;       // triples: slot | run << 32 | neg << 33, attempts, first entry
+    unsigned long long *huge;      // the same for parents with more than kHugeAttempts attempts
     long long max_big;
     long long *acc;                // per slot*L fixed-point spawn sums (found determinants)
     uint32_t *meta;                // per slot*L spawn counts | initiator bit 31
@@ -116,6 +124,10 @@ struct IterParams {
     int t_trunc_initiator, t_init_coherent_rule, t_all_real_coeff, t_real_spawn_cutoff, t_core_inits, precision;
     unsigned long long seed;
     long long iter;
+    // derived on the host: 1/RealSpawnCutoff, 1/AvMCExcits and FP32 copies
+    double inv_cutoff, inv_av;
+    float f_tau, f_inv_av, f_cutoff, f_inv_cutoff;
+    unsigned long long cutoff_q;  // RealSpawnCutoff in fixed point
 };
 
 // ---------------------------------------------------------------------------

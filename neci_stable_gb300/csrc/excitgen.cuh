@@ -19,6 +19,7 @@ template <typename Real>
 struct Excit {
     unsigned long long child[kMaxWords];
     Real pgen;
+    Real invp;  // 1/pgen as a product of reciprocal factors
     Real hel;
     int ic;
     bool ok;
@@ -121,7 +122,9 @@ __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long 
         if (cum[k] >= r) { ind = k + 1; break; }
     const double p_orb = (ind == 1) ? cum[0] / cum_sum : (cum[ind - 1] - cum[ind - 2]) / cum_sum;
     const int orb = orbs[ind - 1];
-    e.pgen = (Real)(s.p_elec * p_orb);
+    const double pg = s.p_elec * p_orb;
+    e.pgen = (Real)pg;
+    e.invp = (Real)(1.0 / pg);
     finish_single<Real>(s, d, src, orb, e);
     e.ok = true;
 }
@@ -159,8 +162,14 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
         if (!orb_occ(d, orb)) { found = true; break; }
     }
     if (!found) { e.pgen = 0; return; }
-    if (sizeof(Real) == 8) e.pgen = (Real)(s.p_singles / (double)(nexcit * (s.nel - elecs_wno)));
-    else e.pgen = (Real)(s.f_p_singles / (float)(nexcit * (s.nel - elecs_wno)));
+    const int count = nexcit * (s.nel - elecs_wno);
+    if (sizeof(Real) == 8) {
+        e.pgen = (Real)(s.p_singles / (double)count);
+        e.invp = (Real)((double)count * s.inv_psingles);
+    } else {
+        e.pgen = (Real)(s.f_p_singles / (float)count);
+        e.invp = (Real)((float)count * s.f_inv_psingles);
+    }
     finish_single<Real>(s, d, nI[eleci - 1], orb, e);
     e.ok = true;
 }
@@ -188,7 +197,7 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     const int aa = s.nOccAlpha * (s.nOccAlpha - 1) / 2;
     const int bb = s.nOccBeta * (s.nOccBeta - 1) / 2;
     int al_req, be_req, al_num[2] = {0, 0}, be_num[2] = {0, 0};
-    Real pgen;
+    Real pgen, invp;
     if (rng.next64() < s.thr_bias) {
         int idx = (int)uniform_index(rng, (unsigned)(aa + bb));
         if (idx < aa) {
@@ -199,12 +208,14 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
             tri_pair(idx - aa, be_num[0], be_num[1]);
         }
         pgen = dbl ? (Real)s.pgen_par : (Real)s.f_pgen_par;
+        invp = dbl ? (Real)s.inv_par : (Real)s.f_inv_par;
     } else {
         al_req = 1; be_req = 1;
         const int idx = (int)uniform_index(rng, (unsigned)(s.nOccAlpha * s.nOccBeta));
         al_num[0] = 1 + idx % s.nOccAlpha;
         be_num[0] = 1 + idx / s.nOccAlpha;
         pgen = dbl ? (Real)s.pgen_opp : (Real)s.f_pgen_opp;
+        invp = dbl ? (Real)s.inv_opp : (Real)s.f_inv_opp;
     }
     int elecs[2] = {0, 0}, found = 0, al_count = 0, be_count = 0;
     for (int i = 1; i <= s.nel; ++i) {
@@ -230,10 +241,12 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
         if (rng.next64() < __ldg(&s.pexch_thr[ij - 1])) {
             type = 3;
             pgen *= pe;
+            invp *= dbl ? (Real)__ldg(&s.pexch_inv[ij - 1]) : (Real)__ldg(&s.pexch_inv32[ij - 1]);
             const int t = spin0; spin0 = spin1; spin1 = t;
         } else {
             type = 2;
             pgen *= ((Real)1 - pe);
+            invp *= dbl ? (Real)__ldg(&s.pnoexch_inv[ij - 1]) : (Real)__ldg(&s.pnoexch_inv32[ij - 1]);
         }
     }
     // sample_AliasTable_t (aliasSampling.F90:310-331): slot and fraction
@@ -264,6 +277,8 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     e.hel = (np & 1) ? -hel : hel;
     pgen *= pholes;
     e.pgen = pgen * (dbl ? (Real)s.p_doubles : (Real)s.f_p_doubles);
+    invp *= dbl ? (Real)__ldg(&s.alias_inv[base + ab - 1]) : (Real)__ldg(&s.alias_inv32[base + ab - 1]);
+    e.invp = invp * (dbl ? (Real)s.inv_pdoub : (Real)s.f_inv_pdoub);
     e.ok = true;
 }
 

@@ -43,6 +43,7 @@ struct Engine {
     // CUDA graph of one step (stats into d_stats[0])
     cudaGraphExec_t graph = nullptr;
     bool graph_core = false;
+    int graph_prec = -1;
     // profiling
     bool profiling = false;
     cudaEvent_t ev[2 * K_NUM] = {};

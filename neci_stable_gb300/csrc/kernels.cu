@@ -8,12 +8,13 @@
 //   k_sweep        loop_over_determinants (:1294-1758) minus the spawn
 //                  attempts: free slots, initiator flags (CalcParentFlag),
 //                  E_proj sums (SumEContrib), number of spawns
-//                  (decide_num_to_spawn) emitted as work chunks, core
-//                  vector gather, and the death step
+//                  (decide_num_to_spawn) emitted as one entry per attempt,
+//                  core vector gather, and the death step
 //                  (perform_death_all_walkers / walker_death)
+//   k_expand       attempt entries of heavily populated parents, a block each
 //   k_spawn        the spawn attempts (generate_excitation, attempt_create,
-//                  create_particle): one thread per chunk of <= kChunk
-//                  attempts of one parent
+//                  create_particle): one attempt per thread per round,
+//                  instantiated per precision and excitation generator
 //   k_core         determ_projection_no_death (semi_stoch_procs.F90:290)
 //   k_ann_probe    annihilation pass 1: look every spawn up in the walker
 //                  hash (hash_table_lookup, hash.F90:294); spawns onto
@@ -181,9 +182,10 @@ __device__ inline bool test_initiator(const IterParams &p, bool was, double sgn,
 __global__ void k_begin(DevState st) {
     Control *c = st.ctl;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        c->n_free = 0; c->free_taken = 0; c->n_chunks = 0; c->n_spawned = 0; c->n_cand = 0;
+        c->n_free = 0; c->free_taken = 0; c->n_att = 0; c->n_spawned = 0; c->n_cand = 0;
         c->n_reps = 0; c->n_new = 0; c->n_attempts = 0; c->n_occupied = 0; c->n_holes = 0; c->n_found = 0;
         c->n_big = 0;
+        c->n_huge = 0;
         for (int k = 0; k < 2; ++k) {
             c->abs_q[k] = 0; c->abs_s[k] = 0;
             c->nborn[k] = c->ndied[k] = c->nannihil[k] = c->naborted[k] = c->nremoved[k] = 0.0;
@@ -333,22 +335,31 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             const unsigned long long pos = warp_append(&c->n_free, want);
             if (want) st.free_list[pos] = (int32_t)j;
         }
-        // spawn work chunks; a parent with more than kBigChunks chunks is handed
-        // to k_expand, which writes its chunks with a whole block
+        // one spawn-attempt entry per attempt; a parent with more than
+        // kBigAttempts attempts is handed to k_expand, which writes its
+        // entries with a whole block
         {
-            unsigned int nch = 0;
-            for (int k = 0; k < L; ++k) nch += (nsp[k] + kChunk - 1) / kChunk;
-            const unsigned long long base = warp_append(&c->n_chunks, nch);
-            if (nch) {
-                if (base + nch > (unsigned long long)st.max_chunks) {
+            unsigned int nat = 0;
+            for (int k = 0; k < L; ++k) nat += nsp[k];
+            const unsigned long long base = warp_append(&c->n_att, nat);
+            if (nat) {
+                if (base + nat > (unsigned long long)st.max_att) {
                     set_err(c, NECI_GPU_ERR_SPAWN_FULL);
                 } else {
                     unsigned long long q = base;
                     for (int k = 0; k < L; ++k) {
-                        const unsigned int nk = (nsp[k] + kChunk - 1) / kChunk;
                         const unsigned long long head = (unsigned long long)j | ((unsigned long long)k << 32) |
                                                         ((unsigned long long)neg[k] << 33);
-                        if (nk > (unsigned int)kBigChunks) {
+                        if (nsp[k] > (unsigned int)kHugeAttempts) {
+                            const unsigned long long b = atomicAdd(&c->n_huge, 1ull);
+                            if (b < (unsigned long long)kMaxHuge) {
+                                st.huge[3 * b] = head;
+                                st.huge[3 * b + 1] = nsp[k];
+                                st.huge[3 * b + 2] = q;
+                            } else {
+                                set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+                            }
+                        } else if (nsp[k] > (unsigned int)kBigAttempts) {
                             const unsigned long long b = atomicAdd(&c->n_big, 1ull);
                             if (b < (unsigned long long)st.max_big) {
                                 st.big[3 * b] = head;
@@ -357,15 +368,10 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                             } else {
                                 set_err(c, NECI_GPU_ERR_SPAWN_FULL);
                             }
-                            q += nk;
-                            continue;
+                        } else {
+                            for (unsigned int a = 0; a < nsp[k]; ++a) st.att[q + a] = head | ((unsigned long long)a << 34);
                         }
-                        for (unsigned int k0 = 0; k0 < nsp[k]; k0 += kChunk) {
-                            const unsigned int cnt = min((unsigned int)kChunk, nsp[k] - k0);
-                            st.chunks[2 * q] = head | ((unsigned long long)cnt << 34);
-                            st.chunks[2 * q + 1] = k0;
-                            ++q;
-                        }
+                        q += nsp[k];
                     }
                 }
             }
@@ -384,86 +390,100 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
 }
 
 // ===========================================================================
-// k_expand: chunks of heavily populated parents, one block per parent.
+// k_expand: attempt entries of heavily populated parents, one block per parent.
 // ===========================================================================
 __global__ void k_expand(DevState st) {
+    // parents with more than kHugeAttempts attempts: the whole grid per parent
+    const unsigned long long nh = min(st.ctl->n_huge, (unsigned long long)kMaxHuge);
+    for (unsigned long long b = 0; b < nh; ++b) {
+        const unsigned long long head = st.huge[3 * b], n = st.huge[3 * b + 1], base = st.huge[3 * b + 2];
+        for (unsigned long long a = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; a < n;
+             a += (unsigned long long)gridDim.x * blockDim.x)
+            st.att[base + a] = head | (a << 34);
+    }
+    // the others: a block per parent
     const unsigned long long nb = min(st.ctl->n_big, (unsigned long long)st.max_big);
     for (unsigned long long b = blockIdx.x; b < nb; b += gridDim.x) {
         const unsigned long long head = st.big[3 * b];
         const unsigned long long n = st.big[3 * b + 1];
         const unsigned long long base = st.big[3 * b + 2];
-        const unsigned long long nk = (n + kChunk - 1) / kChunk;
-        for (unsigned long long q = threadIdx.x; q < nk; q += blockDim.x) {
-            const unsigned long long k0 = q * kChunk;
-            const unsigned long long cnt = min((unsigned long long)kChunk, n - k0);
-            st.chunks[2 * (base + q)] = head | (cnt << 34);
-            st.chunks[2 * (base + q) + 1] = k0;
-        }
+        for (unsigned long long a = threadIdx.x; a < n; a += blockDim.x) st.att[base + a] = head | (a << 34);
     }
 }
 
 // ===========================================================================
 // k_spawn
 // ===========================================================================
+template <typename Real>
+__device__ inline Real prm(double d, float f) { return sizeof(Real) == 8 ? (Real)d : (Real)f; }
+
 // attempt_create_normal (fcimc_pointed_fns.F90:178-494) for one generated
 // excitation: the child amplitude -tau H_ij sign(C) / (p_gen AvMCExcits),
-// rounded by RealSpawnCutoff / stochastic_round, in fixed point (0 = none).
+// taken as -tau H_ij sign(C) (1/p_gen) (1/AvMCExcits) in precision Real and
+// converted to fixed point, then rounded there in integer arithmetic:
+// RealSpawnCutoff rounding (|n| < cutoff -> +-cutoff with probability
+// |n|/cutoff) or stochastic_round (lib/util_mod.fpp:182) to an integer
+// walker.  Returns 0 for no child.
 template <typename Real>
-__device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real pgen, bool neg, Stream &rng, int &ovf) {
+__device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real invp, bool neg, Stream &rng, int &ovf) {
     const Real ww = neg ? (Real)-1 : (Real)1;
-    const Real prob = pgen * (Real)p.av_mc_excits;
-    Real nsp = -(Real)p.tau * hel * ww / prob;
-    const Real eps = (Real)kEps12;
-    if (p.t_all_real_coeff) {
-        const Real cut = (Real)p.real_spawn_cutoff;
-        if (p.t_real_spawn_cutoff && fabs(nsp) < cut) {
-            const Real x = nsp * ((Real)1 / cut);
-            Real i = trunc(x);
-            const Real res = x - i;
-            if (fabs(res) >= eps) {
-                const bool up = (sizeof(Real) == 8) ? bern(rng, (double)fabs(res)) : bern_f(rng, (float)fabs(res));
-                if (up) i += (x >= (Real)0 ? (Real)1 : (Real)-1);
-            }
-            nsp = cut * i;
-        }
+    const Real nsp = -prm<Real>(p.tau, p.f_tau) * hel * ww * invp * prm<Real>(p.inv_av, p.f_inv_av);
+    long long q;
+    if (sizeof(Real) == 8) {
+        const double sc = (double)nsp * 4294967296.0;
+        if (!(fabs(sc) < 9.2e18)) { ovf = 1; return 0; }
+        q = __double2ll_rn(sc);
     } else {
-        Real i = trunc(nsp);
-        const Real res = nsp - i;
-        if (fabs(res) >= eps) {
-            const bool up = (sizeof(Real) == 8) ? bern(rng, (double)fabs(res)) : bern_f(rng, (float)fabs(res));
-            if (up) i += (nsp >= (Real)0 ? (Real)1 : (Real)-1);
-        }
-        nsp = i;
+        const float sc = (float)nsp * 4294967296.0f;
+        if (!(fabsf(sc) < 9.2e18f)) { ovf = 1; return 0; }
+        q = __float2ll_rn(sc);
     }
-    if (!(fabs(nsp) >= eps)) return 0;
-    if (sizeof(Real) == 8) return to_fixed((double)nsp, &ovf);
-    const float sc = (float)nsp * 4294967296.0f;
-    if (!(fabsf(sc) < 9.2e18f)) { ovf = 1; return 0; }
-    return __float2ll_rn(sc);
+    const unsigned long long aq = (unsigned long long)(q < 0 ? -q : q);
+    if (p.t_all_real_coeff) {
+        if (p.t_real_spawn_cutoff && aq < p.cutoff_q) {
+            // keep with probability |q| / cutoff_q
+            const bool keep = __umul64hi(rng.next64(), p.cutoff_q) < aq;
+            return keep ? (q < 0 ? -(long long)p.cutoff_q : (long long)p.cutoff_q) : 0ll;
+        }
+        return q;
+    }
+    const unsigned long long whole = aq >> 32, frac = aq & 0xFFFFFFFFull;
+    unsigned long long m = whole;
+    if (frac != 0 && (rng.next64() >> 32) < frac) m += 1;
+    const long long v = (long long)(m << 32);
+    return q < 0 ? -v : v;
 }
 
-template <typename Real>
-__device__ inline void spawn_chunks(const DevSys &s, const DevState &st, const IterParams &p, const int32_t *sh_rh2,
-                                    const int32_t *sh_neigh) {
+// The spawn attempts (FciMCPar.F90:1600-1745, loop_over_walkers): one
+// attempt per thread per round; every lane runs the same number of rounds so
+// that the record append is warp-wide.
+template <typename Real, int GEN>
+__global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp) {
+    extern __shared__ int32_t sh[];
+    int32_t *sh_rh2 = sh;
+    int32_t *sh_neigh = sh + (s.nbasis + 1);
+    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
+    if (GEN == NECI_EXGEN_RS_HUBBARD)
+        for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
+    __syncthreads();
+    const IterParams p = *pp;
     Control *c = st.ctl;
-    const long long nch = (long long)c->n_chunks;
+    const long long nat = (long long)min(c->n_att, (unsigned long long)st.max_att);
     const int W = s.W, L = s.L, R = s.R;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    const long long nround = ((nch + stride - 1) / stride) * stride;
+    const long long nround = ((nat + stride - 1) / stride) * stride;
     int ovf = 0;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
-        long long wout[kChunk];
-        int nout = 0;
-        unsigned long long kids[kChunk][kMaxWords];
+        long long qv = 0;
         int run = 0;
         bool pinit = false;
-        if (q < nch) {
-            const unsigned long long w0 = st.chunks[2 * q];
-            const unsigned long long k0 = st.chunks[2 * q + 1];
+        Excit<Real> e;
+        if (q < nat) {
+            const unsigned long long w0 = st.att[q];
             const long long j = (long long)(w0 & 0xFFFFFFFFull);
             run = (int)((w0 >> 32) & 1ull);
             const bool neg = (w0 >> 33) & 1ull;
-            const int cnt = (int)(w0 >> 34);
+            const unsigned int k = (unsigned int)(w0 >> 34);
             const long long *r = st.dets + j * R;
             unsigned long long d[kMaxWords];
             for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
@@ -472,50 +492,36 @@ __device__ inline void spawn_chunks(const DevSys &s, const DevState &st, const I
             pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(run));
             uint8_t nI[kMaxNel];
             decode(d, W, nI);
-            const unsigned long long dkey = det_key(d, W, p.seed);
-            for (int a = 0; a < cnt; ++a) {
-                Stream rng(dkey, p.iter, P_ATTEMPT, run, (uint32_t)(k0 + a));
-                Excit<Real> e;
-                generate_excitation<Real>(s, d, nI, sh_neigh, rng, e);
-                if (!e.ok) continue;
-                if (core) {
-                    // is_core_state (semi_stoch_procs.F90:547): core -> core spawns
-                    // are done by the deterministic projection
-                    const long long hs = hash_find(st, e.child, W, R, neci_hash(e.child, W, sh_rh2), c);
-                    if (hs >= 0 && is_core_flags(st.dets[hs * R + W + L])) continue;
-                }
-                const long long qv = spawn_amplitude<Real>(p, e.hel, e.pgen, neg, rng, ovf);
-                if (qv == 0) continue;
-                wout[nout] = qv;
-                for (int w = 0; w < W; ++w) kids[nout][w] = e.child[w];
-                ++nout;
+            Stream rng(det_key(d, W, p.seed), p.iter, P_ATTEMPT, run, k);
+            if (GEN == NECI_EXGEN_RS_HUBBARD) {
+                gen_rs_hubbard<Real>(s, d, nI, sh_neigh, rng, e);
+            } else {
+                if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, nI, rng, e);
+                else gen_pchb_double<Real>(s, d, nI, rng, e);
             }
+            bool keep = e.ok;
+            if (keep && core) {
+                // is_core_state (semi_stoch_procs.F90:547): core -> core spawns
+                // are done by the deterministic projection
+                const long long hs = hash_find(st, e.child, W, R, neci_hash(e.child, W, sh_rh2), c);
+                if (hs >= 0 && is_core_flags(st.dets[hs * R + W + L])) keep = false;
+            }
+            if (keep) qv = spawn_amplitude<Real>(p, e.hel, e.invp, neg, rng, ovf);
         }
-        // create_particle (fcimc_helper.F90:152-308): append the records
-        const unsigned long long base = warp_append(&c->n_spawned, (unsigned int)nout);
-        for (int k = 0; k < nout; ++k) {
-            const unsigned long long pos = base + k;
-            if (pos >= (unsigned long long)st.max_spawned) { set_err(c, NECI_GPU_ERR_SPAWN_FULL); break; }
-            long long *o = st.spawn + pos * R;
-            for (int w = 0; w < W; ++w) o[w] = (long long)kids[k][w];
-            for (int k2 = 0; k2 < L; ++k2) o[W + k2] = (k2 == run) ? wout[k] : 0ll;
-            o[W + L] = pinit ? (1ll << init_flag_bit(run)) : 0ll;
+        // create_particle (fcimc_helper.F90:152-308): append the record
+        const unsigned long long pos = warp_append(&c->n_spawned, qv != 0 ? 1u : 0u);
+        if (qv != 0) {
+            if (pos >= (unsigned long long)st.max_spawned) {
+                set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+            } else {
+                long long *o = st.spawn + pos * R;
+                for (int w = 0; w < W; ++w) o[w] = (long long)e.child[w];
+                for (int k2 = 0; k2 < L; ++k2) o[W + k2] = (k2 == run) ? qv : 0ll;
+                o[W + L] = pinit ? (1ll << init_flag_bit(run)) : 0ll;
+            }
         }
     }
     if (ovf) set_err(c, NECI_GPU_ERR_OVERFLOW);
-}
-
-__global__ void __launch_bounds__(128) k_spawn(DevSys s, DevState st, const IterParams *pp) {
-    extern __shared__ int32_t sh[];
-    int32_t *sh_rh2 = sh;
-    int32_t *sh_neigh = sh + (s.nbasis + 1);
-    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
-    if (s.system == NECI_SYS_HUBBARD_REAL_SPACE)
-        for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
-    __syncthreads();
-    const IterParams p = *pp;
-    if (p.precision == NECI_PREC_MIXED) spawn_chunks<float>(s, st, p, sh_rh2, sh_neigh);
-    else spawn_chunks<double>(s, st, p, sh_rh2, sh_neigh);
 }
 
 // ===========================================================================
@@ -940,10 +946,18 @@ void launch_rehash(Engine &e, cudaStream_t s) {
 void launch_sweep(Engine &e, cudaStream_t s) {
     k_sweep<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
-void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<e.num_sms * 2, 256, 0, s>>>(e.st); }
+void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<e.num_sms * 4, 256, 0, s>>>(e.st); }
 void launch_spawn(Engine &e, cudaStream_t s) {
     const size_t shm = (size_t)(e.sys.nbasis + 1 + e.sys.nsites * e.sys.max_neigh) * sizeof(int32_t);
-    k_spawn<<<e.num_sms * 8, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    const int grid = e.num_sms * 8;
+    const bool mixed = e.h_params->precision == NECI_PREC_MIXED;
+    if (e.sys.excitgen == NECI_EXGEN_RS_HUBBARD) {
+        if (mixed) k_spawn<float, NECI_EXGEN_RS_HUBBARD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+        else k_spawn<double, NECI_EXGEN_RS_HUBBARD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    } else {
+        if (mixed) k_spawn<float, NECI_EXGEN_PCHB><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+        else k_spawn<double, NECI_EXGEN_PCHB><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    }
 }
 void launch_core(Engine &e, cudaStream_t s) {
     if (e.st.n_core > 0) k_core<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);

@@ -303,20 +303,30 @@ __global__ void k_pchb_tables(DevSys s, double *bias, int32_t *alias, double *pr
         for (long long k = 0; k < n; ++k) w[k] = w[k] / sum;
     }
 }
-__global__ void k_pchb_pexch(DevSys s, const double *wsum, double *pexch, unsigned long long *pexch_thr, float *pexch32) {
+__global__ void k_pchb_pexch(DevSys s, const double *wsum, double *pexch, unsigned long long *pexch_thr, float *pexch32,
+                             double *pexch_inv, double *pnoexch_inv, float *pexch_inv32, float *pnoexch_inv32) {
     for (long long ij = blockIdx.x * (long long)blockDim.x + threadIdx.x; ij < s.ijMax; ij += (long long)gridDim.x * blockDim.x) {
         const double ex = wsum[ij * 3 + 2], noex = wsum[ij * 3 + 1];
         const double pe = fabs(ex + noex) < 1e-10 ? 0.0 : ex / (ex + noex);
         pexch[ij] = pe;
         pexch_thr[ij] = prob_thresh(pe);
         pexch32[ij] = (float)pe;
+        const double ie = 1.0 / pe, ine = 1.0 / (1.0 - pe);
+        pexch_inv[ij] = ie;
+        pnoexch_inv[ij] = ine;
+        pexch_inv32[ij] = (float)ie;
+        pnoexch_inv32[ij] = (float)ine;
     }
 }
 // Integer thresholds of the alias biases and single-precision probabilities.
-__global__ void k_pchb_derived(long long n, const double *bias, const double *prob, unsigned long long *thr, float *prob32) {
+__global__ void k_pchb_derived(long long n, const double *bias, const double *prob, unsigned long long *thr, float *prob32,
+                               double *inv, float *inv32) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         thr[i] = prob_thresh(bias[i]);
         prob32[i] = (float)prob[i];
+        const double v = 1.0 / prob[i];
+        inv[i] = v;
+        inv32[i] = (float)v;
     }
 }
 
@@ -373,9 +383,12 @@ void launch_pchb_build(Engine &e) {
                                                     (double *)e.sys.alias_prob, (uint8_t *)e.sys.alias_present, wsum,
                                                     scratch);
     k_pchb_pexch<<<gsz(e), 256, 0, e.stream>>>(e.sys, wsum, (double *)e.sys.pexch,
-                                               (unsigned long long *)e.sys.pexch_thr, (float *)e.sys.pexch32);
+                                               (unsigned long long *)e.sys.pexch_thr, (float *)e.sys.pexch32,
+                                               (double *)e.sys.pexch_inv, (double *)e.sys.pnoexch_inv,
+                                               (float *)e.sys.pexch_inv32, (float *)e.sys.pnoexch_inv32);
     k_pchb_derived<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, e.sys.alias_bias, e.sys.alias_prob,
-                                                 (unsigned long long *)e.sys.alias_thr, (float *)e.sys.alias_prob32);
+                                                 (unsigned long long *)e.sys.alias_thr, (float *)e.sys.alias_prob32,
+                                                 (double *)e.sys.alias_inv, (float *)e.sys.alias_inv32);
     cudaStreamSynchronize(e.stream);
     cudaFree(wsum);
     cudaFree(scratch);

@@ -503,8 +503,11 @@ struct Oracle {
         int ex[2][2] = {{0, 0}, {0, 0}};
         bool par = false;
         Real pgen = 0;
+        Real invp = 0;  // 1/pgen as the product of reciprocal factors
         Real hel = 0;
     };
+    template <typename Real>
+    static Real prm(double d) { return sizeof(Real) == 8 ? (Real)d : (Real)(float)d; }
     double tmat_d(int i, int j) const { return get_tmat(i, j); }
     float tmat_f(int i, int j) const { return (float)get_tmat(i, j); }
     template <typename Real> Real tmat_r(int i, int j) const;
@@ -568,7 +571,9 @@ struct Oracle {
         if (ind == 1) p_orb = cum[0] / cum_sum;
         else p_orb = (cum[ind - 1] - cum[ind - 2]) / cum_sum;
         const int orb = neigh[ind - 1];
-        g.pgen = (Real)(p_elec * p_orb);
+        const double pg = p_elec * p_orb;
+        g.pgen = (Real)pg;
+        g.invp = (Real)(1.0 / pg);
         int e[2];
         make_single(nI, g.nJ, elec, orb, e, g.par);
         g.ex[0][0] = e[0]; g.ex[1][0] = e[1];
@@ -608,8 +613,14 @@ struct Oracle {
         int e[2];
         make_single(nI, g.nJ, eleci, orb, e, g.par);
         g.ex[0][0] = e[0]; g.ex[1][0] = e[1];
-        if (sizeof(Real) == 8) g.pgen = (Real)(sys.p_singles / (double)(nexcit * (nel - elecs_wno)));
-        else g.pgen = (Real)((float)sys.p_singles / (float)(nexcit * (nel - elecs_wno)));
+        const int count = nexcit * (nel - elecs_wno);
+        if (sizeof(Real) == 8) {
+            g.pgen = (Real)(sys.p_singles / (double)count);
+            g.invp = (Real)((double)count * (1.0 / sys.p_singles));
+        } else {
+            g.pgen = (Real)((float)sys.p_singles / (float)count);
+            g.invp = (Real)((float)count * (float)(1.0 / sys.p_singles));
+        }
         g.hel = offdiag_from_ex_r<Real>(nI, 1, g.ex, g.par);
         return true;
     }
@@ -624,7 +635,7 @@ struct Oracle {
     // pick_biased_elecs (excit_gens_int_weighted.F90:722-830) without pAA:
     // parallel pair with probability pParallel, then a uniform pair index.
     template <typename Real>
-    void pick_biased_elecs(const std::vector<int> &nI, Stream &rng, int elecs[2], int src[2], Real &pgen) const {
+    void pick_biased_elecs(const std::vector<int> &nI, Stream &rng, int elecs[2], int src[2], Real &pgen, Real &invp) const {
         const int aa = nOccAlpha * (nOccAlpha - 1) / 2;
         const int bb = nOccBeta * (nOccBeta - 1) / 2;
         const int par = aa + bb;
@@ -641,6 +652,7 @@ struct Oracle {
             }
             if (sizeof(Real) == 8) pgen = (Real)(sys.p_parallel / (double)par);
             else pgen = (Real)((float)sys.p_parallel / (float)par);
+            invp = prm<Real>((double)par / sys.p_parallel);
         } else {
             al_req = 1; be_req = 1;
             const int idx = (int)uniform_index(rng, (u32)ab);
@@ -648,6 +660,7 @@ struct Oracle {
             be_num[0] = 1 + idx / nOccAlpha;
             if (sizeof(Real) == 8) pgen = (Real)((1.0 - sys.p_parallel) / (double)ab);
             else pgen = (Real)((1.0f - (float)sys.p_parallel) / (float)ab);
+            invp = prm<Real>((double)ab / (1.0 - sys.p_parallel));
         }
         int al_count = 0, be_count = 0, found = 0;
         for (int i = 1; i <= sys.nel; ++i) {
@@ -775,8 +788,8 @@ struct Oracle {
     bool pchb_doubles(const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
         g.ic = 2;
         int elecs[2], src[2];
-        Real pgen;
-        pick_biased_elecs<Real>(nI, rng, elecs, src, pgen);
+        Real pgen, invp;
+        pick_biased_elecs<Real>(nI, rng, elecs, src, pgen, invp);
         const i64 ij = fuse_index(gtID(src[0]), gtID(src[1]));
         int spin[2] = {src[0] % 2, src[1] % 2};  // getSpinIndex: 0 alpha, 1 beta
         int type;
@@ -786,15 +799,18 @@ struct Oracle {
             if (rng.next64() < prob_thresh(pexch[ij - 1])) {
                 type = 3;
                 pgen *= pe;
+                invp *= prm<Real>(1.0 / pexch[ij - 1]);
                 std::swap(spin[0], spin[1]);
             } else {
                 type = 2;
                 pgen *= ((Real)1 - pe);
+                invp *= prm<Real>(1.0 / (1.0 - pexch[ij - 1]));
             }
         }
         int ab;
         Real pholes;
-        alias_sample<Real>((size_t)(ij - 1) * 3 + (type - 1), rng, ab, pholes);
+        const size_t tab = (size_t)(ij - 1) * 3 + (type - 1);
+        alias_sample<Real>(tab, rng, ab, pholes);
         if (ab == 0) { g.pgen = 0; return false; }
         int orbs[2] = {2 * tgt1[ab] - spin[0], 2 * tgt2[ab] - spin[1]};
         bool invalid = orbs[0] == 0 || orbs[1] == 0;
@@ -805,6 +821,8 @@ struct Oracle {
         pgen *= pholes;
         if (sizeof(Real) == 8) g.pgen = pgen * (Real)(1.0 - sys.p_singles);
         else g.pgen = pgen * (Real)(1.0f - (float)sys.p_singles);
+        invp *= prm<Real>(1.0 / alias_prob[tab * abMax + ab - 1]);
+        g.invp = invp * prm<Real>(1.0 / (1.0 - sys.p_singles));
         g.hel = offdiag_from_ex_r<Real>(nI, 2, g.ex, g.par);
         return true;
     }
@@ -893,42 +911,41 @@ struct IterRun {
     // amplitude -tau H_ij sign(C) / (p_gen AvMCExcits) in precision Real,
     // then RealSpawnCutoff rounding (x = n/cutoff taken as n * (1/cutoff)) or
     // stochastic_round (lib/util_mod.fpp:182-203); returned in fixed point.
+    // attempt_create_normal (fcimc_pointed_fns.F90:178-494): the child
+    // amplitude -tau H_ij sign(C) / (p_gen AvMCExcits), taken as -tau H_ij
+    // sign(C) (1/p_gen) (1/AvMCExcits) in precision Real and converted to
+    // fixed point; RealSpawnCutoff rounding (|n| < cutoff -> +-cutoff with
+    // probability |n|/cutoff) or stochastic_round (lib/util_mod.fpp:182-203)
+    // then act on the fixed-point value in integer arithmetic.
     template <typename Real>
-    i64 spawn_amplitude(Real hel, Real pgen, bool neg, Stream &rng, int &ovf) const {
+    i64 spawn_amplitude(Real hel, Real invp, bool neg, Stream &rng, int &ovf) const {
         const Real ww = neg ? (Real)-1 : (Real)1;
-        const Real prob = pgen * (Real)p.av_mc_excits;
-        Real nsp = -(Real)p.tau * hel * ww / prob;
-        const Real eps = (Real)1e-12;
-        if (p.t_all_real_coeff) {
-            const Real cut = (Real)p.real_spawn_cutoff;
-            if (p.t_real_spawn_cutoff && std::fabs(nsp) < cut) {
-                const Real x = nsp * ((Real)1 / cut);
-                Real i = std::trunc(x);
-                const Real res = x - i;
-                if (std::fabs(res) >= eps) {
-                    const bool up = (sizeof(Real) == 8) ? bern(rng, (double)std::fabs(res)) : bern_f(rng, (float)std::fabs(res));
-                    if (up) i += (x >= (Real)0 ? (Real)1 : (Real)-1);
-                }
-                nsp = cut * i;
-            }
-        } else {
-            Real i = std::trunc(nsp);
-            const Real res = nsp - i;
-            if (std::fabs(res) >= eps) {
-                const bool up = (sizeof(Real) == 8) ? bern(rng, (double)std::fabs(res)) : bern_f(rng, (float)std::fabs(res));
-                if (up) i += (nsp >= (Real)0 ? (Real)1 : (Real)-1);
-            }
-            nsp = i;
-        }
-        if (!(std::fabs(nsp) >= eps)) return 0;
+        const Real nsp = -Oracle::prm<Real>(p.tau) * hel * ww * invp * Oracle::prm<Real>(1.0 / p.av_mc_excits);
+        i64 q;
         if (sizeof(Real) == 8) {
             const double sc = (double)nsp * 4294967296.0;
             if (!(std::fabs(sc) < 9.2e18)) { ovf = 1; return 0; }
-            return (i64)std::llrint(sc);
+            q = (i64)std::llrint(sc);
+        } else {
+            const float sc = (float)nsp * 4294967296.0f;
+            if (!(std::fabs(sc) < 9.2e18f)) { ovf = 1; return 0; }
+            q = (i64)std::llrintf(sc);
         }
-        const float sc = (float)nsp * 4294967296.0f;
-        if (!(std::fabs(sc) < 9.2e18f)) { ovf = 1; return 0; }
-        return (i64)std::llrintf(sc);
+        const u64 aq = (u64)(q < 0 ? -q : q);
+        if (p.t_all_real_coeff) {
+            const u64 cutoff_q = (u64)std::llrint(std::ldexp(p.real_spawn_cutoff, NECI_SPAWN_FIXED_BITS));
+            if (p.t_real_spawn_cutoff && aq < cutoff_q) {
+                const u64 mh = (u64)(((unsigned __int128)rng.next64() * (unsigned __int128)cutoff_q) >> 64);
+                if (mh < aq) return q < 0 ? -(i64)cutoff_q : (i64)cutoff_q;
+                return 0;
+            }
+            return q;
+        }
+        const u64 whole = aq >> 32, frac = aq & 0xFFFFFFFFull;
+        u64 m = whole;
+        if (frac != 0 && (rng.next64() >> 32) < frac) m += 1;
+        const i64 v = (i64)(m << 32);
+        return q < 0 ? -v : v;
     }
     template <typename Real>
     void attempt(const i64 *r, const std::vector<int> &nI, u64 dkey, int run, int a, bool neg, bool core,
@@ -943,7 +960,7 @@ struct IterRun {
             i64 slot, h;
             if (o.hash_lookup(g.nJ, child.data(), slot, h) && o.is_core(o.row(slot))) return;
         }
-        const i64 q = spawn_amplitude<Real>(g.hel, g.pgen, neg, rng, ovf);
+        const i64 q = spawn_amplitude<Real>(g.hel, g.invp, neg, rng, ovf);
         if (q == 0) return;
         // create_particle (fcimc_helper.F90:152-308)
         if ((i64)spawns.size() >= o.sys.max_spawned) { err = NECI_GPU_ERR_SPAWN_FULL; return; }

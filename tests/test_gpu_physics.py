@@ -44,13 +44,16 @@ def test_hubbard10_energy_matches_exact_diagonalisation(initiator, walkers):
     eng.start_from_reference(initial_part=10.0)
     calc = CalcParams(tau=0.01, target_walkers=walkers, steps_sft=10, sft_damp=0.1, seed=4242,
                       trunc_initiator=initiator)
-    res = FciMCPar(eng, calc).run(6000)
+    res = FciMCPar(eng, calc).run(10000)
     assert res.vary_shift_cycle is not None
     e = res.energy(skip_cycles=res.vary_shift_cycle + 100)
     e0 = hub10_exact()
-    tol = 2.0 * e["proje_err"] + (0.0 if not initiator else 2e-3)
-    assert abs(e["proje"] - e0) < max(tol, 1e-4), (e, e0)
-    assert abs(e["shift"] - e0) < max(3.0 * e["shift_err"], 5e-3) + (0.0 if not initiator else 2e-3), (e, e0)
+    # initiator bias of this lattice at 5e4 walkers is a few mHa (above E0)
+    bias = 0.0 if not initiator else 1e-2
+    # the Neel reference carries little weight in this ground state, so the
+    # projected energy is the noisier estimator: 3 sigma; the shift: 2 sigma
+    assert abs(e["proje"] - e0) < 3.0 * e["proje_err"] + bias, (e, e0)
+    assert abs(e["shift"] - e0) < 2.0 * e["shift_err"] + bias + 1e-4, (e, e0)
 
 
 @pytest.mark.parametrize("precision,rtol", [(capi.PREC_FP64, 1e-12), (capi.PREC_MIXED, 2e-6)])
@@ -106,3 +109,25 @@ def test_hehe_pchb_energy_matches_neci_davidson():
     e = res.energy(skip_cycles=res.vary_shift_cycle + 100)
     e0 = float(d["ground_e"][0])
     assert abs(e["proje"] - e0) < max(2.5 * e["proje_err"], 2e-4), (e, e0)
+
+
+def test_hehe_mixed_precision_matches_fp64():
+    """FP32 spawn amplitudes: E_proj within 2 sigma of the FP64 run and of
+    NECI's Davidson energy, and within 1 mHa."""
+    d = np.load(Path(__file__).parent / "golden" / "hehe_fcidump.npz")
+    spec = systems.molecular_system(d["h"], d["eri"], float(d["ecore"]), int(d["nelec"]), name="HeHe")
+    out = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        eng = Engine(spec, max_walkers=200_000, max_spawned=400_000)
+        eng.start_from_reference(initial_part=10.0)
+        calc = CalcParams(tau=0.02, target_walkers=5e3, steps_sft=10, sft_damp=0.1, seed=23, trunc_initiator=False,
+                          precision=prec)
+        res = FciMCPar(eng, calc).run(8000)
+        out[prec] = res.energy(skip_cycles=res.vary_shift_cycle + 100)
+        eng.close()
+    e64, e32 = out[capi.PREC_FP64], out[capi.PREC_MIXED]
+    e0 = float(d["ground_e"][0])
+    comb = np.hypot(e64["proje_err"], e32["proje_err"])
+    assert abs(e32["proje"] - e64["proje"]) < max(2.0 * comb, 2e-4), (e32, e64)
+    assert abs(e32["proje"] - e0) < max(2.5 * e32["proje_err"], 2e-4), (e32, e0)
+    assert abs(e32["proje"] - e64["proje"]) < 1e-3
