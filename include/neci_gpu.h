@@ -206,6 +206,35 @@ int32_t neci_gpu_annihilate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *param
 int32_t neci_gpu_compress_spawns(neci_gpu_ctx *ctx, const int64_t *spawned, int64_t n_spawned,
                                  int64_t *out, int64_t *n_out, double *nannihil);
 
+/* CompressSpawnedList for callers that cannot allocate memory.  This entry
+ * point has no counterpart in the reference.  It is for hosts that may not
+ * call cudaMalloc (code running inside another program's memory pool, or a
+ * process that must not grow its GPU footprint after start-up): it needs no
+ * context and allocates nothing, host or device.  Its scratch (hash table and
+ * per-determinant sums) is a fixed set of file-scope device arrays, about
+ * 10 MB, that every GPU which loads the library holds until the process exits.
+ *   d_spawned  n rows in SpawnedParts layout, in device memory (read only)
+ *   n          at most 262144 (2^18) rows per call; larger n returns
+ *              NECI_GPU_ERR_INVALID with a message in errbuf
+ *   d_out      device memory for up to n rows: the compressed list, one row
+ *              per determinant with a non-zero summed amplitude, in no
+ *              particular order (neci_gpu_compress_spawns returns the same
+ *              rows sorted by ilut_lt)
+ *   n_out, nannihil (lenof_sign doubles, may be NULL): host memory
+ *   stream     cudaStream_t to run on (NULL: the legacy default stream); the
+ *              call synchronises it before returning
+ *   errbuf     caller-owned buffer for an error message (may be NULL)
+ * The current device is used.  The first call on each device looks up the
+ * device addresses of the scratch arrays (cudaGetSymbolAddress) and should
+ * come before any stream capture.  Every call on a device shares the same
+ * scratch: it is cleared at the start of each call, and calls that overlap on
+ * the GPU race. */
+int32_t neci_gpu_compress_spawns_noalloc(const int64_t *d_spawned, int64_t n, int32_t nifd,
+                                         int32_t lenof_sign, int32_t t_trunc_initiator,
+                                         int32_t t_init_coherent_rule, int64_t *d_out, int64_t *n_out,
+                                         double *nannihil, void *stream, char *errbuf,
+                                         int32_t errbuf_len);
+
 /* ---- bit-string and matrix-element kernels (batch forms) ---------------
  * FindWalkerHash (hash.F90:23-38) of n determinants for a table of
  * table_len buckets: out[i] in 1..table_len.                             */
