@@ -271,6 +271,34 @@ __device__ inline int occ_between(const unsigned long long *d, int W, int lo, in
     }
     return n;
 }
+// Orbital (1-based) of the n-th (1-based) set bit of (d & pattern), counting
+// from orbital 1 upwards: the n-th electron of that spin class in nI order.
+__device__ inline int nth_orbital(const unsigned long long *d, int W, unsigned long long pattern, int n) {
+    for (int w = 0; w < W; ++w) {
+        unsigned long long x = d[w] & pattern;
+        const int c = __popcll(x);
+        if (n > c) { n -= c; continue; }
+        int k = n - 1, pos = 0;
+        int t = __popc((unsigned int)x);
+        if (k >= t) { k -= t; x >>= 32; pos += 32; }
+        t = __popc((unsigned int)(x & 0xFFFFull));
+        if (k >= t) { k -= t; x >>= 16; pos += 16; }
+        t = __popc((unsigned int)(x & 0xFFull));
+        if (k >= t) { k -= t; x >>= 8; pos += 8; }
+        t = __popc((unsigned int)(x & 0xFull));
+        if (k >= t) { k -= t; x >>= 4; pos += 4; }
+        t = __popc((unsigned int)(x & 0x3ull));
+        if (k >= t) { k -= t; x >>= 2; pos += 2; }
+        t = (int)(x & 1ull);
+        if (k >= t) { pos += 1; }
+        return w * 64 + pos + 1;
+    }
+    return 0;
+}
+constexpr unsigned long long kAllBits = ~0ull;
+constexpr unsigned long long kAlphaBits = 0xAAAAAAAAAAAAAAAAull;  // even orbitals
+constexpr unsigned long long kBetaBits = 0x5555555555555555ull;   // odd orbitals
+
 // decode_bit_det: ascending occupied orbitals.
 __device__ inline int decode(const unsigned long long *d, int W, uint8_t *nI) {
     int n = 0;

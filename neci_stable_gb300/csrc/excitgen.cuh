@@ -93,12 +93,12 @@ __device__ inline void finish_single(const DevSys &s, const unsigned long long *
 // create_cum_list_rs_hubbard (:2080) and pick_from_cum_list
 // (lattice_models_utils.F90:150).  The cumulative pick stays in FP64.
 template <typename Real>
-__device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
+__device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long *d,
                                       const int32_t *neigh, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
     e.ok = false;
     const int elec = 1 + (int)uniform_index(rng, (unsigned)s.nel);
-    const int src = nI[elec - 1];
+    const int src = nth_orbital(d, s.W, kAllBits, elec);  // nI(elec)
     const int site = spat(src);
     int orbs[kMaxNeigh];
     double cum[kMaxNeigh];
@@ -133,8 +133,7 @@ __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long 
 // tCycleOrbs = .false. (rejection for the electron and for the hole).
 // Returns the full single pgen, pSingles / (NExcit * (nel - ElecsWNoExcits)).
 template <typename Real>
-__device__ inline void gen_uniform_single(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                          Stream &rng, Excit<Real> &e) {
+__device__ inline void gen_uniform_single(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
     e.ok = false;
     const int norbs = s.nbasis / 2;
@@ -146,10 +145,11 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
     const int nun_a = norbs - nalpha, nun_b = norbs - nbeta;
     const int elecs_wno = (nun_a == 0 ? nalpha : 0) + (nun_b == 0 ? nbeta : 0);
     if (elecs_wno == s.nel) { e.pgen = 0; return; }
-    int eleci = 0, ispn = 0, nexcit = 0;
+    int eleci = 0, ispn = 0, nexcit = 0, src = 0;
     for (int attempts = 0; attempts <= 250; ++attempts) {
         eleci = (int)uniform_index(rng, (unsigned)s.nel) + 1;
-        ispn = beta(nI[eleci - 1]) ? 2 : 1;
+        src = nth_orbital(d, s.W, kAllBits, eleci);  // nI(eleci)
+        ispn = beta(src) ? 2 : 1;
         nexcit = (ispn == 1) ? nun_a : nun_b;
         if (nexcit != 0) break;
     }
@@ -170,7 +170,7 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
         e.pgen = (Real)(s.f_p_singles / (float)count);
         e.invp = (Real)((float)count * s.f_inv_psingles);
     }
-    finish_single<Real>(s, d, nI[eleci - 1], orb, e);
+    finish_single<Real>(s, d, src, orb, e);
     e.ok = true;
 }
 
@@ -178,7 +178,9 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
 // index idx (pick_biased_elecs' ceiling((1+sqrt(9+8 idx))/2), in integers):
 // returns a1 > a2 >= 1 with idx = (a1-1)(a1-2)/2 + a2 - 1.
 __device__ inline void tri_pair(int idx, int &a1, int &a2) {
-    int a = 2;
+    // smallest a with a(a-1)/2 > idx, from a float estimate corrected exactly
+    int a = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)idx)) * 0.5f) + 1;
+    while (a > 2 && (a - 1) * (a - 2) / 2 > idx) --a;
     while (a * (a - 1) / 2 <= idx) ++a;
     a1 = a;
     a2 = idx + 1 - ((a - 1) * (a - 2)) / 2;
@@ -189,8 +191,7 @@ __device__ inline void tri_pair(int idx, int &a1, int &a2) {
 // (excit_gens_int_weighted.F90:722-830).  Returns the full double pgen
 // (times pDoubles).
 template <typename Real>
-__device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                       Stream &rng, Excit<Real> &e) {
+__device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 2;
     e.ok = false;
     const bool dbl = sizeof(Real) == 8;
@@ -217,19 +218,21 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
         pgen = dbl ? (Real)s.pgen_opp : (Real)s.f_pgen_opp;
         invp = dbl ? (Real)s.inv_opp : (Real)s.f_inv_opp;
     }
-    int elecs[2] = {0, 0}, found = 0, al_count = 0, be_count = 0;
-    for (int i = 1; i <= s.nel; ++i) {
-        if (!beta(nI[i - 1])) {
-            ++al_count;
-            if (al_req > 0 && al_count == al_num[al_req - 1]) { elecs[found++] = i; --al_req; }
-        } else {
-            ++be_count;
-            if (be_req > 0 && be_count == be_num[be_req - 1]) { elecs[found++] = i; --be_req; }
-        }
-        if (al_req == 0 && be_req == 0) break;
+    // the al_num/be_num-th alpha/beta electrons in nI order, lower orbital first
+    int src0, src1;
+    if (al_req == 2) {
+        src0 = nth_orbital(d, s.W, kAlphaBits, al_num[1]);
+        src1 = nth_orbital(d, s.W, kAlphaBits, al_num[0]);
+    } else if (be_req == 2) {
+        src0 = nth_orbital(d, s.W, kBetaBits, be_num[1]);
+        src1 = nth_orbital(d, s.W, kBetaBits, be_num[0]);
+    } else {
+        const int oa = nth_orbital(d, s.W, kAlphaBits, al_num[0]);
+        const int ob = nth_orbital(d, s.W, kBetaBits, be_num[0]);
+        src0 = min(oa, ob);
+        src1 = max(oa, ob);
     }
-    if (found < 2) { e.pgen = 0; return; }
-    const int src0 = nI[elecs[0] - 1], src1 = nI[elecs[1] - 1];
+    if (src0 == 0 || src1 == 0) { e.pgen = 0; return; }
     const long long i1 = spat(src0), j1 = spat(src1);
     const long long ij = i1 < j1 ? i1 + j1 * (j1 - 1) / 2 : j1 + i1 * (i1 - 1) / 2;
     int spin0 = src0 & 1, spin1 = src1 & 1;
@@ -284,14 +287,14 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
 
 // gen_exc_sd (excitation_generators.F90:110-133): singles with pSingles.
 template <typename Real>
-__device__ inline void generate_excitation(const DevSys &s, const unsigned long long *d, const uint8_t *nI,
-                                           const int32_t *neigh, Stream &rng, Excit<Real> &e) {
+__device__ inline void generate_excitation(const DevSys &s, const unsigned long long *d, const int32_t *neigh,
+                                           Stream &rng, Excit<Real> &e) {
     if (s.excitgen == NECI_EXGEN_RS_HUBBARD) {
-        gen_rs_hubbard<Real>(s, d, nI, neigh, rng, e);
+        gen_rs_hubbard<Real>(s, d, neigh, rng, e);
         return;
     }
-    if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, nI, rng, e);
-    else gen_pchb_double<Real>(s, d, nI, rng, e);
+    if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, rng, e);
+    else gen_pchb_double<Real>(s, d, rng, e);
 }
 
 }  // namespace neci

@@ -490,14 +490,12 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
             const long long flags = r[W + L];
             const bool core = st.n_core > 0 && is_core_flags(flags);
             pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(run));
-            uint8_t nI[kMaxNel];
-            decode(d, W, nI);
             Stream rng(det_key(d, W, p.seed), p.iter, P_ATTEMPT, run, k);
             if (GEN == NECI_EXGEN_RS_HUBBARD) {
-                gen_rs_hubbard<Real>(s, d, nI, sh_neigh, rng, e);
+                gen_rs_hubbard<Real>(s, d, sh_neigh, rng, e);
             } else {
-                if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, nI, rng, e);
-                else gen_pchb_double<Real>(s, d, nI, rng, e);
+                if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, rng, e);
+                else gen_pchb_double<Real>(s, d, rng, e);
             }
             bool keep = e.ok;
             if (keep && core) {

@@ -36,13 +36,11 @@ __global__ void k_util_gen_excit(DevSys s, const long long *det, long long n, un
                                  long long *child, double *pgen, double *hel) {
     unsigned long long d[kMaxWords];
     for (int w = 0; w < s.W; ++w) d[w] = (unsigned long long)det[w];
-    uint8_t nI[kMaxNel];
-    decode(d, s.W, nI);
     const unsigned long long dkey = det_key(d, s.W, seed);
     for (long long a = blockIdx.x * (long long)blockDim.x + threadIdx.x; a < n; a += (long long)gridDim.x * blockDim.x) {
         Stream rng(dkey, iter, P_ATTEMPT, 0, (uint32_t)a);
         Excit<double> e;
-        generate_excitation<double>(s, d, nI, s.neighbours, rng, e);
+        generate_excitation<double>(s, d, s.neighbours, rng, e);
         for (int w = 0; w < s.W; ++w) child[a * s.W + w] = e.ok ? (long long)e.child[w] : 0ll;
         pgen[a] = e.ok ? e.pgen : 0.0;
         hel[a] = e.ok ? e.hel : 0.0;
