@@ -201,6 +201,87 @@ def run_gpu(args, rank, world):
     }
 
 
+def batched_specs(n_inst=64, base_seed=7000):
+    """Instances of the synthetic FCIDUMP recipe with instance-indexed seeds:
+    n ~ U{12..40} spatial orbitals, even nel ~ U{6..20} (Sz = 0), target
+    walkers log-uniform in [1e4, 1e6], each a replica pair (lenof_sign 2)."""
+    import numpy as np
+    from neci_stable_gb300 import systems
+    rng = np.random.default_rng(base_seed)
+    out = []
+    for i in range(n_inst):
+        n = int(rng.integers(12, 41))
+        nel = int(2 * rng.integers(3, 11))
+        nel = min(nel, n)  # at most half filling of each spin
+        walkers = float(10 ** rng.uniform(4.0, 6.0))
+        h, eri, ecore = systems.synthetic_fcidump(n, base_seed + i)
+        spec = systems.molecular_system(h, eri, ecore, nel, seed=base_seed + 1000 + i, lenof_sign=2,
+                                        name=f"batch-{i}-n{n}-e{nel}")
+        out.append((spec, walkers))
+    return out
+
+
+def run_batched(args):
+    """Plain FP64 single-instance steps (each instance alone, one after the
+    other) against mixed-precision batched steps (all instances side by side)."""
+    from neci_stable_gb300 import capi
+    from neci_stable_gb300.engine import Engine, iterate_batch
+    specs = batched_specs(args.instances)
+    engines, params = [], []
+    for i, (spec, walkers) in enumerate(specs):
+        eng = Engine(spec, max_walkers=int(max(6 * walkers, 1e5)), max_spawned=int(max(6 * walkers, 2e5)))
+        eng.start_from_reference(initial_part=walkers)
+        tau = min(0.02, estimate_tau(eng, 20_000))
+        p = capi.default_params(tau=tau, seed=SEED + i, iter=1)
+        engines.append(eng)
+        params.append(p)
+    # equilibrate all instances together, the shift following the population
+    n_cyc = max(args.batch_equil // 10, 1)
+    olds = [s[1] * 2 for s in specs]
+    for c in range(n_cyc):
+        st, _ = iterate_batch(engines, params, 10)
+        for i, p in enumerate(params):
+            p.iter += 10
+            parts = st[i][-1].tot_parts[0] + st[i][-1].tot_parts[1]
+            p.diag_sft[0] = p.diag_sft[1] = p.diag_sft[0] - 0.05 * math.log(parts / olds[i]) / (p.tau * 10)
+            olds[i] = parts
+    K = args.batch_steps
+    # plain FP64, one instance at a time
+    fp64_upd, fp64_ms = 0.0, 0.0
+    for eng, p in zip(engines, params):
+        p.precision = capi.PREC_FP64
+        eng.iterate_n(p, 3)
+        p.iter += 3
+        st, ms = eng.iterate_timed(p, K)
+        p.iter += K
+        fp64_upd += sum(x.tot_parts_old[0] + x.tot_parts_old[1] for x in st)
+        fp64_ms += ms
+    # mixed precision, batched
+    for p in params:
+        p.precision = capi.PREC_MIXED
+    iterate_batch(engines, params, 3)
+    for p in params:
+        p.iter += 3
+    st, mixed_ms = iterate_batch(engines, params, K)
+    mixed_upd = sum(x.tot_parts_old[0] + x.tot_parts_old[1] for per in st for x in per)
+    # FP64 batched too (separates the batching gain from the precision gain)
+    for p in params:
+        p.iter += K
+        p.precision = capi.PREC_FP64
+    st, fb_ms = iterate_batch(engines, params, K)
+    fb_upd = sum(x.tot_parts_old[0] + x.tot_parts_old[1] for per in st for x in per)
+    for e in engines:
+        e.close()
+    v_single = fp64_upd / (fp64_ms / 1e3)
+    v_mixed = mixed_upd / (mixed_ms / 1e3)
+    return {"instances": len(specs), "steps": K, "unit": UNIT,
+            "fp64_single_instance": v_single, "fp64_batched": fb_upd / (fb_ms / 1e3), "mixed_batched": v_mixed,
+            "speedup_mixed_batched_vs_fp64_single": v_mixed / v_single,
+            "walkers_total": sum(w for _, w in specs),
+            "workload": "64 synthetic FCIDUMP instances (instance-indexed seeds), n 12..40, nel 6..20, "
+                        "walkers 1e4..1e6 log-uniform, replica pairs, PCHB"}
+
+
 def cpu_baseline_sample(seconds=12.0):
     """Oracle (CPU restatement) on one core: a 20 000-walker sample of the workload."""
     from neci_stable_gb300 import capi
@@ -310,6 +391,10 @@ def main():
     ap.add_argument("--walkers", type=float, default=TARGET_WALKERS, help="target walker number")
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances measurement")
+    ap.add_argument("--instances", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=20)
+    ap.add_argument("--batch-equil", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -385,6 +470,8 @@ def main():
                             "speedup_vs_fp64": (r["mixed_updates"] / r["mixed_ms"]) / (updates / (dev_s * 1000.0)),
                             "note": "FP32 H_ij, p_gen and spawn amplitude; FP64 death, E_proj and signs"},
     }
+    if not args.no_batched and world == 1:
+        line["batched"] = run_batched(args)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))

@@ -190,6 +190,18 @@ int32_t neci_gpu_iterate_n(neci_gpu_ctx *ctx, const neci_gpu_iter_params *params
 int32_t neci_gpu_iterate_timed(neci_gpu_ctx *ctx, const neci_gpu_iter_params *params,
                                int32_t n_iter, neci_gpu_iter_stats *stats, double *device_ms);
 
+/* Batched steps: n_iter iterations of each of n_ctx independent contexts
+ * (one system and walker list each, e.g. instances of different size or
+ * replica pairs), all on one device.  Each context runs its step graph on its
+ * own stream, so the GPU executes the instances side by side; the result of
+ * every instance is the same as when it is stepped alone.  params holds one
+ * record per context; stats receives n_iter records per context (context-major);
+ * *device_ms (may be NULL) the CUDA-event time of the whole batch.  The
+ * reference runs such instances as separate jobs (replicas: the dneci/mneci
+ * builds, CMakeLists.txt:97-106). */
+int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gpu_iter_params *params,
+                               int32_t n_iter, neci_gpu_iter_stats *stats, double *device_ms);
+
 /* ---- annihilation of an injected spawn list -----------------------------
  * CompressSpawnedList (Annihilation.F90:249-515) followed by
  * AnnihilateSpawnedParts + CalcHashTableStats (Annihilation.F90:965-1352,

@@ -118,6 +118,7 @@ _SIGS = {
     "neci_gpu_iterate": (_i32, [_P, C.POINTER(IterParams), C.POINTER(IterStats)]),
     "neci_gpu_iterate_n": (_i32, [_P, C.POINTER(IterParams), _i32, _P]),
     "neci_gpu_iterate_timed": (_i32, [_P, C.POINTER(IterParams), _i32, _P, _P]),
+    "neci_gpu_iterate_batch": (_i32, [_P, _i32, _P, _i32, _P, _P]),
     "neci_gpu_annihilate": (_i32, [_P, C.POINTER(IterParams), _P, _i64, C.POINTER(IterStats)]),
     "neci_gpu_compress_spawns": (_i32, [_P, _P, _i64, _P, _P, _P]),
     "neci_gpu_compress_spawns_noalloc": (_i32, [_P, _i64, _i32, _i32, _i32, _i32, _P, _P, _P, _P, C.c_char_p, _i32]),

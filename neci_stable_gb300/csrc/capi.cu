@@ -572,6 +572,67 @@ int32_t neci_gpu_iterate_timed(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p,
     return run_steps(ctx->e, p, n_iter, stats, device_ms);
 }
 
+int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gpu_iter_params *params, int32_t n_iter,
+                               neci_gpu_iter_stats *stats, double *device_ms) {
+    if (!ctxs || !params || !stats || n_ctx < 1 || n_iter < 1) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    const int dev = ctxs[0] ? ctxs[0]->e.device : 0;
+    for (int c = 0; c < n_ctx; ++c) {
+        if (!ctxs[c]) return fail(NECI_GPU_ERR_INVALID, "null context in batch");
+        Engine &e = ctxs[c]->e;
+        if (e.device != dev) return fail(NECI_GPU_ERR_INVALID, "batched contexts must share one device");
+        if (e.profiling) return fail(NECI_GPU_ERR_INVALID, "batched steps need profiling off");
+        if (n_iter > e.max_stats) return fail(NECI_GPU_ERR_INVALID, "n_iter above the per-context stats buffer");
+        if (!e.have_ref || !e.sys.tmat || (e.sys.system == NECI_SYS_MOLECULAR && !e.have_pchb) ||
+            (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours))
+            return fail(NECI_GPU_ERR_INVALID, "context not set up");
+    }
+    CK(cudaSetDevice(dev));
+    for (int c = 0; c < n_ctx; ++c) {
+        Engine &e = ctxs[c]->e;
+        copy_params(*e.h_params, params[c]);
+        CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
+        if (int r = ensure_graph(e)) return r;
+    }
+    // a start event on the first context's stream that every stream waits on,
+    // and every stream's end recorded back onto it, brackets the whole batch
+    Engine &e0 = ctxs[0]->e;
+    CK(cudaEventRecord(e0.ev[0], e0.stream));
+    for (int c = 1; c < n_ctx; ++c) CK(cudaStreamWaitEvent(ctxs[c]->e.stream, e0.ev[0], 0));
+    // issue step by step across contexts so that the streams advance together
+    for (int i = 0; i < n_iter; ++i)
+        for (int c = 0; c < n_ctx; ++c) {
+            Engine &e = ctxs[c]->e;
+            CK(cudaGraphLaunch(e.graph, e.stream));
+            CK(cudaMemcpyAsync(e.d_stats + i, e.d_stats + e.max_stats, sizeof(neci_gpu_iter_stats),
+                               cudaMemcpyDeviceToDevice, e.stream));
+        }
+    for (int c = 0; c < n_ctx; ++c) {
+        Engine &e = ctxs[c]->e;
+        CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats) * n_iter, cudaMemcpyDeviceToHost,
+                           e.stream));
+        if (c > 0) {
+            CK(cudaEventRecord(e.ev[1], e.stream));
+            CK(cudaStreamWaitEvent(e0.stream, e.ev[1], 0));
+        }
+    }
+    CK(cudaEventRecord(e0.ev[1], e0.stream));
+    for (int c = 0; c < n_ctx; ++c) CK(cudaStreamSynchronize(ctxs[c]->e.stream));
+    CK(cudaGetLastError());
+    if (device_ms) {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, e0.ev[0], e0.ev[1]));
+        *device_ms = ms;
+    }
+    int first_err = 0;
+    for (int c = 0; c < n_ctx; ++c) {
+        Engine &e = ctxs[c]->e;
+        std::memcpy(stats + (size_t)c * n_iter, e.h_stats, sizeof(neci_gpu_iter_stats) * n_iter);
+        for (int i = 0; i < n_iter && !first_err; ++i) first_err = e.h_stats[i].err;
+    }
+    if (first_err) return fail(first_err, "device reported an error in a batched step");
+    return NECI_GPU_OK;
+}
+
 static int upload_spawns(Engine &e, const int64_t *sp, int64_t n) {
     if (n < 0 || n > e.st.max_spawned) return fail(NECI_GPU_ERR_SPAWN_FULL, "spawn list longer than MaxSpawned");
     if (n > 0) CK(cudaMemcpyAsync(e.st.spawn, sp, (size_t)n * e.sys.R * 8, cudaMemcpyHostToDevice, e.stream));

@@ -929,9 +929,16 @@ __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, i
 // ===========================================================================
 // Host-side launch helpers (declared in internal.h).
 // ===========================================================================
+// Grids are sized to the context's capacity, so that small contexts run
+// side by side (neci_gpu_iterate_batch) instead of each filling the GPU.
+static int clamp_grid(long long want, int hi) { return (int)(want < 8 ? 8 : (want > hi ? hi : want)); }
+static int grid_slots(const Engine &e) { return clamp_grid(e.st.max_walkers / 2048 + 1, e.num_sms * 4); }
+static int grid_spawns(const Engine &e, int threads) {
+    return clamp_grid(e.st.max_spawned / (threads * 4) + 1, e.num_sms * (threads == 128 ? 8 : 4));
+}
 static int grid_for(const Engine &e, int threads) {
     (void)threads;
-    return e.num_sms * 4;
+    return grid_slots(e);
 }
 
 void launch_begin(Engine &e, cudaStream_t s) { k_begin<<<1, 32, 0, s>>>(e.st); }
@@ -944,10 +951,10 @@ void launch_rehash(Engine &e, cudaStream_t s) {
 void launch_sweep(Engine &e, cudaStream_t s) {
     k_sweep<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
-void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<e.num_sms * 4, 256, 0, s>>>(e.st); }
+void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256), 256, 0, s>>>(e.st); }
 void launch_spawn(Engine &e, cudaStream_t s) {
     const size_t shm = (size_t)(e.sys.nbasis + 1 + e.sys.nsites * e.sys.max_neigh) * sizeof(int32_t);
-    const int grid = e.num_sms * 8;
+    const int grid = grid_spawns(e, 128);
     const bool mixed = e.h_params->precision == NECI_PREC_MIXED;
     if (e.sys.excitgen == NECI_EXGEN_RS_HUBBARD) {
         if (mixed) k_spawn<float, NECI_EXGEN_RS_HUBBARD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
@@ -961,13 +968,13 @@ void launch_core(Engine &e, cudaStream_t s) {
     if (e.st.n_core > 0) k_core<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_ann_probe(Engine &e, cudaStream_t s) {
-    k_ann_probe<<<grid_for(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
+    k_ann_probe<<<grid_spawns(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
 }
 void launch_ann_compress(Engine &e, cudaStream_t s) {
-    k_ann_compress<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st);
+    k_ann_compress<<<grid_spawns(e, 256), 256, 0, s>>>(e.sys, e.st);
 }
 void launch_ann_insert(Engine &e, cudaStream_t s) {
-    k_ann_insert<<<e.num_sms * 8, 128, 0, s>>>(e.sys, e.st, e.d_params);
+    k_ann_insert<<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
     k_merge_stats<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params, with_core);

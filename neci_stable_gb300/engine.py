@@ -161,3 +161,17 @@ class Engine:
         cnt = np.zeros(n, dtype=np.int64)
         check(self.lib.neci_gpu_kernel_times(self.ctx, ptr(ms), ptr(cnt), n))
         return {self.lib.neci_gpu_kernel_name(k).decode(): (float(ms[k]), int(cnt[k])) for k in range(n)}
+
+
+def iterate_batch(engines, params, n_iter: int):
+    """n_iter steps of several engines side by side on one device
+    (neci_gpu_iterate_batch).  Returns (stats[engine][step], device ms)."""
+    lib = capi.load()
+    n = len(engines)
+    ctxs = (C.c_void_p * n)(*[e.ctx for e in engines])
+    par = (capi.IterParams * n)(*params)
+    st = (capi.IterStats * (n * n_iter))()
+    ms = C.c_double()
+    check(lib.neci_gpu_iterate_batch(C.cast(ctxs, C.c_void_p), n, C.cast(par, C.c_void_p), n_iter,
+                                     C.cast(st, C.c_void_p), C.byref(ms)))
+    return [list(st[i * n_iter:(i + 1) * n_iter]) for i in range(n)], ms.value

@@ -187,3 +187,32 @@ def test_errors_are_reported_not_faulted():
     eng.start_from_reference(initial_part=1.0)
     st = eng.perform_fcimc_cyc_par(capi.default_params(tau=0.001, seed=1, iter=1))
     assert st.err == 0
+
+
+def test_batched_steps_equal_single_steps():
+    """neci_gpu_iterate_batch changes only concurrency: every instance ends
+    with the walker list it has when stepped alone."""
+    from neci_stable_gb300.engine import iterate_batch
+    from neci_stable_gb300 import systems
+    d = np.load(__import__("pathlib").Path(__file__).parent / "golden" / "hehe_fcidump.npz")
+    specs = [hubbard10(), hubbard10(lenof_sign=2), molecule(12, 6),
+             systems.molecular_system(d["h"], d["eri"], float(d["ecore"]), int(d["nelec"]))]
+    pops = [40.0, 25.0, 60.0, 30.0]
+
+    def fresh():
+        engs = []
+        for sp, pop in zip(specs, pops):
+            e = Engine(sp, 200_000, 400_000)
+            e.start_from_reference(initial_part=pop)
+            engs.append(e)
+        return engs
+
+    params = [capi.default_params(tau=0.01 + 0.005 * i, seed=50 + i, iter=1) for i in range(len(specs))]
+    batch = fresh()
+    st, ms = iterate_batch(batch, params, 12)
+    assert ms > 0.0 and all(len(s) == 12 for s in st)
+    single = fresh()
+    for e, p in zip(single, params):
+        e.iterate_n(p, 12)
+    for a, b, sp in zip(batch, single, specs):
+        assert np.array_equal(canonical(a.download()[0], sp.W), canonical(b.download()[0], sp.W))
