@@ -365,6 +365,7 @@ int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii
     s.f_p_doubles = 1.0f - (float)s.p_singles;
     s.f_p_singles = (float)s.p_singles;
     s.f_p_elec = 1.0f / (float)s.nel;
+    s.f_inv_nalpha = na > 0 ? 1.0f / (float)na : 0.0f;
     s.inv_par = (double)par / s.p_parallel;
     s.inv_opp = (double)(na * nb) / (1.0 - s.p_parallel);
     s.inv_pdoub = 1.0 / s.p_doubles;

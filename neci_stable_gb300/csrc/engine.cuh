@@ -75,6 +75,7 @@ struct DevSys {
     const unsigned long long *pexch_thr;                 // prob_thresh(pExch(ij))
     // single-precision copies for the mixed-precision spawn amplitudes
     float f_pgen_par, f_pgen_opp, f_p_doubles, f_p_singles, f_p_elec;
+    float f_inv_nalpha;  // 1/nOccAlpha (0 without alpha electrons): pair index -> (alpha, beta) positions
     const float *umat32, *tmat32, *alias_prob32, *pexch32;
     // reciprocals: the spawn amplitude multiplies by 1/p_gen built from them
     double inv_par, inv_opp, inv_pdoub, inv_psingles;

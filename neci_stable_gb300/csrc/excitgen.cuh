@@ -197,60 +197,42 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     const bool dbl = sizeof(Real) == 8;
     const int aa = s.nOccAlpha * (s.nOccAlpha - 1) / 2;
     const int bb = s.nOccBeta * (s.nOccBeta - 1) / 2;
-    int al_req, be_req, al_num[2] = {0, 0}, be_num[2] = {0, 0};
-    Real pgen, invp;
-    if (rng.next64() < s.thr_bias) {
-        int idx = (int)uniform_index(rng, (unsigned)(aa + bb));
-        if (idx < aa) {
-            al_req = 2; be_req = 0;
-            tri_pair(idx, al_num[0], al_num[1]);
-        } else {
-            al_req = 0; be_req = 2;
-            tri_pair(idx - aa, be_num[0], be_num[1]);
-        }
-        pgen = dbl ? (Real)s.pgen_par : (Real)s.f_pgen_par;
-        invp = dbl ? (Real)s.inv_par : (Real)s.f_inv_par;
-    } else {
-        al_req = 1; be_req = 1;
-        const int idx = (int)uniform_index(rng, (unsigned)(s.nOccAlpha * s.nOccBeta));
-        al_num[0] = 1 + idx % s.nOccAlpha;
-        be_num[0] = 1 + idx / s.nOccAlpha;
-        pgen = dbl ? (Real)s.pgen_opp : (Real)s.f_pgen_opp;
-        invp = dbl ? (Real)s.inv_opp : (Real)s.f_inv_opp;
-    }
-    // the al_num/be_num-th alpha/beta electrons in nI order, lower orbital first
-    int src0, src1;
-    if (al_req == 2) {
-        src0 = nth_orbital(d, s.W, kAlphaBits, al_num[1]);
-        src1 = nth_orbital(d, s.W, kAlphaBits, al_num[0]);
-    } else if (be_req == 2) {
-        src0 = nth_orbital(d, s.W, kBetaBits, be_num[1]);
-        src1 = nth_orbital(d, s.W, kBetaBits, be_num[0]);
-    } else {
-        const int oa = nth_orbital(d, s.W, kAlphaBits, al_num[0]);
-        const int ob = nth_orbital(d, s.W, kBetaBits, be_num[0]);
-        src0 = min(oa, ob);
-        src1 = max(oa, ob);
-    }
-    if (src0 == 0 || src1 == 0) { e.pgen = 0; return; }
+    // Both spin cases run the same instructions (selects, no branches), so a
+    // warp whose lanes drew different cases stays converged.
+    const bool par = rng.next64() < s.thr_bias;
+    const int idx = (int)uniform_index(rng, par ? (unsigned)(aa + bb) : (unsigned)(s.nOccAlpha * s.nOccBeta));
+    // parallel pair: positions a1 > a2 among the electrons of one spin
+    const bool alpha_pair = idx < aa;
+    int a1, a2;
+    tri_pair(alpha_pair ? idx : idx - aa, a1, a2);
+    // opposite-spin pair: idx = (n_beta - 1) nOccAlpha + (n_alpha - 1)
+    int qb = (int)((float)idx * s.f_inv_nalpha);
+    qb -= (qb * s.nOccAlpha > idx);
+    qb += ((qb + 1) * s.nOccAlpha <= idx);
+    const int ra = idx - qb * s.nOccAlpha;
+    const unsigned long long spin_mask = alpha_pair ? kAlphaBits : kBetaBits;
+    const int o_a = nth_orbital(d, s.W, par ? spin_mask : kAlphaBits, par ? a2 : 1 + ra);
+    const int o_b = nth_orbital(d, s.W, par ? spin_mask : kBetaBits, par ? a1 : 1 + qb);
+    Real pgen = par ? (dbl ? (Real)s.pgen_par : (Real)s.f_pgen_par) : (dbl ? (Real)s.pgen_opp : (Real)s.f_pgen_opp);
+    Real invp = par ? (dbl ? (Real)s.inv_par : (Real)s.f_inv_par) : (dbl ? (Real)s.inv_opp : (Real)s.f_inv_opp);
+    // the exchange draw is taken for every pair and used for opposite spins
+    const unsigned long long rx = rng.next64();
+    // the chosen electrons in nI order, lower orbital first
+    const int src0 = min(o_a, o_b), src1 = max(o_a, o_b);
+    if (src0 == 0) { e.pgen = 0; return; }
     const long long i1 = spat(src0), j1 = spat(src1);
     const long long ij = i1 < j1 ? i1 + j1 * (j1 - 1) / 2 : j1 + i1 * (i1 - 1) / 2;
     int spin0 = src0 & 1, spin1 = src1 & 1;
-    int type;
-    if (spin0 == spin1) {
-        type = 1;
-    } else {
+    int type = 1;
+    if (spin0 != spin1) {
+        const bool exch = rx < __ldg(&s.pexch_thr[ij - 1]);
+        type = exch ? 3 : 2;
         const Real pe = dbl ? (Real)__ldg(&s.pexch[ij - 1]) : (Real)__ldg(&s.pexch32[ij - 1]);
-        if (rng.next64() < __ldg(&s.pexch_thr[ij - 1])) {
-            type = 3;
-            pgen *= pe;
-            invp *= dbl ? (Real)__ldg(&s.pexch_inv[ij - 1]) : (Real)__ldg(&s.pexch_inv32[ij - 1]);
-            const int t = spin0; spin0 = spin1; spin1 = t;
-        } else {
-            type = 2;
-            pgen *= ((Real)1 - pe);
-            invp *= dbl ? (Real)__ldg(&s.pnoexch_inv[ij - 1]) : (Real)__ldg(&s.pnoexch_inv32[ij - 1]);
-        }
+        pgen *= exch ? pe : ((Real)1 - pe);
+        const Real f = dbl ? (Real)__ldg(exch ? &s.pexch_inv[ij - 1] : &s.pnoexch_inv[ij - 1])
+                           : (Real)__ldg(exch ? &s.pexch_inv32[ij - 1] : &s.pnoexch_inv32[ij - 1]);
+        invp *= f;
+        if (exch) { const int t = spin0; spin0 = spin1; spin1 = t; }
     }
     // sample_AliasTable_t (aliasSampling.F90:310-331): slot and fraction
     // from the high and low halves of one 64x(abMax) product

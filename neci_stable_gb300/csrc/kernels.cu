@@ -454,72 +454,145 @@ __device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real 
     return q < 0 ? -v : v;
 }
 
+// One spawn attempt's parent, unpacked from its 8-byte attempt entry
+// (slot | run << 32 | sign bit << 33 | attempt index << 34).
+struct Parent {
+    unsigned long long d[kMaxWords];
+    unsigned long long key;
+    unsigned int k;
+    int run;
+    bool neg, core, pinit;
+};
+__device__ inline void load_parent(const DevSys &s, const DevState &st, const IterParams &p, unsigned long long w0,
+                                   Parent &P) {
+    const long long j = (long long)(w0 & 0xFFFFFFFFull);
+    P.run = (int)((w0 >> 32) & 1ull);
+    P.neg = (w0 >> 33) & 1ull;
+    P.k = (unsigned int)(w0 >> 34);
+    const long long *r = st.dets + j * s.R;
+    for (int w = 0; w < s.W; ++w) P.d[w] = (unsigned long long)r[w];
+    const long long flags = r[s.W + s.L];
+    P.core = st.n_core > 0 && is_core_flags(flags);
+    P.pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(P.run));
+    P.key = det_key(P.d, s.W, p.seed);
+}
+
+// attempt_create for a generated excitation: the core -> core filter
+// (is_core_state, semi_stoch_procs.F90:547; those spawns are done by the
+// deterministic projection) and the rounded fixed-point amplitude.
+template <typename Real>
+__device__ inline long long attempt_create(const DevSys &s, const DevState &st, const IterParams &p, const Parent &P,
+                                           const Excit<Real> &e, Stream &rng, const int32_t *sh_rh2, int &ovf) {
+    if (!e.ok) return 0;
+    if (P.core) {
+        const long long hs = hash_find(st, e.child, s.W, s.R, neci_hash(e.child, s.W, sh_rh2), st.ctl);
+        if (hs >= 0 && is_core_flags(st.dets[hs * s.R + s.W + s.L])) return 0;
+    }
+    return spawn_amplitude<Real>(p, e.hel, e.invp, P.neg, rng, ovf);
+}
+
+// create_particle (fcimc_helper.F90:152-308): append the record; warp-wide.
+template <typename Real>
+__device__ inline void create_particle(const DevSys &s, const DevState &st, long long qv, const Parent &P,
+                                       const Excit<Real> &e) {
+    const unsigned long long pos = warp_append(&st.ctl->n_spawned, qv != 0 ? 1u : 0u);
+    if (qv == 0) return;
+    if (pos >= (unsigned long long)st.max_spawned) {
+        set_err(st.ctl, NECI_GPU_ERR_SPAWN_FULL);
+        return;
+    }
+    long long *o = st.spawn + pos * s.R;
+    for (int w = 0; w < s.W; ++w) o[w] = (long long)e.child[w];
+    for (int k2 = 0; k2 < s.L; ++k2) o[s.W + k2] = (k2 == P.run) ? qv : 0ll;
+    o[s.W + s.L] = P.pinit ? (1ll << init_flag_bit(P.run)) : 0ll;
+}
+
+// A single excitation parked in the block's queue: the attempt's stream is
+// rebuilt and its first draw (the singles/doubles choice) skipped, so the
+// draws are those of an inline single.
+template <typename Real>
+__device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
+                                           unsigned long long w0, const int32_t *sh_rh2, int &ovf) {
+    Parent P;
+    Excit<Real> e;
+    e.ok = false;
+    long long qv = 0;
+    P.run = 0;
+    P.pinit = false;
+    if (valid) {
+        load_parent(s, st, p, w0, P);
+        Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
+        (void)rng.next64();
+        gen_uniform_single<Real>(s, P.d, rng, e);
+        qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf);
+    }
+    create_particle<Real>(s, st, qv, P, e);
+}
+
 // The spawn attempts (FciMCPar.F90:1600-1745, loop_over_walkers): one
 // attempt per thread per round; every lane runs the same number of rounds so
-// that the record append is warp-wide.
+// that the record append is warp-wide.  For molecular systems an attempt
+// that draws a single excitation is parked in a block-local queue; once the
+// queue holds a block's worth, every thread takes one (singles are rare and
+// long: run inline they would stall the doubles of their warp).
 template <typename Real, int GEN>
 __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp) {
     extern __shared__ int32_t sh[];
+    __shared__ unsigned long long sq[256];
+    __shared__ int sq_n;
     int32_t *sh_rh2 = sh;
     int32_t *sh_neigh = sh + (s.nbasis + 1);
     for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
     if (GEN == NECI_EXGEN_RS_HUBBARD)
         for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
+    if (threadIdx.x == 0) sq_n = 0;
     __syncthreads();
     const IterParams p = *pp;
-    Control *c = st.ctl;
-    const long long nat = (long long)min(c->n_att, (unsigned long long)st.max_att);
-    const int W = s.W, L = s.L, R = s.R;
+    const long long nat = (long long)min(st.ctl->n_att, (unsigned long long)st.max_att);
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((nat + stride - 1) / stride) * stride;
+    const int nb = blockDim.x;  // 128: the queue holds at most two rounds
     int ovf = 0;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
         long long qv = 0;
-        int run = 0;
-        bool pinit = false;
+        Parent P;
+        P.run = 0;
+        P.pinit = false;
         Excit<Real> e;
+        e.ok = false;
         if (q < nat) {
             const unsigned long long w0 = st.att[q];
-            const long long j = (long long)(w0 & 0xFFFFFFFFull);
-            run = (int)((w0 >> 32) & 1ull);
-            const bool neg = (w0 >> 33) & 1ull;
-            const unsigned int k = (unsigned int)(w0 >> 34);
-            const long long *r = st.dets + j * R;
-            unsigned long long d[kMaxWords];
-            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
-            const long long flags = r[W + L];
-            const bool core = st.n_core > 0 && is_core_flags(flags);
-            pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(run));
-            Stream rng(det_key(d, W, p.seed), p.iter, P_ATTEMPT, run, k);
+            load_parent(s, st, p, w0, P);
+            Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
             if (GEN == NECI_EXGEN_RS_HUBBARD) {
-                gen_rs_hubbard<Real>(s, d, sh_neigh, rng, e);
+                gen_rs_hubbard<Real>(s, P.d, sh_neigh, rng, e);
+            } else if (rng.next64() < s.thr_singles) {
+                sq[atomicAdd(&sq_n, 1)] = w0;
             } else {
-                if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, rng, e);
-                else gen_pchb_double<Real>(s, d, rng, e);
+                gen_pchb_double<Real>(s, P.d, rng, e);
             }
-            bool keep = e.ok;
-            if (keep && core) {
-                // is_core_state (semi_stoch_procs.F90:547): core -> core spawns
-                // are done by the deterministic projection
-                const long long hs = hash_find(st, e.child, W, R, neci_hash(e.child, W, sh_rh2), c);
-                if (hs >= 0 && is_core_flags(st.dets[hs * R + W + L])) keep = false;
-            }
-            if (keep) qv = spawn_amplitude<Real>(p, e.hel, e.invp, neg, rng, ovf);
+            qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf);
         }
-        // create_particle (fcimc_helper.F90:152-308): append the record
-        const unsigned long long pos = warp_append(&c->n_spawned, qv != 0 ? 1u : 0u);
-        if (qv != 0) {
-            if (pos >= (unsigned long long)st.max_spawned) {
-                set_err(c, NECI_GPU_ERR_SPAWN_FULL);
-            } else {
-                long long *o = st.spawn + pos * R;
-                for (int w = 0; w < W; ++w) o[w] = (long long)e.child[w];
-                for (int k2 = 0; k2 < L; ++k2) o[W + k2] = (k2 == run) ? qv : 0ll;
-                o[W + L] = pinit ? (1ll << init_flag_bit(run)) : 0ll;
+        create_particle<Real>(s, st, qv, P, e);
+        if (GEN != NECI_EXGEN_RS_HUBBARD) {
+            __syncthreads();
+            const int n = sq_n;
+            if (n >= nb) {
+                spawn_queued_single<Real>(s, st, p, true, sq[n - nb + threadIdx.x], sh_rh2, ovf);
+                __syncthreads();
+                if (threadIdx.x == 0) sq_n = n - nb;
+                __syncthreads();
             }
         }
     }
-    if (ovf) set_err(c, NECI_GPU_ERR_OVERFLOW);
+    if (GEN != NECI_EXGEN_RS_HUBBARD) {
+        __syncthreads();
+        const int n = sq_n;
+        for (int b = 0; b < n; b += nb)
+            spawn_queued_single<Real>(s, st, p, b + (int)threadIdx.x < n, b + threadIdx.x < n ? sq[b + threadIdx.x] : 0ull,
+                                      sh_rh2, ovf);
+    }
+    if (ovf) set_err(st.ctl, NECI_GPU_ERR_OVERFLOW);
 }
 
 // ===========================================================================

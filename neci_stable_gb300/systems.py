@@ -254,6 +254,58 @@ def aufbau_reference(n: int, nel: int, ms2: int = 0) -> list[int]:
     return sorted([2 * p for p in range(1, na + 1)] + [2 * p - 1 for p in range(1, nb_ + 1)])
 
 
+def fock_diagonal(h: np.ndarray, eri: np.ndarray, occ) -> np.ndarray:
+    """Closed-shell Fock diagonal f_pp = h_pp + sum_c [2 (pp|cc) - (pc|cp)] over
+    the doubly occupied spatial orbitals c (0-based)."""
+    occ = np.asarray(list(occ), dtype=np.int64)
+    p = np.arange(h.shape[0])
+    J = eri[p, p][:, occ, occ].sum(axis=1)
+    K = eri[p[:, None], occ[None, :], occ[None, :], p[:, None]].sum(axis=1)
+    return np.diag(h) + 2.0 * J - K
+
+
+def fock_ordered_occupation(h: np.ndarray, eri: np.ndarray, nocc: int, max_iter: int = 100) -> list[int]:
+    """The nocc spatial orbitals (0-based, sorted) of lowest closed-shell Fock
+    energy, iterated to self-consistency of the occupation.  NECI orders its
+    basis by orbital energy before filling the reference (Fermi det) and
+    before choosing the orbitals to freeze (SysReadInput ... freeze)."""
+    occ = tuple(sorted(np.argsort(np.diag(h), kind="stable")[:nocc].tolist()))
+    for _ in range(max_iter):
+        nxt = tuple(sorted(np.argsort(fock_diagonal(h, eri, occ), kind="stable")[:nocc].tolist()))
+        if nxt == occ:
+            break
+        occ = nxt
+    return list(occ)
+
+
+def freeze_core(h: np.ndarray, eri: np.ndarray, ecore: float, frozen):
+    """Fold doubly occupied frozen spatial orbitals (0-based) into the core
+    energy and the one-electron integrals (the 'freeze' of IntFreeze,
+    Integrals_neci.F90):
+        E_core' = E_core + sum_c 2 h_cc + sum_cd [2 (cc|dd) - (cd|dc)]
+        h'_pq  = h_pq + sum_c [2 (pq|cc) - (pc|cq)]
+    and drop the frozen orbitals.  Returns (h', eri', E_core', active)."""
+    frozen = np.asarray(sorted(frozen), dtype=np.int64)
+    n = h.shape[0]
+    active = np.array([p for p in range(n) if p not in set(frozen.tolist())], dtype=np.int64)
+    ec = float(ecore)
+    if frozen.size:
+        ec += 2.0 * float(np.trace(h[np.ix_(frozen, frozen)]))
+        ec += float(sum(2.0 * eri[c, c, d, d] - eri[c, d, d, c] for c in frozen for d in frozen))
+    h2 = h.copy()
+    for c in frozen:
+        h2 += 2.0 * eri[:, :, c, c] - eri[:, c, c, :]
+    h2 = h2[np.ix_(active, active)]
+    eri2 = eri[np.ix_(active, active, active, active)]
+    return np.ascontiguousarray(h2), np.ascontiguousarray(eri2), ec, active.tolist()
+
+
+def closed_shell_reference(occ_spatial) -> list[int]:
+    """Spin orbitals (1-based; beta odd, alpha even) of a closed-shell
+    determinant on the given 0-based spatial orbitals."""
+    return sorted([2 * p + 1 for p in occ_spatial] + [2 * p + 2 for p in occ_spatial])
+
+
 def p_singles_from_reference(n: int, nalpha: int, nbeta: int) -> float:
     """pSingles = nSingles / (nSingles + nDoubles) counted from the reference (C1)."""
     ua, ub = n - nalpha, n - nbeta
@@ -323,9 +375,11 @@ def hubbard_system(kind: str, dims, nel: int, u: float, t: float = 1.0, seed: in
 
 
 def molecular_system(h, eri, ecore, nel: int, ms2: int = 0, seed: int = 7, lenof_sign: int = 1,
-                     p_parallel: float = 0.5, name: str = "fcidump") -> SystemSpec:
+                     p_parallel: float = 0.5, name: str = "fcidump", reference=None) -> SystemSpec:
+    """A molecular system from spatial integrals; the reference defaults to
+    the aufbau determinant in orbital index order."""
     n = h.shape[0]
-    ref = aufbau_reference(n, nel, ms2)
+    ref = sorted(reference) if reference is not None else aufbau_reference(n, nel, ms2)
     na = sum(1 for o in ref if o % 2 == 0)
     return SystemSpec(kind=capi.SYS_MOLECULAR, nel=nel, nbasis=2 * n, tmat=spin_tmat(h), reference=ref,
                       random_hash2=random_hash2(2 * n, seed), umat=pack_umat(eri), ecore=ecore,

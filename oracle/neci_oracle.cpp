@@ -790,13 +790,18 @@ struct Oracle {
         int elecs[2], src[2];
         Real pgen, invp;
         pick_biased_elecs<Real>(nI, rng, elecs, src, pgen, invp);
+        // The exchange draw is taken for every pair and used for
+        // opposite-spin pairs only, so that every double consumes the same
+        // number of draws (the device generator runs both spin cases as one
+        // instruction stream).  The distribution is that of the reference.
+        const u64 rx = rng.next64();
         const i64 ij = fuse_index(gtID(src[0]), gtID(src[1]));
         int spin[2] = {src[0] % 2, src[1] % 2};  // getSpinIndex: 0 alpha, 1 beta
         int type;
         if (spin[0] == spin[1]) type = 1;
         else {
             const Real pe = (Real)pexch[ij - 1];
-            if (rng.next64() < prob_thresh(pexch[ij - 1])) {
+            if (rx < prob_thresh(pexch[ij - 1])) {
                 type = 3;
                 pgen *= pe;
                 invp *= prm<Real>(1.0 / pexch[ij - 1]);

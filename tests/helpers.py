@@ -21,6 +21,24 @@ def molecule(n, nel, seed=11, lenof_sign=1):
     return systems.molecular_system(h, eri, ecore, nel, seed=seed + 1, lenof_sign=lenof_sign, name=f"synthetic-{n}")
 
 
+def ne_frozen_system(lenof_sign=1):
+    """NECI's Ne PCHB test input (FCIDUMP of test_suite/neci/parallel/
+    Ne_FciMCPar_pchb, 'freeze 2 0'): the lowest spatial orbital by Fock
+    energy is frozen, the reference fills the next four.  Returns (spec, fixture)."""
+    from pathlib import Path
+    d = np.load(Path(__file__).parent / "golden" / "ne_pchb_fcidump.npz")
+    h, eri, ecore = d["h"], d["eri"], float(d["ecore"])
+    nocc = int(d["nelec"]) // 2
+    occ = systems.fock_ordered_occupation(h, eri, nocc)
+    f = systems.fock_diagonal(h, eri, occ)
+    frozen = [int(np.argmin(f))]
+    h2, eri2, ec2, active = systems.freeze_core(h, eri, ecore, frozen)
+    ref = systems.closed_shell_reference([active.index(p) for p in occ if p not in frozen])
+    spec = systems.molecular_system(h2, eri2, ec2, int(d["nelec"]) - 2, reference=ref, lenof_sign=lenof_sign,
+                                    name="Ne-frozen")
+    return spec, d
+
+
 def random_dets(spec, n, rng):
     """n random determinants with the reference's alpha/beta counts."""
     ref = spec.reference

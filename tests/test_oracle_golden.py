@@ -106,6 +106,20 @@ def test_hehe_exact_diagonalisation_reproduces_neci_davidson():
     assert abs(e0 - float(d["ground_e"][0])) < 5e-10  # NECI prints 10 decimals
 
 
+def test_ne_frozen_core_reproduces_neci_set_up():
+    """NECI's Ne PCHB run ('freeze 2 0') printed the core energy after
+    freezing and <D0|H|D0>; the frozen-core fold and the Fock-ordered
+    reference reproduce both, and the reference NECI printed
+    ((1,2,15,16,21,22,31,32) after freezing)."""
+    from helpers import ne_frozen_system
+    spec, d = ne_frozen_system()
+    assert spec.reference == [1, 2, 15, 16, 21, 22, 31, 32]
+    assert abs(spec.ecore - float(d["ecore_frozen"][0])) < 1e-10
+    o = orc.Oracle(spec, 16, 16, pchb=False)
+    d0 = o.helement(o.ilut_ref[None], o.ilut_ref[None])[0]
+    assert abs(d0 - float(d["d0_energy"][0])) < 1e-10
+
+
 def test_philox_known_answer_vectors():
     lib = orc.lib()
     kat = [((0, 0, 0, 0), (0, 0), (0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8)),
