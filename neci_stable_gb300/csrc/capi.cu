@@ -71,6 +71,7 @@ void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
     d.f_cutoff = (float)p.real_spawn_cutoff;
     d.f_inv_cutoff = (float)d.inv_cutoff;
     d.cutoff_q = (unsigned long long)std::llrint(std::ldexp(p.real_spawn_cutoff, NECI_SPAWN_FIXED_BITS));
+    d.av_unit = p.av_mc_excits == 1.0;
 }
 
 const char *kKernelNames[K_NUM] = {"rehash",    "begin",        "sweep",      "expand",      "spawn", "core",

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/neci_gpu.h"
+#include "bitsplit.h"
 
 namespace neci {
 
@@ -129,6 +130,7 @@ struct IterParams {
     double inv_cutoff, inv_av;
     float f_tau, f_inv_av, f_cutoff, f_inv_cutoff;
     unsigned long long cutoff_q;  // RealSpawnCutoff in fixed point
+    int av_unit;                  // AvMCExcits == 1: the spawn count is split in integers
 };
 
 // ---------------------------------------------------------------------------

@@ -52,25 +52,26 @@ __device__ inline unsigned long long warp_sum_u(unsigned long long v) {
     return v;
 }
 
-// Block-wide sum of NV doubles into global atomics (one atomic per value per block).
+// Block-wide sum of NV doubles into global atomics (one atomic per value per
+// block).  The values are per run, run-minor (v[2i + run]); with one run the
+// odd entries are skipped.  Every thread's values are staged in shared
+// memory and each warp sums whole values (8 adds per lane, then 5 shuffle
+// levels), so a block issues about a quarter of the FP64 adds of a shuffle
+// tree per warp.  blockDim.x <= 256.
 template <int NV>
-__device__ inline void block_add(double (&v)[NV], double *const (&dst)[NV]) {
-    __shared__ double red[NV][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+__device__ inline void block_add(const double (&v)[NV], double *const (&dst)[NV], int L) {
+    __shared__ double red[NV][256];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5, nw = blockDim.x >> 5;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        const double s = warp_sum(v[k]);
-        if (lane == 0) red[k][wid] = s;
-    }
+    for (int m = 0; m < NV; ++m)
+        if ((m & 1) < L) red[m][t] = v[m];
     __syncthreads();
-    if (wid == 0) {
-        const int nw = blockDim.x >> 5;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double s = lane < nw ? red[k][lane] : 0.0;
-            s = warp_sum(s);
-            if (lane == 0 && s != 0.0) atomicAdd(dst[k], s);
-        }
+    for (int m = wid; m < NV; m += nw) {
+        if ((m & 1) >= L) continue;
+        double s = 0.0;
+        for (int i = lane; i < (int)blockDim.x; i += 32) s += red[m][i];
+        s = warp_sum(s);
+        if (lane == 0 && s != 0.0) atomicAdd(dst[m], s);
     }
     __syncthreads();
 }
@@ -170,7 +171,7 @@ __device__ inline void hash_insert(const DevState &st, long long slot, unsigned 
 // TestInitiator_explicit (fcimc_helper.F90:1142-1240) without ADI, senior
 // initiators or an initiator space.
 __device__ inline bool test_initiator(const IterParams &p, bool was, double sgn, bool is_ref, bool core) {
-    const bool popInit = fabs(sgn) > p.initiator_walk_no;
+    const bool popInit = abs_bits(sgn) > dbl_bits(p.initiator_walk_no);  // |sgn| > InitiatorWalkNo
     if (!was) return popInit;
     if (!is_ref && !(core && p.t_core_inits) && !popInit) return false;
     return true;
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             core = st.n_core > 0 && is_core_flags(flags);
             for (int k = 0; k < L; ++k) {
                 acc_old[k] += fabs(C[k]);
-                if (fabs(C[k]) >= kEps12) occ = true;
+                if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
             }
             if (core) {
                 const int ci = st.core_of_slot[j];
@@ -280,11 +281,19 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             for (int k = 0; k < L; ++k) {
                 // decide_num_to_spawn (fcimc_helper.F90:2160-2174)
                 Stream rs(dkey, p.iter, P_NSPAWN, k, 0);
-                const double pa = C[k] * p.av_mc_excits;
-                int ns = abs((int)pa);
-                if (fabs(fabs(pa) - (double)ns) > kEps12) {
-                    const double pe = fabs(pa) - (double)ns;
-                    if (bern(rs, pe)) ++ns;
+                uint32_t whole;
+                bool extra;
+                uint64_t thr;
+                unsigned int ns;
+                if (p.av_unit && split_count(C[k], whole, extra, thr)) {
+                    ns = whole + (extra && rs.next64() < thr);
+                } else {
+                    const double pa = C[k] * p.av_mc_excits;
+                    ns = abs((int)pa);
+                    if (fabs(fabs(pa) - (double)ns) > kEps12) {
+                        const double pe = fabs(pa) - (double)ns;
+                        if (bern(rs, pe)) ++ns;
+                    }
                 }
                 nsp[k] = ns;
                 neg[k] = C[k] < 0.0;
@@ -310,14 +319,16 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 }
                 acc_died[k] += fmin(idie, fabs(C[k]));
                 acc_born[k] += fmax(idie - fabs(C[k]), 0.0);
-                cp[k] = C[k] - idie * fsign(1.0, C[k]);
-                if (fabs(cp[k]) > kEps12) any = true;
+                // C - idie * sign(1, C) with Fortran's sign (+1 for C = -0.0); both products are exact
+                const bool nonneg = !(dbl_bits(C[k]) >> 63) || abs_bits(C[k]) == 0;
+                cp[k] = C[k] - (nonneg ? idie : -idie);
+                if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
             }
             if (p.t_trunc_initiator && any) {
                 for (int k = 0; k < L; ++k)
-                    if ((cp[k] > 0.0) != (C[k] > 0.0)) { acc_ab[k] += fabs(cp[k]); cp[k] = 0.0; }
+                    if (is_positive(cp[k]) != is_positive(C[k])) { acc_ab[k] += fabs(cp[k]); cp[k] = 0.0; }
                 any = false;
-                for (int k = 0; k < L; ++k) if (fabs(cp[k]) > kEps12) any = true;
+                for (int k = 0; k < L; ++k) if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
             }
             if (any || core) {
                 for (int k = 0; k < L; ++k) r[W + k] = double_to_word(cp[k]);
@@ -327,8 +338,8 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 for (int k = 0; k < L; ++k) r[W + k] = double_to_word(0.0);
             }
         }
-        const bool freed = live && occ && !core && word_to_double(r[W]) == 0.0 &&
-                           (L == 1 || word_to_double(r[W + 1]) == 0.0);
+        const bool freed = live && occ && !core && abs_bits(word_to_double(r[W])) == 0 &&
+                           (L == 1 || abs_bits(word_to_double(r[W + 1])) == 0);
         // append free slots
         {
             const unsigned int want = (hole || freed) ? 1u : 0u;
@@ -377,13 +388,12 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             }
         }
     }
-    double v[14] = {acc_old[0], acc_old[1], acc_hf[0], acc_hf[1], acc_en[0], acc_en[1], acc_died[0], acc_died[1],
-                    acc_born[0], acc_born[1], acc_ab[0], acc_ab[1], 0.0, 0.0};
-    double *const dst[14] = {&c->tot_parts_old[0], &c->tot_parts_old[1], &c->hf_cyc[0], &c->hf_cyc[1],
+    const double v[12] = {acc_old[0], acc_old[1], acc_hf[0], acc_hf[1], acc_en[0], acc_en[1], acc_died[0],
+                          acc_died[1], acc_born[0], acc_born[1], acc_ab[0], acc_ab[1]};
+    double *const dst[12] = {&c->tot_parts_old[0], &c->tot_parts_old[1], &c->hf_cyc[0], &c->hf_cyc[1],
                              &c->enum_cyc[0], &c->enum_cyc[1], &c->ndied[0], &c->ndied[1],
-                             &c->nborn[0], &c->nborn[1], &c->naborted[0], &c->naborted[1],
-                             &c->norm[0], &c->norm[1]};
-    block_add<14>(v, dst);
+                             &c->nborn[0], &c->nborn[1], &c->naborted[0], &c->naborted[1]};
+    block_add<12>(v, dst, L);
     unsigned long long u[1] = {acc_att};
     unsigned long long *const du[1] = {&c->n_attempts};
     block_add_u<1>(u, du);
@@ -829,7 +839,7 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
     double v[6] = {a_ab[0], a_ab[1], a_rm[0], a_rm[1], a_born[0], a_born[1]};
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                             &c->nborn[0], &c->nborn[1]};
-    block_add<6>(v, dst);
+    block_add<6>(v, dst, s.L);
     unsigned long long *const du[2] = {&c->abs_s[0], &c->abs_s[1]};
     block_add_u<2>(a_s, du);
 }
@@ -859,7 +869,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
             for (int k = 0; k < L; ++k) {
                 const double y = st.core_y[(long long)ci * L + k];
                 a_born[k] += fabs(y);
-                if (C[k] * y < 0.0) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(y));
+                if (prod_negative(C[k], y)) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(y));
                 C[k] = y + C[k];
             }
             changed = true;
@@ -882,18 +892,18 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                 S[k] = from_fixed(q);
             }
             for (int k = 0; k < L; ++k) {
-                if (fabs(C[k]) < kEps12 && p.t_trunc_initiator) {
+                if (abs_bits(C[k]) < dbl_bits(kEps12) && p.t_trunc_initiator) {
                     const bool sp_init = (m[k] & 0x80000000u) ||
                                          (p.t_init_coherent_rule && (m[k] & 0x7FFFFFFFu) >= 2u);
                     if (!sp_init && !core) { a_ab[k] += fabs(S[k]); S[k] = 0.0; }
                 }
-                if (C[k] * S[k] < 0.0) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(S[k]));
+                if (prod_negative(C[k], S[k])) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(S[k]));
             }
             for (int k = 0; k < L; ++k) C[k] = S[k] + C[k];
             changed = true;
             if (!core) {
                 bool unocc = true;
-                for (int k = 0; k < L; ++k) if (fabs(C[k]) >= kEps12) unocc = false;
+                for (int k = 0; k < L; ++k) if (abs_bits(C[k]) >= dbl_bits(kEps12)) unocc = false;
                 if (unocc) {
                     hash_remove(st, j);
                     r[W + L] = flags | 1ll;
@@ -902,7 +912,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         }
         // CalcHashTableStats (load_balancer.fpp:646-806)
         bool occ = false;
-        for (int k = 0; k < L; ++k) if (fabs(C[k]) >= kEps12) occ = true;
+        for (int k = 0; k < L; ++k) if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
         if (!occ && !core) {
             if (changed) for (int k = 0; k < L; ++k) r[W + k] = double_to_word(C[k]);
             ++a_holes;
@@ -911,7 +921,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         if (!core) {
             for (int k = 0; k < L; ++k) {
                 const double a = fabs(C[k]);
-                if (a > kEps12 && a < p.occupied_thresh) {
+                if (abs_bits(a) > dbl_bits(kEps12) && abs_bits(a) < dbl_bits(p.occupied_thresh)) {
                     unsigned long long d[kMaxWords];
                     for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
                     Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
@@ -920,7 +930,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                         a_rm[k] += a;
                         C[k] = 0.0;
                         bool unocc = true;
-                        for (int k2 = 0; k2 < L; ++k2) if (fabs(C[k2]) >= kEps12) unocc = false;
+                        for (int k2 = 0; k2 < L; ++k2) if (abs_bits(C[k2]) >= dbl_bits(kEps12)) unocc = false;
                         if (unocc) {
                             hash_remove(st, j);
                             r[W + L] = flags | 1ll;
@@ -938,7 +948,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         for (int k = 0; k < L; ++k) {
             a_tp[k] += fabs(C[k]);
             a_norm[k] += C[k] * C[k];
-            if (fabs(C[k]) >= kEps12) occ = true;
+            if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
         }
         if (occ || core) {
             ++a_occ;
@@ -954,7 +964,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
     double *const dst[12] = {&c->nborn[0], &c->nborn[1], &c->nannihil[0], &c->nannihil[1],
                              &c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                              &c->tot_parts[0], &c->tot_parts[1], &c->norm[0], &c->norm[1]};
-    block_add<12>(v, dst);
+    block_add<12>(v, dst, L);
     unsigned long long u[5] = {a_s[0], a_s[1], a_occ, a_holes, a_found};
     unsigned long long *const du[5] = {&c->abs_s[0], &c->abs_s[1], &c->n_occupied, &c->n_holes, &c->n_found};
     block_add_u<5>(u, du);
