@@ -164,8 +164,8 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
         if (sys->excitgen != NECI_EXGEN_RS_HUBBARD) return fail(NECI_GPU_ERR_UNSUPPORTED, "lattice needs rs-hubbard generator");
         if (sys->max_neighbours < 1 || sys->max_neighbours > kMaxNeigh) return fail(NECI_GPU_ERR_UNSUPPORTED, "max_neighbours");
     } else if (sys->system == NECI_SYS_MOLECULAR) {
-        if (sys->excitgen != NECI_EXGEN_PCHB)
-            return fail(NECI_GPU_ERR_UNSUPPORTED, "molecular systems run the PCHB generator on the device");
+        if (sys->excitgen != NECI_EXGEN_PCHB && sys->excitgen != NECI_EXGEN_UNIFORM)
+            return fail(NECI_GPU_ERR_UNSUPPORTED, "molecular systems run the PCHB or the uniform generator");
     } else {
         return fail(NECI_GPU_ERR_UNSUPPORTED, "unknown system");
     }
@@ -357,7 +357,37 @@ int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii
     const int par = na * (na - 1) / 2 + nb * (nb - 1) / 2;
     s.pgen_par = s.p_parallel / (double)par;
     s.pgen_opp = (1.0 - s.p_parallel) / (double)(na * nb);
+    s.p_singles = e.desc.p_singles;  // the caller's pSingles (this may run more than once)
     s.p_doubles = 1.0 - s.p_singles;
+    if (s.excitgen == NECI_EXGEN_UNIFORM) {
+        // gen_rand_excit draws doubles with pDoubles = 1 - pSingles
+        // (fcimc_initialisation.fpp CalcApproxpDoubles); a single's pgen
+        // carries 1 - pDoubles (CreateSingleExcit, :1264)
+        s.p_singles = 1.0 - s.p_doubles;
+        s.thr_doubles = prob_thresh(s.p_doubles);
+        // FindDoubleProb (GenRandSymExcitNUMod.F90:208) with the C1 counts of
+        // FindNumForbiddenOrbsNoSym, PickAOrb and PickBOrb
+        const int nua = s.nBI - na, nub = s.nBI - nb, ep = s.nel * (s.nel - 1) / 2;
+        for (int ispn = 1; ispn <= 3; ++ispn) {
+            int nA, forb, nB, nOther;
+            if (ispn == 2) {
+                nA = s.nbasis - s.nel;
+                forb = (nua == 0 ? nub : 0) + (nub == 0 ? nua : 0);
+                nB = nub; nOther = nua;  // the sum below is symmetric in the two
+            } else if (ispn == 1) {
+                nA = nub; forb = nub == 1; nB = nub - 1; nOther = nub - 1;
+            } else {
+                nA = nua; forb = nua == 1; nB = nua - 1; nOther = nua - 1;
+            }
+            double pg = 0.0;
+            if (nA > forb && nB > 0 && nOther > 0)
+                pg = s.p_doubles * ((1.0 / (double)nB) + (1.0 / (double)nOther)) / (double)(ep * (nA - forb));
+            s.pgen_unif[ispn - 1] = pg;
+            s.inv_unif[ispn - 1] = pg > 0.0 ? 1.0 / pg : 0.0;
+            s.f_pgen_unif[ispn - 1] = (float)pg;
+            s.f_inv_unif[ispn - 1] = (float)s.inv_unif[ispn - 1];
+        }
+    }
     s.p_elec = 1.0 / (double)s.nel;
     s.thr_singles = prob_thresh(s.p_singles);
     s.thr_bias = prob_thresh(s.p_parallel);
@@ -509,12 +539,20 @@ int32_t neci_gpu_download_walkers(neci_gpu_ctx *ctx, int64_t *ilut, double *dh, 
     return NECI_GPU_OK;
 }
 
+// What a context still lacks before it can step (nullptr when ready).
+static const char *not_ready(const Engine &e) {
+    if (!e.have_ref) return "set the reference first";
+    if (!e.sys.tmat) return "set TMat2D first";
+    if (e.sys.system == NECI_SYS_MOLECULAR && !e.sys.umat) return "set UMAT first";
+    if (e.sys.system == NECI_SYS_MOLECULAR && e.sys.excitgen == NECI_EXGEN_PCHB && !e.have_pchb)
+        return "call neci_gpu_init_pchb first";
+    if (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours) return "set the lattice first";
+    return nullptr;
+}
+
 static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_gpu_iter_stats *stats,
                      double *device_ms = nullptr) {
-    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
-    if (e.sys.system == NECI_SYS_MOLECULAR && !e.have_pchb) return fail(NECI_GPU_ERR_INVALID, "call neci_gpu_init_pchb first");
-    if (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours) return fail(NECI_GPU_ERR_INVALID, "set the lattice first");
-    if (!e.sys.tmat) return fail(NECI_GPU_ERR_INVALID, "set TMat2D first");
+    if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
     if (p->tau <= 0.0 || p->av_mc_excits <= 0.0) return fail(NECI_GPU_ERR_INVALID, "tau and AvMCExcits must be positive");
     copy_params(*e.h_params, *p);
     CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
@@ -584,9 +622,7 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         if (e.device != dev) return fail(NECI_GPU_ERR_INVALID, "batched contexts must share one device");
         if (e.profiling) return fail(NECI_GPU_ERR_INVALID, "batched steps need profiling off");
         if (n_iter > e.max_stats) return fail(NECI_GPU_ERR_INVALID, "n_iter above the per-context stats buffer");
-        if (!e.have_ref || !e.sys.tmat || (e.sys.system == NECI_SYS_MOLECULAR && !e.have_pchb) ||
-            (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours))
-            return fail(NECI_GPU_ERR_INVALID, "context not set up");
+        if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
     }
     CK(cudaSetDevice(dev));
     for (int c = 0; c < n_ctx; ++c) {
@@ -774,9 +810,7 @@ int32_t neci_gpu_gen_excit(neci_gpu_ctx *ctx, const int64_t *det, int64_t n, uin
     if (int r = check_ctx(ctx)) return r;
     Engine &e = ctx->e;
     if (n < 0 || !det || (n > 0 && (!child || !pgen || !hel))) return fail(NECI_GPU_ERR_INVALID, "bad argument");
-    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
-    if (e.sys.system == NECI_SYS_MOLECULAR && !e.have_pchb) return fail(NECI_GPU_ERR_INVALID, "call neci_gpu_init_pchb first");
-    if (e.sys.system == NECI_SYS_HUBBARD_REAL_SPACE && !e.sys.neighbours) return fail(NECI_GPU_ERR_INVALID, "set the lattice first");
+    if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
     if (n == 0) return NECI_GPU_OK;
     int nel = 0;
     for (int w = 0; w < e.sys.W; ++w) nel += __builtin_popcountll((unsigned long long)det[w]);

@@ -81,6 +81,11 @@ struct DevSys {
     // reciprocals: the spawn amplitude multiplies by 1/p_gen built from them
     double inv_par, inv_opp, inv_pdoub, inv_psingles;
     float f_inv_par, f_inv_opp, f_inv_pdoub, f_inv_psingles;
+    // uniform generator (C1): r < pDoubles picks a double; the double's
+    // pgen and 1/pgen per iSpn (1 beta/beta, 2 alpha/beta, 3 alpha/alpha)
+    unsigned long long thr_doubles;
+    double pgen_unif[3], inv_unif[3];
+    float f_pgen_unif[3], f_inv_unif[3];
     const double *alias_inv, *pexch_inv, *pnoexch_inv;   // 1/prob, 1/pExch, 1/(1-pExch)
     const float *alias_inv32, *pexch_inv32, *pnoexch_inv32;
 };

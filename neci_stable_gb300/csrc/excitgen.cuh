@@ -174,6 +174,24 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
     e.ok = true;
 }
 
+// Child determinant and H_ij of the double src0 < src1 -> {o0, o1}:
+// make_double (excit_parity.F90:78) pairs the sources with the sorted
+// targets, the parity counts the occupied orbitals each move passes.
+template <typename Real>
+__device__ inline void finish_double(const DevSys &s, const unsigned long long *d, int src0, int src1, int o0, int o1,
+                                     Excit<Real> &e) {
+    const int ta = min(o0, o1), tb = max(o0, o1);
+    for (int w = 0; w < s.W; ++w) e.child[w] = d[w];
+    int np = occ_between(e.child, s.W, min(src0, ta), max(src0, ta));
+    flip_orb(e.child, src0);
+    flip_orb(e.child, ta);
+    np += occ_between(e.child, s.W, min(src1, tb), max(src1, tb));
+    flip_orb(e.child, src1);
+    flip_orb(e.child, tb);
+    const Real hel = sltcnd_2_r<Real>(s, src0, src1, ta, tb);
+    e.hel = (np & 1) ? -hel : hel;
+}
+
 // Position among the electrons of one spin of the pair with triangular
 // index idx (pick_biased_elecs' ceiling((1+sqrt(9+8 idx))/2), in integers):
 // returns a1 > a2 >= 1 with idx = (a1-1)(a1-2)/2 + a2 - 1.
@@ -249,21 +267,103 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     const int tp = __ldg(&s.tgt_pair[ab]);
     const int o0 = 2 * (tp >> 16) - spin0, o1 = 2 * (tp & 0xFFFF) - spin1;
     if (o0 == 0 || o1 == 0 || orb_occ(d, o0) || orb_occ(d, o1) || !(pholes > (Real)1e-10)) { e.pgen = 0; return; }
-    const int ta = min(o0, o1), tb = max(o0, o1);
-    for (int w = 0; w < s.W; ++w) e.child[w] = d[w];
-    // parity of src0 -> ta then src1 -> tb (make_double pairing)
-    int np = occ_between(e.child, s.W, min(src0, ta), max(src0, ta));
-    flip_orb(e.child, src0);
-    flip_orb(e.child, ta);
-    np += occ_between(e.child, s.W, min(src1, tb), max(src1, tb));
-    flip_orb(e.child, src1);
-    flip_orb(e.child, tb);
-    const Real hel = sltcnd_2_r<Real>(s, src0, src1, ta, tb);
-    e.hel = (np & 1) ? -hel : hel;
+    finish_double<Real>(s, d, src0, src1, o0, o1, e);
     pgen *= pholes;
     e.pgen = pgen * (dbl ? (Real)s.p_doubles : (Real)s.f_p_doubles);
     invp *= dbl ? (Real)__ldg(&s.alias_inv[base + ab - 1]) : (Real)__ldg(&s.alias_inv32[base + ab - 1]);
     e.invp = invp * (dbl ? (Real)s.inv_pdoub : (Real)s.f_inv_pdoub);
+    e.ok = true;
+}
+
+// The c-th (1-based) unoccupied spin orbital among those of `pattern`, 0 if none.
+__device__ inline int nth_unoccupied(const DevSys &s, const unsigned long long *d, unsigned long long pattern, int c) {
+    unsigned long long u[kMaxWords];
+    for (int w = 0; w < s.W; ++w) {
+        const int lo = 64 * w;
+        const unsigned long long valid = s.nbasis >= lo + 64 ? ~0ull : (s.nbasis > lo ? (1ull << (s.nbasis - lo)) - 1 : 0ull);
+        u[w] = ~d[w] & valid;
+    }
+    return nth_orbital(u, s.W, pattern, c);
+}
+
+// CreateDoubExcit (GenRandSymExcitNUMod.F90:155-205) without spatial
+// symmetry (C1: tNoSymGenRandExcits), tCycleOrbs = .false.:
+//   PickElecPair (:954)  a uniform electron pair, iSpn = 1 beta/beta,
+//                        2 alpha/beta, 3 alpha/alpha
+//   FindNumForbiddenOrbsNoSym (:380), PickAOrb (:669) with
+//   IsAOrbSymAllowed: the first hole by rejection (cycled when at most 3
+//                        are allowed), PickBOrb (:222) the second by rejection
+//   FindDoubleProb (:208) pgen, which depends only on iSpn here (all
+//                        determinants share the alpha/beta counts), so it is
+//                        taken from the host's table of the three cases.
+// NECI stops the run where a rejection loop exceeds its limit; here the
+// attempt produces no child.
+template <typename Real>
+__device__ inline void gen_uniform_double(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
+    e.ic = 2;
+    e.ok = false;
+    e.pgen = 0;
+    const int nel = s.nel;
+    const int ep = nel * (nel - 1) / 2;
+    const int X = ep - ((int)uniform_index(rng, (unsigned)ep) + 1);
+    // K = int((sqrt(8X + 1) - 1) / 2): the largest K with K(K+1)/2 <= X
+    int K = (int)((sqrtf(8.0f * (float)X + 1.0f) - 1.0f) * 0.5f);
+    while (K > 0 && K * (K + 1) / 2 > X) --K;
+    while ((K + 1) * (K + 2) / 2 <= X) ++K;
+    const int src0 = nth_orbital(d, s.W, kAllBits, nel - 1 - K);
+    const int src1 = nth_orbital(d, s.W, kAllBits, nel - X + K * (K + 1) / 2);
+    if (src0 == 0 || src1 == 0) return;
+    const int ispn = beta(src0) != beta(src1) ? 2 : (beta(src0) ? 1 : 3);
+    const int nua = s.nBI - s.nOccAlpha, nub = s.nBI - s.nOccBeta;
+    int na, forbidden;
+    unsigned long long allowed;  // spin orbitals whose partner class has room (IsAOrbSymAllowed)
+    if (ispn == 2) {
+        na = s.nbasis - nel;
+        forbidden = (nua == 0 ? nub : 0) + (nub == 0 ? nua : 0);
+        allowed = (nub != 0 ? kAlphaBits : 0ull) | (nua != 0 ? kBetaBits : 0ull);
+    } else if (ispn == 1) {
+        na = nub;
+        forbidden = nub == 1;
+        allowed = nub != 1 ? kBetaBits : 0ull;
+    } else {
+        na = nua;
+        forbidden = nua == 1;
+        allowed = nua != 1 ? kAlphaBits : 0ull;
+    }
+    if (na == forbidden) return;
+    int orbA = 0;
+    if (na - forbidden <= 3) {
+        orbA = nth_unoccupied(s, d, allowed, (int)uniform_index(rng, (unsigned)(na - forbidden)) + 1);
+    } else {
+        const unsigned n_draw = ispn == 2 ? (unsigned)s.nbasis : (unsigned)s.nBI;
+        bool found = false;
+        // NECI's counters: at most 252 draws per pick, 20 nBasis + 2 picks
+        for (int overall = 0; overall <= 20 * s.nbasis + 1 && !found; ++overall) {
+            orbA = 0;
+            for (int att = 0; att <= 251; ++att) {
+                const int c = (int)uniform_index(rng, n_draw);
+                const int o = ispn == 2 ? c + 1 : (ispn == 1 ? 2 * (c + 1) - 1 : 2 * (c + 1));
+                if (!orb_occ(d, o)) { orbA = o; break; }
+            }
+            if (orbA == 0) return;
+            found = (allowed >> ((orbA - 1) & 63)) & 1ull;
+        }
+        if (!found) return;
+    }
+    if (orbA == 0) return;
+    // PickBOrb: the second hole's spin
+    const bool b_beta = ispn == 1 || (ispn == 2 && !beta(orbA));
+    int orbB = 0;
+    for (int att = 0; att <= 1001; ++att) {
+        const int c = (int)uniform_index(rng, (unsigned)s.nBI);
+        const int o = 2 * (c + 1) - (b_beta ? 1 : 0);
+        if (!orb_occ(d, o) && o != orbA) { orbB = o; break; }
+    }
+    if (orbB == 0) return;
+    finish_double<Real>(s, d, src0, src1, orbA, orbB, e);
+    const bool dbl = sizeof(Real) == 8;
+    e.pgen = dbl ? (Real)s.pgen_unif[ispn - 1] : (Real)s.f_pgen_unif[ispn - 1];
+    e.invp = dbl ? (Real)s.inv_unif[ispn - 1] : (Real)s.f_inv_unif[ispn - 1];
     e.ok = true;
 }
 
@@ -273,6 +373,12 @@ __device__ inline void generate_excitation(const DevSys &s, const unsigned long 
                                            Stream &rng, Excit<Real> &e) {
     if (s.excitgen == NECI_EXGEN_RS_HUBBARD) {
         gen_rs_hubbard<Real>(s, d, neigh, rng, e);
+        return;
+    }
+    if (s.excitgen == NECI_EXGEN_UNIFORM) {
+        // gen_rand_excit (GenRandSymExcitNUMod.F90:120-147): r < pDoubles -> double
+        if (rng.next64() < s.thr_doubles) gen_uniform_double<Real>(s, d, rng, e);
+        else gen_uniform_single<Real>(s, d, rng, e);
         return;
     }
     if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, rng, e);

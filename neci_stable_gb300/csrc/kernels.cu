@@ -576,10 +576,13 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
             Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
             if (GEN == NECI_EXGEN_RS_HUBBARD) {
                 gen_rs_hubbard<Real>(s, P.d, sh_neigh, rng, e);
-            } else if (rng.next64() < s.thr_singles) {
-                sq[atomicAdd(&sq_n, 1)] = w0;
             } else {
-                gen_pchb_double<Real>(s, P.d, rng, e);
+                // gen_exc_sd: r < pSingles is a single; gen_rand_excit: r < pDoubles is a double
+                const unsigned long long r0 = rng.next64();
+                const bool single = GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles;
+                if (single) sq[atomicAdd(&sq_n, 1)] = w0;
+                else if (GEN == NECI_EXGEN_UNIFORM) gen_uniform_double<Real>(s, P.d, rng, e);
+                else gen_pchb_double<Real>(s, P.d, rng, e);
             }
             qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf);
         }
@@ -1042,6 +1045,9 @@ void launch_spawn(Engine &e, cudaStream_t s) {
     if (e.sys.excitgen == NECI_EXGEN_RS_HUBBARD) {
         if (mixed) k_spawn<float, NECI_EXGEN_RS_HUBBARD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
         else k_spawn<double, NECI_EXGEN_RS_HUBBARD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    } else if (e.sys.excitgen == NECI_EXGEN_UNIFORM) {
+        if (mixed) k_spawn<float, NECI_EXGEN_UNIFORM><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+        else k_spawn<double, NECI_EXGEN_UNIFORM><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
     } else {
         if (mixed) k_spawn<float, NECI_EXGEN_PCHB><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
         else k_spawn<double, NECI_EXGEN_PCHB><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);

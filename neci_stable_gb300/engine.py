@@ -41,7 +41,7 @@ class Engine:
         check(self.lib.neci_gpu_set_reference(self.ctx, ptr(self.ilut_ref), 0.0))
         self.hii = float(self.helement(self.ilut_ref[None], self.ilut_ref[None])[0])
         check(self.lib.neci_gpu_set_reference(self.ctx, ptr(self.ilut_ref), self.hii))
-        if spec.kind == capi.SYS_MOLECULAR and pchb:
+        if spec.kind == capi.SYS_MOLECULAR and spec.generator == capi.EXGEN_PCHB and pchb:
             check(self.lib.neci_gpu_init_pchb(self.ctx))
 
     def close(self):

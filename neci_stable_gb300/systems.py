@@ -335,6 +335,13 @@ class SystemSpec:
     lenof_sign: int = 1
     name: str = ""
     extra: dict = field(default_factory=dict)
+    excitgen: int | None = None          # NECI_EXGEN_*; None: rs-Hubbard for lattices, PCHB for FCIDUMPs
+
+    @property
+    def generator(self) -> int:
+        if self.excitgen is not None:
+            return self.excitgen
+        return capi.EXGEN_RS_HUBBARD if self.kind == capi.SYS_HUBBARD_REAL_SPACE else capi.EXGEN_PCHB
 
     @property
     def nifd(self) -> int:
@@ -348,7 +355,7 @@ class SystemSpec:
         s = capi.System()
         s.nel, s.nbasis, s.nifd, s.lenof_sign = self.nel, self.nbasis, self.nifd, self.lenof_sign
         s.system = self.kind
-        s.excitgen = capi.EXGEN_RS_HUBBARD if self.kind == capi.SYS_HUBBARD_REAL_SPACE else capi.EXGEN_PCHB
+        s.excitgen = self.generator
         s.max_neighbours = 0 if self.neighbours is None else int(self.neighbours.shape[1])
         s.uhub, s.bhub, s.ecore = self.uhub, self.bhub, self.ecore
         s.p_singles, s.p_parallel = self.p_singles, self.p_parallel
@@ -375,7 +382,8 @@ def hubbard_system(kind: str, dims, nel: int, u: float, t: float = 1.0, seed: in
 
 
 def molecular_system(h, eri, ecore, nel: int, ms2: int = 0, seed: int = 7, lenof_sign: int = 1,
-                     p_parallel: float = 0.5, name: str = "fcidump", reference=None) -> SystemSpec:
+                     p_parallel: float = 0.5, name: str = "fcidump", reference=None,
+                     excitgen: int = capi.EXGEN_PCHB) -> SystemSpec:
     """A molecular system from spatial integrals; the reference defaults to
     the aufbau determinant in orbital index order."""
     n = h.shape[0]
@@ -384,4 +392,4 @@ def molecular_system(h, eri, ecore, nel: int, ms2: int = 0, seed: int = 7, lenof
     return SystemSpec(kind=capi.SYS_MOLECULAR, nel=nel, nbasis=2 * n, tmat=spin_tmat(h), reference=ref,
                       random_hash2=random_hash2(2 * n, seed), umat=pack_umat(eri), ecore=ecore,
                       p_singles=p_singles_from_reference(n, na, nel - na), p_parallel=p_parallel,
-                      lenof_sign=lenof_sign, name=name)
+                      lenof_sign=lenof_sign, name=name, excitgen=excitgen)

@@ -174,6 +174,7 @@ struct Oracle {
     std::vector<i64> ilut_ref;
     double hii = 0.0;
     int nOccAlpha = 0, nOccBeta = 0;
+    double p_doubles = 0.0;             // 1 - pSingles
 
     // PCHB
     bool pchb_ready = false;
@@ -831,10 +832,137 @@ struct Oracle {
         g.hel = offdiag_from_ex_r<Real>(nI, 2, g.ex, g.par);
         return true;
     }
-    // gen_exc_sd (excitation_generators.F90:110-133) with UniformSingles_t.
+    // Uniform generator (gen_rand_excit) without spatial symmetry: the pgen of
+    // a double from CreateDoubExcit's counts for electron-pair spin case iSpn
+    // (1 beta/beta, 2 alpha/beta, 3 alpha/alpha).  FindDoubleProb
+    // (GenRandSymExcitNUMod.F90:208) with FindNumForbiddenOrbsNoSym (:380),
+    // PickAOrb's NExcit (:669) and PickBOrb's NExcit/NExcitOtherWay (:222).
+    double uniform_double_pgen(int ispn, int &nexcit_a, int &forbidden, int &nexcit_b, int &other,
+                               int spin_a_ms) const {
+        const int norbs = sys.nbasis / 2, nel = sys.nel;
+        const int cc[2] = {norbs - nOccAlpha, norbs - nOccBeta};  // ClassCountUnocc2: alpha, beta
+        forbidden = 0;
+        if (ispn == 2) {
+            if (cc[0] == 0) forbidden = cc[1];
+            if (cc[1] == 0) forbidden += cc[0];
+            nexcit_a = sys.nbasis - nel;
+            if (spin_a_ms == -1) { nexcit_b = cc[0]; other = cc[1]; }
+            else { nexcit_b = cc[1]; other = cc[0]; }
+        } else if (ispn == 1) {
+            if (cc[1] == 1) forbidden = 1;
+            nexcit_a = norbs - nOccBeta;
+            nexcit_b = cc[1] - 1; other = cc[1] - 1;
+        } else {
+            if (cc[0] == 1) forbidden = 1;
+            nexcit_a = norbs - nOccAlpha;
+            nexcit_b = cc[0] - 1; other = cc[0] - 1;
+        }
+        if (nexcit_a == forbidden || nexcit_b <= 0 || other <= 0) return 0.0;
+        const int elec_pairs = nel * (nel - 1) / 2;
+        return p_doubles * ((1.0 / (double)nexcit_b) + (1.0 / (double)other)) /
+               (double)(elec_pairs * (nexcit_a - forbidden));
+    }
+    // IsAOrbSymAllowed (GenRandSymExcitNUMod.F90:873) with tNoSymGenRandExcits.
+    bool a_orb_allowed(int ispn, int spin_a_ms) const {
+        const int norbs = sys.nbasis / 2;
+        const int cc[2] = {norbs - nOccAlpha, norbs - nOccBeta};
+        if (ispn == 2) return spin_a_ms == 1 ? cc[1] != 0 : cc[0] != 0;
+        if (ispn == 1) return cc[1] != 1;
+        return cc[0] != 1;
+    }
+    // CreateDoubExcit (GenRandSymExcitNUMod.F90:155-205), C1, tCycleOrbs =
+    // .false.; where NECI stops the run (a rejection loop past its limit) the
+    // attempt makes no child.
+    template <typename Real>
+    bool create_doub_excit(const i64 *ilut, const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
+        g.ic = 2;
+        const int nel = sys.nel, nbasis = sys.nbasis, norbs = nbasis / 2;
+        const int elec_pairs = nel * (nel - 1) / 2;
+        // PickElecPair (:954-1025)
+        const int ind = (int)uniform_index(rng, (u32)elec_pairs) + 1;
+        const int X = elec_pairs - ind;
+        const int K = (int)((std::sqrt(8.0 * (double)X + 1.0) - 1.0) / 2.0);
+        const int elec1 = nel - 1 - K;
+        const int elec2 = nel - X + (K * (K + 1)) / 2;
+        const int orb1 = nI[elec1 - 1], orb2 = nI[elec2 - 1];
+        const int ms1 = is_beta(orb1) ? -1 : 1, ms2 = is_beta(orb2) ? -1 : 1;
+        const int ispn = ms1 * ms2 == -1 ? 2 : (ms1 == 1 ? 3 : 1);
+        int nexcit_a, forbidden, nb_, no_;
+        uniform_double_pgen(ispn, nexcit_a, forbidden, nb_, no_, 1);
+        // PickAOrb (:669-869)
+        if (nexcit_a == forbidden) { g.pgen = 0; return false; }
+        int orb_a = 0, spin_a = 0;
+        for (int overall = 0;; ++overall) {
+            if (nexcit_a - forbidden <= 3) {
+                const int chosen = (int)uniform_index(rng, (u32)(nexcit_a - forbidden)) + 1;
+                int z = 1;
+                if (ispn == 2) {
+                    for (int i = 0; i < nbasis && !orb_a; ++i) {
+                        if (orb_occ(ilut, i + 1)) continue;
+                        spin_a = is_beta(i + 1) ? -1 : 1;
+                        if (a_orb_allowed(ispn, spin_a)) {
+                            if (z == chosen) orb_a = i + 1;
+                            ++z;
+                        }
+                    }
+                } else {
+                    for (int i = 1; i <= norbs && !orb_a; ++i) {
+                        const int o = ispn == 1 ? 2 * i - 1 : 2 * i;
+                        if (!orb_occ(ilut, o) && a_orb_allowed(ispn, 0)) {
+                            if (z == chosen) orb_a = o;
+                            ++z;
+                        }
+                    }
+                }
+                if (!orb_a) { g.pgen = 0; return false; }
+                break;  // NECI returns here, without the check below
+            }
+            int attempts = 0, chosen;
+            while (true) {
+                if (ispn == 2) {
+                    chosen = (int)uniform_index(rng, (u32)nbasis) + 1;
+                } else {
+                    chosen = (int)uniform_index(rng, (u32)norbs) + 1;
+                    chosen = ispn == 1 ? 2 * chosen - 1 : 2 * chosen;
+                }
+                if (!orb_occ(ilut, chosen)) break;
+                if (attempts > 250) { g.pgen = 0; return false; }
+                ++attempts;
+            }
+            orb_a = chosen;
+            if (ispn == 2) spin_a = is_beta(orb_a) ? -1 : 1;
+            if (a_orb_allowed(ispn, spin_a)) break;
+            if (overall > nbasis * 20) { g.pgen = 0; return false; }
+        }
+        // PickBOrb (:222-378), METHOD 2
+        int spin_b;  // 1 alpha, 2 beta
+        if (ispn == 2) spin_b = spin_a == -1 ? 1 : 2;
+        else spin_b = ispn == 1 ? 2 : 1;
+        int orb_b, attempts = 0;
+        while (true) {
+            const int chosen = (int)uniform_index(rng, (u32)norbs);
+            orb_b = 2 * (chosen + 1) - (spin_b - 1);
+            if (!orb_occ(ilut, orb_b) && orb_b != orb_a) break;
+            if (attempts > 1000) { g.pgen = 0; return false; }
+            ++attempts;
+        }
+        make_double(nI, g.nJ, elec1, elec2, orb_a, orb_b, g.ex, g.par);
+        const double pg = uniform_double_pgen(ispn, nexcit_a, forbidden, nb_, no_, spin_a);
+        g.pgen = (Real)pg;
+        g.invp = prm<Real>(1.0 / pg);
+        g.hel = offdiag_from_ex_r<Real>(nI, 2, g.ex, g.par);
+        return true;
+    }
+
+    // gen_exc_sd (excitation_generators.F90:110-133) with UniformSingles_t;
+    // gen_rand_excit (GenRandSymExcitNUMod.F90:120-147) for the uniform generator.
     template <typename Real>
     bool generate_excitation(const i64 *ilut, const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
         if (sys.excitgen == NECI_EXGEN_RS_HUBBARD) return gen_excit_rs_hubbard<Real>(ilut, nI, rng, g);
+        if (sys.excitgen == NECI_EXGEN_UNIFORM) {
+            if (rng.next64() < prob_thresh(p_doubles)) return create_doub_excit<Real>(ilut, nI, rng, g);
+            return create_single_excit<Real>(ilut, nI, rng, g);
+        }
         if (rng.next64() < prob_thresh(sys.p_singles)) return create_single_excit<Real>(ilut, nI, rng, g);
         return pchb_doubles<Real>(nI, rng, g);
     }
@@ -1436,6 +1564,10 @@ int32_t orc_init(void **out, const neci_gpu_system *sys) {
     o->HashIndex.assign(sys->n_walker_hashes, {});
     o->random_hash2.assign(sys->nbasis + 1, 0);
     o->ilut_ref.assign(o->W, 0);
+    // pDoubles = 1 - pSingles (CalcApproxpDoubles); gen_rand_excit's singles
+    // carry 1 - pDoubles (CreateSingleExcit, GenRandSymExcitNUMod.F90:1264)
+    o->p_doubles = 1.0 - sys->p_singles;
+    if (sys->excitgen == NECI_EXGEN_UNIFORM) o->sys.p_singles = 1.0 - o->p_doubles;
     *out = o;
     return NECI_GPU_OK;
 }
@@ -1616,6 +1748,14 @@ int32_t orc_calc_pgen(void *h, const int64_t *det, const int64_t *child, double 
         for (int x : nI) if (nun[x & 1] == 0) ++wno;
         const int nexcit = nun[ex[0][0] & 1];
         *out = o->sys.p_singles / (double)(nexcit * (o->sys.nel - wno));
+        return NECI_GPU_OK;
+    }
+    if (o->sys.excitgen == NECI_EXGEN_UNIFORM) {
+        // calc_pgen_symrandexcit2 doubles, C1: FindDoubleProb of the pair's spins
+        const bool b0 = ex[0][0] & 1, b1 = ex[0][1] & 1;
+        const int ispn = b0 != b1 ? 2 : (b0 ? 1 : 3);
+        int na, forb, nb, no;
+        *out = o->uniform_double_pgen(ispn, na, forb, nb, no, 1);
         return NECI_GPU_OK;
     }
     // GAS_doubles_PCHB_get_pgen (spatorb_fastweighted.fpp)

@@ -97,6 +97,7 @@ class Oracle:
     """CPU restatement of the engine for one system (same inputs as Engine)."""
 
     def __init__(self, spec, max_walkers: int, max_spawned: int, hii: float | None = None, pchb: bool = True):
+        from neci_stable_gb300 import capi
         from neci_stable_gb300.systems import encode_det
         self.spec = spec
         self.W = spec.W
@@ -118,7 +119,7 @@ class Oracle:
         _ok(lib().orc_set_reference(h, _ptr(self.ilut_ref), 0.0))
         self.hii = float(self.helement(self.ilut_ref[None], self.ilut_ref[None])[0]) if hii is None else hii
         _ok(lib().orc_set_reference(h, _ptr(self.ilut_ref), self.hii))
-        if spec.umat is not None and pchb:
+        if spec.umat is not None and pchb and spec.generator == capi.EXGEN_PCHB:
             _ok(lib().orc_init_pchb(h))
 
     def __del__(self):

@@ -21,6 +21,12 @@ def molecule(n, nel, seed=11, lenof_sign=1):
     return systems.molecular_system(h, eri, ecore, nel, seed=seed + 1, lenof_sign=lenof_sign, name=f"synthetic-{n}")
 
 
+def molecule_uniform(n, nel, seed=11, lenof_sign=1):
+    h, eri, ecore = systems.synthetic_fcidump(n, seed)
+    return systems.molecular_system(h, eri, ecore, nel, seed=seed + 1, lenof_sign=lenof_sign,
+                                    name=f"synthetic-{n}-uniform", excitgen=capi.EXGEN_UNIFORM)
+
+
 def ne_frozen_system(lenof_sign=1):
     """NECI's Ne PCHB test input (FCIDUMP of test_suite/neci/parallel/
     Ne_FciMCPar_pchb, 'freeze 2 0'): the lowest spatial orbital by Fock

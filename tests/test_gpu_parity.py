@@ -14,8 +14,8 @@ from neci_stable_gb300 import capi
 from neci_stable_gb300.engine import Engine
 from oracle.oracle import Oracle
 
-from helpers import (canonical, canonical_with, excite, hubbard10, hubbard_square, molecule, random_dets,
-                     random_spawns, random_walkers)
+from helpers import (canonical, canonical_with, excite, hubbard10, hubbard_square, molecule, molecule_uniform,
+                     random_dets, random_spawns, random_walkers)
 
 pytestmark = pytest.mark.gpu
 
@@ -27,6 +27,8 @@ SYSTEMS = {
     "mol24": lambda: molecule(24, 10),
     "mol40": lambda: molecule(40, 12),      # 80 spin orbitals: two det words
     "mol64": lambda: molecule(64, 20),      # 128 spin orbitals: three det words
+    "mol12u": lambda: molecule_uniform(12, 6),   # the uniform generator (gen_rand_excit)
+    "mol40u": lambda: molecule_uniform(40, 12),
 }
 
 _cache = {}
@@ -67,7 +69,7 @@ def test_helement(name):
     assert np.array_equal(g, c), "FP64 matrix elements are expected bit-exact"
 
 
-@pytest.mark.parametrize("name", ["hub10", "hub6x6", "mol12", "mol24", "mol40", "mol64"])
+@pytest.mark.parametrize("name", ["hub10", "hub6x6", "mol12", "mol24", "mol40", "mol64", "mol12u", "mol40u"])
 def test_gen_excit(name):
     spec, eng, orc = pair(name)
     rng = np.random.default_rng(3)
@@ -150,7 +152,8 @@ def run_pair(name, iters, start_pop, tau, shift=0.0, seed=31, precision=capi.PRE
 
 @pytest.mark.parametrize("name,iters,pop,tau", [("hub10", 40, 50.0, 0.02), ("hub10x2", 25, 20.0, 0.02),
                                                 ("hub6x6", 12, 30.0, 0.01), ("mol12", 30, 40.0, 0.02),
-                                                ("mol24", 20, 200.0, 0.005)])
+                                                ("mol24", 20, 200.0, 0.005), ("mol12u", 30, 40.0, 0.02),
+                                                ("mol40u", 12, 100.0, 0.005)])
 def test_iterations_bit_exact(name, iters, pop, tau):
     st = run_pair(name, iters, pop, tau)
     assert st.n_occupied > 1

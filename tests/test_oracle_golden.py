@@ -10,8 +10,8 @@
 * Philox-4x32-10 against the published known-answer vectors
 * alias tables reproduce their target distribution
   (unit_tests/sampler/test_aliasTables.F90)
-* the PCHB and uniform-singles generators: sampled frequencies match p_gen
-  and p_gen matches the exact get_pgen restatement
+* the PCHB and uniform (gen_rand_excit) generators: sampled frequencies
+  match p_gen and p_gen matches the exact get_pgen restatement
   (unit_tests/excitgen/pchb_excitgen_test_helper.F90, tolerance 0.15)
 """
 from __future__ import annotations
@@ -148,13 +148,16 @@ def test_alias_table_reproduces_distribution():
         np.testing.assert_allclose(p, w / w.sum(), rtol=1e-10, atol=1e-14)
 
 
-@pytest.mark.parametrize("which", ["pchb", "hubbard"])
+@pytest.mark.parametrize("which", ["pchb", "uniform", "hubbard"])
 def test_generator_pgen_diagnostic(which):
     """Draws from one determinant: every draw's p_gen equals the exact
     get_pgen restatement, and frequency / p_gen is 1 within 0.15 for
-    determinants drawn often enough."""
-    if which == "pchb":
-        spec = molecule(8, 4)
+    determinants drawn often enough.  The uniform generator reaches every
+    single and double of the determinant, so its p_gen sum to 1."""
+    if which in ("pchb", "uniform"):
+        h, eri, ecore = systems.synthetic_fcidump(8, 11)
+        gen = capi.EXGEN_PCHB if which == "pchb" else capi.EXGEN_UNIFORM
+        spec = systems.molecular_system(h, eri, ecore, 4, seed=12, excitgen=gen)
         o = orc.Oracle(spec, 16, 16)
         det = encode_det([1, 4, 5, 10], spec.nifd)
     else:
@@ -172,6 +175,9 @@ def test_generator_pgen_diagnostic(which):
     big = counts > 2000
     ratio = counts[big] / n / pg[big]
     assert np.all(np.abs(ratio - 1.0) < 0.15), ratio
+    if which == "uniform":
+        assert len(keys) == 2 * 6 + 2 * 6 + 15 + 15 + 4 * 36  # singles + aa + bb + ab doubles
+        assert abs(pg.sum() - 1.0) < 1e-12
     # hel of each draw equals the Slater-Condon element between the two
     hk = np.zeros(len(keys))
     hk[inv.ravel()] = hel[ok]
