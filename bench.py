@@ -4,13 +4,15 @@
 Workload (synthetic, seeded): molecular system from the synthetic FCIDUMP
 recipe -- 24 spatial orbitals, 10 electrons, Sz = 0 (48 spin orbitals, one
 64-bit determinant word), PCHB excitation generator, initiator FCIQMC with
-real coefficients, 1e7 walkers, tau from the excitation statistics
-(max |H_ij|/p_gen, walker-bloom limit 3).  A step is one PerformFCIMCycPar
+real coefficients, 1e7 walkers; tau starts from the excitation statistics
+of the reference (max |H_ij|/p_gen, walker-bloom limit 3) and is then set by
+the conventional tau search on the device during equilibration.  A step is one PerformFCIMCycPar
 over the whole walker list; a walker update is one unit of |C| processed
 (TotParts entering the step).
 
-  value   device time of K back-to-back steps (CUDA events on the engine
-          stream; walker list resident in HBM, working set > L2)
+  value   device time of K steps (CUDA events on the engine stream around
+          each step; L2 flushed before every step; walker list resident in
+          HBM)
   e2e     the same steps driven one at a time through the C ABI
           (neci_gpu_iterate: parameters host->device, stats device->host
           every step), timed on the host clock
@@ -28,7 +30,6 @@ import math
 import os
 import subprocess
 import sys
-import threading
 import time
 from pathlib import Path
 
@@ -40,6 +41,11 @@ UNIT = "walker updates/s"
 N_ORB, N_EL, SEED = 24, 10, 20240601
 TARGET_WALKERS = 1.0e7
 BLOOM = 3.0
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of
+# this workload at 1e7 walkers) per unit of work, for roofline.traffic:
+# kernel -> (bytes per unit, step count that is the unit).
+NCU_DRAM_BYTES_PER_UNIT = {}
 
 
 def workload_spec():
@@ -73,35 +79,39 @@ def peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms by one
+    nvidia-smi process that runs for the whole timed region."""
     FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.samples = []
-        self._stop = threading.Event()
-        self._th = None
-
-    def _run(self):
-        cmd = ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits"]
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(cmd, capture_output=True, text=True, timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        self._proc = None
 
     def __enter__(self):
-        self._th = threading.Thread(target=self._run, daemon=True)
-        self._th.start()
+        cmd = ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+               "-lms", "50"]
+        try:
+            self._proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)  # the first sample lands before the timed steps start
+        except OSError:
+            self._proc = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._th.join(timeout=10)
+        if self._proc is None:
+            return
+        self._proc.terminate()
+        try:
+            out, _ = self._proc.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self._proc.kill()
+            out, _ = self._proc.communicate()
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) == 6:
+                self.samples.append(f)
 
     def summary(self):
         if not self.samples:
@@ -144,19 +154,27 @@ def run_gpu(args, rank, world):
     from neci_stable_gb300.engine import Engine
     from neci_stable_gb300.fcimc import CalcParams, FciMCPar
 
+    import torch
     spec = workload_spec()
-    max_walkers = int(3.0e7)
-    max_spawned = int(4.0e7)
+    max_walkers = int(3.0 * args.walkers)
+    max_spawned = int(4.0 * args.walkers)
     eng = Engine(spec, max_walkers, max_spawned, device=0)
-    tau = estimate_tau(eng)
-    calc = CalcParams(tau=tau, target_walkers=args.walkers, steps_sft=10, sft_damp=0.05,
-                      seed=SEED + 1000 * rank, precision=capi.PREC_FP64)
+    # written between timed steps so that no step starts with a warm L2 (129 MB)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda:0")  # 256 MB
+    tau0 = estimate_tau(eng)
+    # the conventional tau search runs on the device over the first half of
+    # the equilibration (max_iter stop method), starting from tau0
+    calc = CalcParams(tau=tau0, target_walkers=args.walkers, steps_sft=10, sft_damp=0.05,
+                      seed=SEED + 1000 * rank, precision=capi.PREC_FP64, tau_search=True,
+                      tau_search_max_iter=max(args.equil // 2, 20))
     drv = FciMCPar(eng, calc)
     # start: the population on the reference, shift varying from the start
     eng.start_from_reference(initial_part=args.walkers)
     drv.single_part_phase = [False] * eng.L
     drv.diag_sft = [0.0] * eng.L
     equil = drv.run(args.equil)  # untimed equilibration of the walker distribution
+    tau = drv.calc.tau
+    tau_info = {"start": tau0, "final": tau, "cycles_searched": len(equil.tau)}
     p = drv.params()
     # warm-up steps (untimed)
     eng.iterate_n(p, args.warmup)
@@ -167,25 +185,49 @@ def run_gpu(args, rank, world):
         dist.barrier()
     eng.lib.neci_gpu_sync(eng.ctx)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        stats, dev_ms = eng.iterate_timed(p, args.steps)
-    p.iter += args.steps
+        # Each step is timed alone by CUDA events on the engine stream, with
+        # L2 flushed (256 MB written) before it.  Cycles of StepsSft steps
+        # alternate FP64 and mixed precision, and the shift is updated after
+        # every cycle (update_shift), so that both precisions step the same,
+        # stationary population.
+        timed = {capi.PREC_FP64: [[], 0.0], capi.PREC_MIXED: [[], 0.0]}
+        steps_sft = drv.calc.steps_sft
+        old = None
+        k = 0
+        while len(timed[capi.PREC_MIXED][0]) < args.steps:
+            for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+                pc = drv.params()
+                pc.precision = prec
+                n = min(steps_sft, args.steps - len(timed[prec][0]))
+                for _ in range(n):
+                    flush.fill_(float(k))
+                    k += 1
+                    torch.cuda.synchronize()
+                    st1, ms = eng.iterate_timed(pc, 1)
+                    pc.iter += 1
+                    timed[prec][0].extend(st1)
+                    timed[prec][1] += ms
+                drv.iter = pc.iter
+                parts = timed[prec][0][-1].tot_parts[0]
+                if old is not None:
+                    drv.diag_sft[0] -= math.log(parts / old) * drv.calc.sft_damp / (drv.calc.tau * steps_sft)
+                old = parts
+        stats, dev_ms = timed[capi.PREC_FP64]
+        mstats, mixed_ms = timed[capi.PREC_MIXED]
+        p = drv.params()
+        # the same number of FP64 steps back to back (CUDA graph replays, no flush)
+        bb_stats, bb_ms = eng.iterate_timed(p, args.steps)
+        p.iter += args.steps
+        # ---- e2e: one C-ABI call per step with host buffers
+        t0 = time.perf_counter()
+        e2e_updates = 0.0
+        for _ in range(args.steps):
+            st = eng.perform_fcimc_cyc_par(p)
+            p.iter += 1
+            e2e_updates += st.tot_parts_old[0]
+        e2e_s = time.perf_counter() - t0
     updates = sum(s.tot_parts_old[0] for s in stats)
-    # ---- e2e: one C-ABI call per step with host buffers
-    t0 = time.perf_counter()
-    e2e_updates = 0.0
-    for k in range(args.steps):
-        st = eng.perform_fcimc_cyc_par(p)
-        p.iter += 1
-        e2e_updates += st.tot_parts_old[0]
-    e2e_s = time.perf_counter() - t0
-    # ---- the same steps with FP32 spawn amplitudes (mixed precision)
-    pm = drv.params()
-    pm.iter = p.iter
-    pm.precision = capi.PREC_MIXED
-    eng.iterate_n(pm, 3)
-    pm.iter += 3
-    mstats, mixed_ms = eng.iterate_timed(pm, args.steps)
-    p.iter = pm.iter + args.steps
+    bb_updates = sum(s.tot_parts_old[0] for s in bb_stats)
     mixed_updates = sum(s.tot_parts_old[0] for s in mstats)
     # ---- per-kernel timing pass (events around each kernel; not the timed number)
     eng.set_profiling(True)
@@ -195,9 +237,11 @@ def run_gpu(args, rank, world):
     eng.set_profiling(False)
     last = prof_stats[-1].as_dict()
     return {
-        "eng": eng, "spec": spec, "tau": tau, "updates": updates, "dev_ms": dev_ms, "clk": clk.summary(),
+        "eng": eng, "spec": spec, "tau": tau, "tau_info": tau_info, "updates": updates, "dev_ms": dev_ms, "clk": clk.summary(),
         "e2e_updates": e2e_updates, "e2e_s": e2e_s, "ktimes": ktimes, "last": last, "stats": stats,
-        "equil": equil, "mixed_updates": mixed_updates, "mixed_ms": mixed_ms,
+        "first": stats[0].as_dict(),
+        "equil": equil, "mixed_updates": mixed_updates, "mixed_ms": mixed_ms, "bb_updates": bb_updates,
+        "bb_ms": bb_ms,
     }
 
 
@@ -282,101 +326,125 @@ def run_batched(args):
                         "walkers 1e4..1e6 log-uniform, replica pairs, PCHB"}
 
 
+class OracleSample:
+    """The CPU restatement of the iteration (the oracle) on one core: a
+    `walkers`-walker population of the workload, equilibrated for
+    equil_cycles x 10 steps with the conventional tau search (update_tau on
+    the oracle's own logs, as on the device) and the shift following the
+    population; `step(seconds)` then runs iterations for that long."""
+
+    def __init__(self, seed, walkers=20000.0, equil_cycles=8):
+        import numpy as np
+        from neci_stable_gb300.fcimc import TauSearch
+        from neci_stable_gb300.systems import encode_det, make_rows
+        from oracle.oracle import Oracle
+        spec = workload_spec()
+        self.seed = seed
+        self.orc = Oracle(spec, 2_000_000, 4_000_000)
+        ref = encode_det(spec.reference, spec.nifd)
+        self.orc.upload(make_rows(ref[None], np.array([[walkers]]), np.array([1 << 13])))
+        self.orc.set_tau_search(True)
+        ts = TauSearch(consider_par_bias=True, p_singles=spec.p_singles, p_parallel=spec.p_parallel)
+        self.tau, self.shift, self.old, self.it, self.n = 0.0014, 0.0, walkers, 0, 0
+        for _ in range(equil_cycles):
+            for _ in range(10):
+                st = self._iterate()
+            self.tau, ps, pp = ts.update(self.orc.tau_stats(), self.tau)
+            self.orc.set_excit_biases(ps, pp)
+            self._update_shift(st)
+        self.orc.set_tau_search(False)
+        self.p_singles, self.p_parallel = ts.p_singles, ts.p_parallel
+
+    def _iterate(self):
+        from neci_stable_gb300 import capi
+        self.it += 1
+        st, rc = self.orc.iterate(capi.default_params(tau=self.tau, seed=self.seed, iter=self.it,
+                                                      diag_sft=[self.shift, self.shift]))
+        if rc:
+            raise RuntimeError(f"oracle iteration failed with {rc}")
+        return st
+
+    def _update_shift(self, st):
+        self.shift -= 0.05 * math.log(st.tot_parts[0] / self.old) / (self.tau * 10)
+        self.old = st.tot_parts[0]
+
+    def step(self, seconds):
+        t0 = time.perf_counter()
+        upd, n = 0.0, 0
+        while time.perf_counter() - t0 < seconds:
+            st = self._iterate()
+            upd += st.tot_parts_old[0]
+            n += 1
+            self.n += 1
+            if self.n % 10 == 0:
+                self._update_shift(st)
+        return upd, time.perf_counter() - t0, n
+
+    def describe(self):
+        return f"tau {self.tau:.4g}, pSingles {self.p_singles:.3f}, pParallel {self.p_parallel:.3f}"
+
+
 def cpu_baseline_sample(seconds=12.0):
     """Oracle (CPU restatement) on one core: a 20 000-walker sample of the workload."""
-    from neci_stable_gb300 import capi
-    from oracle.oracle import Oracle
-    from neci_stable_gb300.systems import encode_det, make_rows
-    import numpy as np
-    spec = workload_spec()
-    orc = Oracle(spec, 2_000_000, 4_000_000)
-    ref = encode_det(spec.reference, spec.nifd)
-    orc.upload(make_rows(ref[None], np.array([[20000.0]]), np.array([1 << 13])))
-    p = capi.default_params(tau=0.01, seed=5, iter=1)
-    # short equilibration with the shift tracking the population
-    shift = 0.0
-    old = 20000.0
-    for it in range(1, 41):
-        p.iter = it
-        p.diag_sft[0] = shift
-        st, rc = orc.iterate(p)
-        if it % 10 == 0:
-            shift -= 0.05 * math.log(st.tot_parts[0] / old) / (0.01 * 10)
-            old = st.tot_parts[0]
-    t0 = time.perf_counter()
-    upd = 0.0
-    n = 0
-    while time.perf_counter() - t0 < seconds:
-        n += 1
-        p.iter = 100 + n
-        st, rc = orc.iterate(p)
-        upd += st.tot_parts_old[0]
-    dt = time.perf_counter() - t0
+    smp = OracleSample(5)
+    upd, dt, n = smp.step(seconds)
     return {"value": upd / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"oracle on the n24/e10 synthetic FCIDUMP, 20000-walker sample, {n} steps in {dt:.1f} s"}
+            "sample": f"oracle on the n24/e10 synthetic FCIDUMP, 20000-walker sample after its own tau search "
+                      f"({smp.describe()}), {n} steps in {dt:.1f} s"}
 
 
-def _ref_worker(args):
-    seconds, seed = args
-    import math as _m
-    from neci_stable_gb300 import capi
-    from oracle.oracle import Oracle
-    from neci_stable_gb300.systems import encode_det, make_rows
-    import numpy as np
-    spec = workload_spec()
-    orc = Oracle(spec, 2_000_000, 4_000_000)
-    ref = encode_det(spec.reference, spec.nifd)
-    orc.upload(make_rows(ref[None], np.array([[20000.0]]), np.array([1 << 13])))
-    p = capi.default_params(tau=0.01, seed=seed, iter=1)
-    shift, old = 0.0, 20000.0
-    for it in range(1, 31):
-        p.iter = it
-        p.diag_sft[0] = shift
-        st, rc = orc.iterate(p)
-        if it % 10 == 0:
-            shift -= 0.05 * _m.log(st.tot_parts[0] / old) / (0.01 * 10)
-            old = st.tot_parts[0]
-    t0 = time.perf_counter()
-    upd, n = 0.0, 0
-    while time.perf_counter() - t0 < seconds:
-        n += 1
-        p.iter = 100 + n
-        st, rc = orc.iterate(p)
-        upd += st.tot_parts_old[0]
-    return upd, time.perf_counter() - t0, n
+_SAMPLE = None
+
+
+def _ref_init(seed):
+    """Pool initializer: this process's equilibrated oracle sample."""
+    global _SAMPLE
+    _SAMPLE = OracleSample(seed + os.getpid() % 1000)
+
+
+def _ref_worker(seconds):
+    upd, dt, n = _SAMPLE.step(seconds)
+    return upd, dt, n, _SAMPLE.describe()
 
 
 def run_reference(args, rank, world):
-    """CPU restatement of the reference's iteration on all host cores."""
+    """CPU restatement of the reference's iteration on all host cores: one
+    equilibrated 20000-walker oracle per process; a step is one round of
+    per_step seconds of iterations on every process, timed on the host clock
+    around the round."""
     if rank != 0:
         return None
     import multiprocessing as mp
     from oracle import oracle as o
-    o.lib()  # build/load before forking workers
+    o.lib()  # build/load before the workers start
     cores = os.cpu_count() or 1
-    per_step = max(0.5, min(4.0, 150.0 / max(args.steps, 1)))
+    per_step = max(0.25, min(2.0, 90.0 / max(args.steps + args.warmup, 1)))
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     total_upd, total_s = 0.0, 0.0
     steps_done = 0
-    with ctx.Pool(cores) as pool:
+    desc = ""
+    with ctx.Pool(cores, initializer=_ref_init, initargs=(1000,)) as pool:
         for _ in range(args.warmup):
-            pool.map(_ref_worker, [(0.5, 100 + c) for c in range(cores)])
+            pool.map(_ref_worker, [per_step] * cores, chunksize=1)
         for k in range(args.steps):
-            res = pool.map(_ref_worker, [(per_step, 1000 + 17 * k + c) for c in range(cores)])
+            w0 = time.perf_counter()
+            res = pool.map(_ref_worker, [per_step] * cores, chunksize=1)
+            total_s += time.perf_counter() - w0
             total_upd += sum(r[0] for r in res)
-            total_s += max(r[1] for r in res)
             steps_done += sum(r[2] for r in res)
+            desc = res[0][3]
     value = total_upd / total_s
     return {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / max(args.steps, 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "synthetic FCIDUMP n=24 orbitals, 10 electrons, PCHB, initiator FCIQMC, real coefficients",
+        "config": {"workload": "synthetic FCIDUMP n=24 orbitals, 10 electrons, PCHB, initiator FCIQMC, real "
+                               "coefficients, conventional tau search",
                    "sample": "20000-walker population per core"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes x {per_step:.0f} s per step of the oracle iteration "
-                                   f"(20000 walkers each), {steps_done} iterations"},
+                         "sample": f"{cores} processes x {per_step:.2f} s per step of the oracle iteration "
+                                   f"(20000 walkers each, {desc}), {steps_done} iterations"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }
@@ -385,7 +453,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--equil", type=int, default=600, help="untimed equilibration iterations")
     ap.add_argument("--walkers", type=float, default=TARGET_WALKERS, help="target walker number")
@@ -442,12 +510,18 @@ def main():
     hbm, peak_kind = peaks()
     achieved = ab / (top_ms / 1e3) / 1e9
     traffic = None
-    tp = ROOT / "profiles" / "ncu_traffic.json"
-    if tp.exists():
-        tj = json.loads(tp.read_text())
-        if top in tj.get("bytes_per_unit", {}):
-            unit = tj["unit_of"][top]
-            traffic = tj["bytes_per_unit"][top] * r["last"][unit]
+    if top in NCU_DRAM_BYTES_PER_UNIT:
+        per_unit, unit = NCU_DRAM_BYTES_PER_UNIT[top]
+        traffic = per_unit * r["last"][unit]
+    # achieved GB/s of every kernel (algorithmic bytes of the last profiled step)
+    kernel_gbs = {}
+    for k, (ms, cnt) in kt.items():
+        b = algorithmic_bytes(k, r["last"], W, L)
+        if b > 0:
+            kernel_gbs[k] = b / (ms / cnt / 1e3) / 1e9
+    ann = ("ann_probe", "ann_compress", "ann_insert")
+    ann_ms = sum(kt[k][0] / kt[k][1] for k in ann if k in kt)
+    ann_bytes = sum(algorithmic_bytes(k, r["last"], W, L) for k in ann)
     launches_per_step = 11 + (1 if r["last"]["n_core"] > 0 else 0)
     line = {
         "metric": METRIC, "value": updates / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -455,20 +529,34 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "synthetic FCIDUMP n=24 orbitals (48 spin orbitals), 10 electrons, Sz=0, PCHB, "
                                f"initiator FCIQMC, real coefficients, FP64, {args.walkers:.3g} walkers",
-                   "tau": r["tau"], "walkers": r["stats"][-1].tot_parts[0],
-                   "determinants": r["stats"][-1].n_occupied, "l2": "working set larger than L2 (walker rows, "
-                   "hash and spawn buffers > 129 MB); no flush", "parallelism": f"replica x{world}"},
+                   "tau": r["tau"], "tau_search": r["tau_info"], "walkers": r["stats"][-1].tot_parts[0],
+                   "determinants": r["stats"][-1].n_occupied,
+                   "step_counts": {k: r["last"][k] for k in ("n_attempts", "n_spawned", "n_unique", "n_new",
+                                                             "tot_walkers")},
+                   "first_step_counts": {k: r["first"][k] for k in ("n_attempts", "n_spawned", "n_unique",
+                                                                    "n_new", "tot_walkers")},
+                   "l2": "flushed before every timed step (256 MB written); each step timed alone by CUDA events",
+                   "parallelism": f"replica x{world}"},
+        "value_back_to_back": {"value": r["bb_updates"] / (r["bb_ms"] / 1000.0), "unit": UNIT,
+                               "ms_per_step": r["bb_ms"] / args.steps,
+                               "note": "the same number of steps as CUDA-graph replays back to back, no flush"},
         "clocks": r["clk"],
         "e2e": {"value": e2e_upd / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 96, "d2h_bytes_per_step": 200},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": ab, "ms_per_launch": top_ms},
+                     "algorithmic_bytes": ab, "ms_per_launch": top_ms,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per unit of this workload"},
+        "annihilation_roofline": {"kernels": list(ann), "achieved": ann_bytes / (ann_ms / 1e3) / 1e9, "peak": hbm,
+                                  "unit": "GB/s", "frac": ann_bytes / (ann_ms / 1e3) / 1e9 / hbm,
+                                  "ms_per_step": ann_ms, "algorithmic_bytes": ann_bytes},
         "kernel_ms_per_step": {k: v[0] / v[1] for k, v in kt.items()},
+        "kernel_gbs": kernel_gbs,
         "mixed_precision": {"value": r["mixed_updates"] / (r["mixed_ms"] / 1000.0), "unit": UNIT,
                             "ms_per_step": r["mixed_ms"] / args.steps,
                             "speedup_vs_fp64": (r["mixed_updates"] / r["mixed_ms"]) / (updates / (dev_s * 1000.0)),
-                            "note": "FP32 H_ij, p_gen and spawn amplitude; FP64 death, E_proj and signs"},
+                            "note": "FP32 H_ij, p_gen and spawn amplitude; FP64 death, E_proj and signs; "
+                                    "cycles of 10 steps interleaved with the FP64 steps on the same population"},
     }
     if not args.no_batched and world == 1:
         line["batched"] = run_batched(args)

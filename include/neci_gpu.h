@@ -157,6 +157,12 @@ int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *umat, int64_t umat_le
 int32_t neci_gpu_set_lattice(neci_gpu_ctx *ctx, const int32_t *neighbours, int32_t nsites);
 /* iLutRef(0:NIfD) and Hii = <D0|H|D0> (FciMCData iLutRef, Hii). */
 int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ilut_ref, double hii);
+/* Changes pSingles and pParallel, as the conventional tau search does
+ * (update_tau, tau/tau_search_conventional.F90:274-499, which assigns the
+ * FciMCData globals pSingles/pDoubles/pParallel).  Takes effect from the
+ * next step; needs the reference set.                                    */
+int32_t neci_gpu_set_excit_biases(neci_gpu_ctx *ctx, double p_singles, double p_parallel);
+
 /* Builds the PCHB alias tables on the device from UMAT
  * (gasci_pchb_doubles_spatorb_fastweighted.fpp compute_samplers).        */
 int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx);
@@ -201,6 +207,28 @@ int32_t neci_gpu_iterate_timed(neci_gpu_ctx *ctx, const neci_gpu_iter_params *pa
  * builds, CMakeLists.txt:97-106). */
 int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gpu_iter_params *params,
                                int32_t n_iter, neci_gpu_iter_stats *stats, double *device_ms);
+
+/* ---- conventional tau search --------------------------------------------
+ * With the search on, every step logs, for each generated excitation that
+ * reaches attempt_create, gamma = |H_ij| / (p_gen / p_class) into the
+ * maximum of its class (log_spawn_magnitude,
+ * tau/tau_search_conventional.F90:138-258; classes sing, doub for the
+ * uniform generator, par/opp for PCHB's parallel/opposite-spin doubles) and,
+ * for every determinant that undergoes death, K_ii - S into max_death_cpt
+ * (log_death_magnitude, tau/tau_main.F90:197-206).  The maxima persist over
+ * steps until read with reset != 0; the host applies update_tau to them.
+ * The counts stop mattering past the reference's threshold of 50 and are
+ * reported capped at 51.                                                 */
+typedef struct {
+    double  gamma_sing;     /* max |H_ij| / (p_gen / pSingles), singles            */
+    double  gamma_doub;     /* max |H_ij| / (p_gen / pDoubles), uniform doubles    */
+    double  gamma_par;      /* ... / (pDoubles pParallel), same-spin PCHB doubles  */
+    double  gamma_opp;      /* ... / (pDoubles (1-pParallel)), opposite-spin       */
+    double  max_death_cpt;  /* max(K_ii - S) over the dying determinants, >= 0      */
+    int64_t cnt_sing, cnt_doub, cnt_par, cnt_opp;
+} neci_gpu_tau_stats;
+int32_t neci_gpu_set_tau_search(neci_gpu_ctx *ctx, int32_t on);
+int32_t neci_gpu_get_tau_stats(neci_gpu_ctx *ctx, neci_gpu_tau_stats *out, int32_t reset);
 
 /* ---- annihilation of an injected spawn list -----------------------------
  * CompressSpawnedList (Annihilation.F90:249-515) followed by

@@ -75,6 +75,18 @@ class IterStats(C.Structure):
         return out
 
 
+class TauStats(C.Structure):
+    """neci_gpu_tau_stats: the conventional tau search's class maxima."""
+    _fields_ = [
+        ("gamma_sing", C.c_double), ("gamma_doub", C.c_double), ("gamma_par", C.c_double),
+        ("gamma_opp", C.c_double), ("max_death_cpt", C.c_double),
+        ("cnt_sing", C.c_int64), ("cnt_doub", C.c_int64), ("cnt_par", C.c_int64), ("cnt_opp", C.c_int64),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 def default_params(**kw) -> IterParams:
     """NECI's defaults for an initiator run with real coefficients."""
     p = IterParams()
@@ -113,6 +125,9 @@ _SIGS = {
     "neci_gpu_set_lattice": (_i32, [_P, _P, _i32]),
     "neci_gpu_set_reference": (_i32, [_P, _P, _dbl]),
     "neci_gpu_init_pchb": (_i32, [_P]),
+    "neci_gpu_set_excit_biases": (_i32, [_P, _dbl, _dbl]),
+    "neci_gpu_set_tau_search": (_i32, [_P, _i32]),
+    "neci_gpu_get_tau_stats": (_i32, [_P, C.POINTER(TauStats), _i32]),
     "neci_gpu_upload_walkers": (_i32, [_P, _P, _i64, _P, _P]),
     "neci_gpu_download_walkers": (_i32, [_P, _P, _P, _P, _i64, _P]),
     "neci_gpu_iterate": (_i32, [_P, C.POINTER(IterParams), C.POINTER(IterStats)]),

@@ -5,6 +5,7 @@
 // once into a CUDA graph and replayed every step).
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -110,21 +111,35 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, advance); });
 }
 
+// Destroys the cached step graphs (after any change the kernels see by value).
+void drop_graphs(Engine &e) {
+    for (int k = 0; k < 2; ++k)
+        if (e.graphs[k]) {
+            cudaGraphExecDestroy(e.graphs[k]);
+            e.graphs[k] = nullptr;
+        }
+    e.graph = nullptr;
+}
+
+// Makes e.graph the step graph of the current precision; one graph per
+// precision is kept, so that steps of both precisions can alternate.
 int ensure_graph(Engine &e) {
     const bool core = e.st.n_core > 0;
-    if (e.graph && e.graph_core == core && e.graph_prec == e.h_params->precision) return NECI_GPU_OK;
-    if (e.graph) {
-        cudaGraphExecDestroy(e.graph);
-        e.graph = nullptr;
+    const int k = e.h_params->precision == NECI_PREC_MIXED ? 1 : 0;
+    if (e.graphs[k] && e.graph_core[k] != core) {
+        cudaGraphExecDestroy(e.graphs[k]);
+        e.graphs[k] = nullptr;
     }
-    cudaGraph_t g;
-    CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
-    step_sequence(e, e.d_stats + e.max_stats, 1);  // scratch record, copied out per step
-    CK(cudaStreamEndCapture(e.stream, &g));
-    CK(cudaGraphInstantiate(&e.graph, g, 0));
-    cudaGraphDestroy(g);
-    e.graph_core = core;
-    e.graph_prec = e.h_params->precision;
+    if (!e.graphs[k]) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
+        step_sequence(e, e.d_stats + e.max_stats, 1);  // scratch record, copied out per step
+        CK(cudaStreamEndCapture(e.stream, &g));
+        CK(cudaGraphInstantiate(&e.graphs[k], g, 0));
+        cudaGraphDestroy(g);
+        e.graph_core[k] = core;
+    }
+    e.graph = e.graphs[k];
     return NECI_GPU_OK;
 }
 
@@ -257,7 +272,7 @@ int32_t neci_gpu_free(neci_gpu_ctx *ctx) {
     Engine &e = ctx->e;
     cudaSetDevice(e.device);
     if (e.stream) cudaStreamSynchronize(e.stream);
-    if (e.graph) cudaGraphExecDestroy(e.graph);
+    drop_graphs(e);
     for (void *p : e.allocs) cudaFree(p);
     if (e.h_params) cudaFreeHost(e.h_params);
     if (e.h_stats) cudaFreeHost(e.h_stats);
@@ -293,7 +308,7 @@ int32_t neci_gpu_set_tmat(neci_gpu_ctx *ctx, const double *t) {
     CK(cudaStreamSynchronize(e.stream));
     e.sys.tmat = d;
     e.sys.tmat32 = d32;
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    drop_graphs(e);
     return NECI_GPU_OK;
 }
 
@@ -310,10 +325,24 @@ int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *u, int64_t len) {
     float *d32 = nullptr;
     if (int r = dalloc(e, &d32, (size_t)len)) return r;
     CK(cudaMemcpyAsync(d32, u32.data(), (size_t)len * sizeof(float), cudaMemcpyHostToDevice, e.stream));
-    CK(cudaStreamSynchronize(e.stream));
     e.sys.umat = d;
     e.sys.umat32 = d32;
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    // Coulomb and exchange rows of the singles (nBI^3 each, FP64 and FP32)
+    const size_t n3 = (size_t)e.sys.nBI * e.sys.nBI * e.sys.nBI;
+    double *jr = nullptr, *kr = nullptr;
+    float *jr32 = nullptr, *kr32 = nullptr;
+    if (int r = dalloc(e, &jr, n3)) return r;
+    if (int r = dalloc(e, &kr, n3)) return r;
+    if (int r = dalloc(e, &jr32, n3)) return r;
+    if (int r = dalloc(e, &kr32, n3)) return r;
+    launch_build_jk(e, jr, kr, jr32, kr32);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e.stream));
+    e.sys.jrow = jr;
+    e.sys.krow = kr;
+    e.sys.jrow32 = jr32;
+    e.sys.krow32 = kr32;
+    drop_graphs(e);
     return NECI_GPU_OK;
 }
 
@@ -330,29 +359,16 @@ int32_t neci_gpu_set_lattice(neci_gpu_ctx *ctx, const int32_t *nb, int32_t nsite
     CK(cudaStreamSynchronize(e.stream));
     e.sys.neighbours = d;
     e.sys.nsites = nsites;
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    drop_graphs(e);
     return NECI_GPU_OK;
 }
 
-int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii) {
-    if (int r = check_ctx(ctx)) return r;
-    if (!ref) return fail(NECI_GPU_ERR_INVALID, "null reference");
-    Engine &e = ctx->e;
-    int na = 0, nb = 0, ne = 0;
-    for (int w = 0; w < kMaxWords; ++w) e.sys.ilut_ref[w] = 0;
-    for (int w = 0; w < e.sys.W; ++w) {
-        const unsigned long long x = (unsigned long long)ref[w];
-        e.sys.ilut_ref[w] = x;
-        na += __builtin_popcountll(x & 0xAAAAAAAAAAAAAAAAull);
-        nb += __builtin_popcountll(x & 0x5555555555555555ull);
-    }
-    ne = na + nb;
-    if (ne != e.sys.nel) return fail(NECI_GPU_ERR_INVALID, "reference has the wrong electron count");
-    e.sys.nOccAlpha = na;
-    e.sys.nOccBeta = nb;
-    e.sys.hii = hii;
-    // hoisted constants of the generators (pick_biased_elecs pgen,
-    // excit_gens_int_weighted.F90:770-790; pDoubles = 1 - pSingles)
+// Hoisted constants of the excitation generators from pSingles, pParallel
+// and the reference's alpha/beta counts (pick_biased_elecs pgen,
+// excit_gens_int_weighted.F90:770-790; pDoubles = 1 - pSingles), and the
+// factors of the tau-search log.
+static void derive_generator_constants(Engine &e) {
+    const int na = e.sys.nOccAlpha, nb = e.sys.nOccBeta;
     DevSys &s = e.sys;
     const int par = na * (na - 1) / 2 + nb * (nb - 1) / 2;
     s.pgen_par = s.p_parallel / (double)par;
@@ -405,8 +421,86 @@ int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii
     s.f_inv_opp = (float)s.inv_opp;
     s.f_inv_pdoub = (float)s.inv_pdoub;
     s.f_inv_psingles = (float)s.inv_psingles;
+    // gamma = |H_ij| / (p_gen / p_class) (tau_search_conventional.F90:149-202);
+    // the real-space Hubbard model runs with pSingles = 1
+    // (real_space_hubbard.F90:231)
+    s.tau_fac[TC_SING] = s.system == NECI_SYS_HUBBARD_REAL_SPACE ? 1.0 : s.p_singles;
+    s.tau_fac[TC_DOUB] = s.p_doubles;
+    s.tau_fac[TC_PAR] = s.p_doubles * s.p_parallel;
+    s.tau_fac[TC_OPP] = s.p_doubles * (1.0 - s.p_parallel);
+    for (int k = 0; k < 4; ++k) s.f_tau_fac[k] = (float)s.tau_fac[k];
+}
+
+int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!ref) return fail(NECI_GPU_ERR_INVALID, "null reference");
+    Engine &e = ctx->e;
+    int na = 0, nb = 0, ne = 0;
+    for (int w = 0; w < kMaxWords; ++w) e.sys.ilut_ref[w] = 0;
+    for (int w = 0; w < e.sys.W; ++w) {
+        const unsigned long long x = (unsigned long long)ref[w];
+        e.sys.ilut_ref[w] = x;
+        na += __builtin_popcountll(x & 0xAAAAAAAAAAAAAAAAull);
+        nb += __builtin_popcountll(x & 0x5555555555555555ull);
+    }
+    ne = na + nb;
+    if (ne != e.sys.nel) return fail(NECI_GPU_ERR_INVALID, "reference has the wrong electron count");
+    e.sys.nOccAlpha = na;
+    e.sys.nOccBeta = nb;
+    e.sys.hii = hii;
+    derive_generator_constants(e);
     e.have_ref = true;
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    drop_graphs(e);
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_excit_biases(neci_gpu_ctx *ctx, double p_singles, double p_parallel) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!(p_singles >= 0.0 && p_singles < 1.0) || !(p_parallel > 0.0 && p_parallel < 1.0))
+        return fail(NECI_GPU_ERR_INVALID, "pSingles must lie in [0, 1) and pParallel in (0, 1)");
+    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
+    e.desc.p_singles = p_singles;
+    e.desc.p_parallel = p_parallel;
+    e.sys.p_parallel = p_parallel;
+    derive_generator_constants(e);
+    drop_graphs(e);
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_tau_search(neci_gpu_ctx *ctx, int32_t on) {
+    if (int r = check_ctx(ctx)) return r;
+    ctx->e.sys.tau_search = on ? 1 : 0;
+    drop_graphs(ctx->e);
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_get_tau_stats(neci_gpu_ctx *ctx, neci_gpu_tau_stats *out, int32_t reset) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!out) return fail(NECI_GPU_ERR_INVALID, "null argument");
+    Engine &e = ctx->e;
+    unsigned long long h[9];
+    CK(cudaMemcpyAsync(h, &e.st.ctl->tau_gamma[0], sizeof(h), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    double g[5];
+    std::memcpy(g, h, 4 * sizeof(double));
+    std::memcpy(&g[4], &h[8], sizeof(double));
+    out->gamma_sing = g[TC_SING];
+    out->gamma_doub = g[TC_DOUB];
+    out->gamma_par = g[TC_PAR];
+    out->gamma_opp = g[TC_OPP];
+    out->max_death_cpt = g[4];
+    // the counts only decide whether more than cnt_threshold excitations were
+    // seen (the reference stops counting there); report them capped alike
+    const long long cap = kTauCntThreshold + 1;
+    out->cnt_sing = std::min<long long>((long long)h[4 + TC_SING], cap);
+    out->cnt_doub = std::min<long long>((long long)h[4 + TC_DOUB], cap);
+    out->cnt_par = std::min<long long>((long long)h[4 + TC_PAR], cap);
+    out->cnt_opp = std::min<long long>((long long)h[4 + TC_OPP], cap);
+    if (reset) {
+        CK(cudaMemsetAsync(&e.st.ctl->tau_gamma[0], 0, sizeof(h), e.stream));
+        CK(cudaStreamSynchronize(e.stream));
+    }
     return NECI_GPU_OK;
 }
 
@@ -465,7 +559,7 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e.stream));
     e.have_pchb = true;
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    drop_graphs(e);
     return NECI_GPU_OK;
 }
 
@@ -489,7 +583,8 @@ int32_t neci_gpu_upload_walkers(neci_gpu_ctx *ctx, const int64_t *ilut, int64_t 
     }
     Control c{};
     c.tot_walkers = (unsigned long long)nrows;
-    CK(cudaMemcpyAsync(e.st.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice, e.stream));
+    // the tau-search log at the end of the block outlives the walker list
+    CK(cudaMemcpyAsync(e.st.ctl, &c, offsetof(Control, tau_gamma), cudaMemcpyHostToDevice, e.stream));
     // the core space belongs to the previous list
     e.st.n_core = 0;
     if (nrows > 0) launch_upload_fix(e, nrows, compute);
@@ -498,7 +593,7 @@ int32_t neci_gpu_upload_walkers(neci_gpu_ctx *ctx, const int64_t *ilut, int64_t 
     int err = 0;
     CK(cudaMemcpy(&err, &e.st.ctl->err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) return fail(err, "upload: hash table full");
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    drop_graphs(e);
     return NECI_GPU_OK;
 }
 
@@ -873,7 +968,7 @@ int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core, int64_t 
     launch_core_fill(e, dcore, n_core);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e.stream));
-    if (e.graph) { cudaGraphExecDestroy(e.graph); e.graph = nullptr; }
+    drop_graphs(e);
     return NECI_GPU_OK;
 }
 

@@ -51,7 +51,18 @@ struct Control {
     int rehash;                         // rebuild the walker hash at the next step
     double nborn[2], ndied[2], nannihil[2], naborted[2], nremoved[2];
     double tot_parts[2], tot_parts_old[2], noat_hf[2], hf_cyc[2], enum_cyc[2], norm[2];
+    // tau search (log_spawn_magnitude / log_death_magnitude): kept across
+    // steps until the host resets them.  Maxima are the bit patterns of
+    // non-negative doubles, which order like the values.
+    unsigned long long tau_gamma[4];    // per TauClass
+    unsigned long long tau_cnt[4];
+    unsigned long long tau_death;       // max_death_cpt
 };
+
+// Excitation classes of the conventional tau search
+// (tau_search_conventional.F90:138-258).
+enum TauClass : int { TC_SING = 0, TC_DOUB = 1, TC_PAR = 2, TC_OPP = 3 };
+constexpr unsigned int kTauCntThreshold = 50;  // cnt_threshold
 
 // System description as seen by the kernels (passed by value).
 struct DevSys {
@@ -78,6 +89,11 @@ struct DevSys {
     float f_pgen_par, f_pgen_opp, f_p_doubles, f_p_singles, f_p_elec;
     float f_inv_nalpha;  // 1/nOccAlpha (0 without alpha electrons): pair index -> (alpha, beta) positions
     const float *umat32, *tmat32, *alias_prob32, *pexch32;
+    // Coulomb and exchange rows of the single-excitation elements:
+    // [((i-1) n + (a-1)) n + (k-1)] = <ik|ak> (jrow) and <ik|ka> (krow) for
+    // spatial orbitals i, a, k of n = nBI
+    const double *jrow, *krow;
+    const float *jrow32, *krow32;
     // reciprocals: the spawn amplitude multiplies by 1/p_gen built from them
     double inv_par, inv_opp, inv_pdoub, inv_psingles;
     float f_inv_par, f_inv_opp, f_inv_pdoub, f_inv_psingles;
@@ -88,6 +104,11 @@ struct DevSys {
     float f_pgen_unif[3], f_inv_unif[3];
     const double *alias_inv, *pexch_inv, *pnoexch_inv;   // 1/prob, 1/pExch, 1/(1-pExch)
     const float *alias_inv32, *pexch_inv32, *pnoexch_inv32;
+    // tau search: on/off, and per TauClass the factor that unbiases p_gen
+    // (pSingles, pDoubles, pDoubles pParallel, pDoubles (1 - pParallel))
+    int tau_search;
+    double tau_fac[4];
+    float f_tau_fac[4];
 };
 
 // Resident walker state (device pointers).
@@ -351,10 +372,12 @@ __device__ inline unsigned long long hash_mod(unsigned long long hash, unsigned 
 __device__ inline double tmat_el(const DevSys &s, int i, int j) {
     return __ldg(&s.tmat[(size_t)(j - 1) * s.nbasis + (i - 1)]);
 }
-__device__ inline long long umat_ind(int I, int J, int K, int L) {
-    long long A, B;
-    if (I > K) A = (long long)I * (I - 1) / 2 + K; else A = (long long)K * (K - 1) / 2 + I;
-    if (J > L) B = (long long)J * (J - 1) / 2 + L; else B = (long long)L * (L - 1) / 2 + J;
+// UMatInd (UMatCache.F90:257-306) in 32-bit arithmetic: with at most 128
+// spatial orbitals (kMaxWords) a pair index is at most 8256 and the result
+// at most 34,084,896.
+__device__ inline int umat_ind(int I, int J, int K, int L) {
+    const int A = I > K ? I * (I - 1) / 2 + K : K * (K - 1) / 2 + I;
+    const int B = J > L ? J * (J - 1) / 2 + L : L * (L - 1) / 2 + J;
     return A > B ? A * (A - 1) / 2 + B : B * (B - 1) / 2 + A;
 }
 __device__ inline double umat_el(const DevSys &s, int i, int j, int k, int l) {
@@ -364,25 +387,31 @@ __device__ inline int spat(int orb) { return (orb + 1) >> 1; }
 __device__ inline bool beta(int orb) { return orb & 1; }
 
 // sltcnd_1_kernel (sltcnd.fpp:643-679): Coulomb terms over the occupied
-// list, then exchange terms, then the one-electron element.
+// list, then exchange terms, then the one-electron element.  The terms are
+// read from the Coulomb and exchange rows of (id1, id2): jrow[k] =
+// <id1 k|id2 k>, krow[k] = <id1 k|k id2> (the same UMAT values, summed in
+// the same order).
 __device__ inline double sltcnd_1(const DevSys &s, const unsigned long long *d, int src, int tgt) {
     double hel = 0.0;
     const int id1 = spat(src), id2 = spat(tgt);
     if (beta(src) == beta(tgt)) {
+        const size_t row = ((size_t)(id1 - 1) * s.nBI + (id2 - 1)) * s.nBI - 1;
+        const double *jr = s.jrow + row, *kr = s.krow + row;
         for (int w = 0; w < s.W; ++w) {
             unsigned long long x = d[w];
             while (x) {
                 const int o = w * 64 + __ffsll((long long)x);
                 x &= x - 1;
-                if (o != src) hel += umat_el(s, id1, spat(o), id2, spat(o));
+                if (o != src) hel += __ldg(&jr[spat(o)]);
             }
         }
+        const unsigned long long same = beta(src) ? 0x5555555555555555ull : 0xAAAAAAAAAAAAAAAAull;
         for (int w = 0; w < s.W; ++w) {
-            unsigned long long x = d[w];
+            unsigned long long x = d[w] & same;
             while (x) {
                 const int o = w * 64 + __ffsll((long long)x);
                 x &= x - 1;
-                if (o != src && beta(o) == beta(src)) hel -= umat_el(s, id1, spat(o), spat(o), id2);
+                if (o != src) hel -= __ldg(&kr[spat(o)]);
             }
         }
     }

@@ -22,6 +22,7 @@ struct Excit {
     Real invp;  // 1/pgen as a product of reciprocal factors
     Real hel;
     int ic;
+    int cls;  // TauClass
     bool ok;
 };
 
@@ -42,26 +43,31 @@ __device__ inline float umat_r<float>(const DevSys &s, int i, int j, int k, int 
     return __ldg(&s.umat32[umat_ind(i, j, k, l) - 1]);
 }
 
-// sltcnd_1_kernel (sltcnd.fpp:643-679) in precision Real.
+// sltcnd_1_kernel (sltcnd.fpp:643-679) in precision Real, from the Coulomb
+// and exchange rows of (spat(src), spat(tgt)) in the same summation order.
 template <typename Real>
 __device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, int src, int tgt) {
     Real hel = 0;
     const int id1 = spat(src), id2 = spat(tgt);
     if (beta(src) == beta(tgt)) {
+        const size_t row = ((size_t)(id1 - 1) * s.nBI + (id2 - 1)) * s.nBI - 1;
+        const Real *jr = (sizeof(Real) == 8 ? (const Real *)s.jrow : (const Real *)s.jrow32) + row;
+        const Real *kr = (sizeof(Real) == 8 ? (const Real *)s.krow : (const Real *)s.krow32) + row;
         for (int w = 0; w < s.W; ++w) {
             unsigned long long x = d[w];
             while (x) {
                 const int o = w * 64 + __ffsll((long long)x);
                 x &= x - 1;
-                if (o != src) hel += umat_r<Real>(s, id1, spat(o), id2, spat(o));
+                if (o != src) hel += __ldg(&jr[spat(o)]);
             }
         }
+        const unsigned long long same = beta(src) ? kBetaBits : kAlphaBits;
         for (int w = 0; w < s.W; ++w) {
-            unsigned long long x = d[w];
+            unsigned long long x = d[w] & same;
             while (x) {
                 const int o = w * 64 + __ffsll((long long)x);
                 x &= x - 1;
-                if (o != src && beta(o) == beta(src)) hel -= umat_r<Real>(s, id1, spat(o), spat(o), id2);
+                if (o != src) hel -= __ldg(&kr[spat(o)]);
             }
         }
     }
@@ -96,6 +102,7 @@ template <typename Real>
 __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long *d,
                                       const int32_t *neigh, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
+    e.cls = TC_SING;
     e.ok = false;
     const int elec = 1 + (int)uniform_index(rng, (unsigned)s.nel);
     const int src = nth_orbital(d, s.W, kAllBits, elec);  // nI(elec)
@@ -135,6 +142,7 @@ __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long 
 template <typename Real>
 __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
+    e.cls = TC_SING;
     e.ok = false;
     const int norbs = s.nbasis / 2;
     int nalpha = 0, nbeta = 0;
@@ -218,6 +226,7 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     // Both spin cases run the same instructions (selects, no branches), so a
     // warp whose lanes drew different cases stays converged.
     const bool par = rng.next64() < s.thr_bias;
+    e.cls = par ? TC_PAR : TC_OPP;
     const int idx = (int)uniform_index(rng, par ? (unsigned)(aa + bb) : (unsigned)(s.nOccAlpha * s.nOccBeta));
     // parallel pair: positions a1 > a2 among the electrons of one spin
     const bool alpha_pair = idx < aa;
@@ -301,6 +310,7 @@ __device__ inline int nth_unoccupied(const DevSys &s, const unsigned long long *
 template <typename Real>
 __device__ inline void gen_uniform_double(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 2;
+    e.cls = TC_DOUB;
     e.ok = false;
     e.pgen = 0;
     const int nel = s.nel;

@@ -40,10 +40,11 @@ struct Engine {
     int max_stats = 0;
     std::vector<void *> allocs;
     bool have_ref = false, have_pchb = false;
-    // CUDA graph of one step (stats into d_stats[0])
+    // CUDA graph of one step per precision (FP64, mixed); `graph` is the one
+    // ensure_graph selected for the current parameters
+    cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+    bool graph_core[2] = {false, false};
     cudaGraphExec_t graph = nullptr;
-    bool graph_core = false;
-    int graph_prec = -1;
     // profiling
     bool profiling = false;
     cudaEvent_t ev[2 * K_NUM] = {};
@@ -79,5 +80,6 @@ void launch_core_mark(Engine &e, const long long *core_dets, long long n_core);
 void launch_core_count(Engine &e, const long long *core_dets, long long n_core, long long *counts);
 void launch_core_fill(Engine &e, const long long *core_dets, long long n_core);
 void launch_pchb_build(Engine &e);
+void launch_build_jk(Engine &e, double *jrow, double *krow, float *jrow32, float *krow32);
 
 }  // namespace neci

@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
     const int W = s.W, L = s.L, R = s.R;
     double acc_old[2] = {0.0, 0.0}, acc_hf[2] = {0.0, 0.0}, acc_en[2] = {0.0, 0.0};
     double acc_died[2] = {0.0, 0.0}, acc_born[2] = {0.0, 0.0}, acc_ab[2] = {0.0, 0.0};
+    double death_max = 0.0;  // max_death_cpt of this thread's determinants (tau search)
     unsigned long long acc_att = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;  // all lanes iterate together
@@ -307,6 +308,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             bool any = false;
             for (int k = 0; k < L; ++k) {
                 const double fac = p.tau * (Kii - p.diag_sft[k]);
+                if (s.tau_search) death_max = fmax(death_max, Kii - p.diag_sft[k]);  // log_death_magnitude
                 if (fac > 2.0) set_err(c, NECI_GPU_ERR_UNSTABLE);
                 double idie;
                 if (p.t_all_real_coeff) {
@@ -397,6 +399,16 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
     unsigned long long u[1] = {acc_att};
     unsigned long long *const du[1] = {&c->n_attempts};
     block_add_u<1>(u, du);
+    if (s.tau_search) {
+        // non-negative doubles order like their bit patterns
+        unsigned long long b = (unsigned long long)__double_as_longlong(death_max);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(0xffffffffu, b, o);
+            b = y > b ? y : b;
+        }
+        if ((threadIdx.x & 31) == 0 && b) atomicMax(&c->tau_death, b);
+    }
 }
 
 // ===========================================================================
@@ -487,17 +499,42 @@ __device__ inline void load_parent(const DevSys &s, const DevState &st, const It
     P.key = det_key(P.d, s.W, p.seed);
 }
 
+// Block-local tau-search log of k_spawn: per TauClass the largest gamma (as
+// bits) and the logged count, capped near the reference's threshold.
+struct TauAcc {
+    unsigned long long g[4];
+    unsigned int c[4];
+};
+
+// log_spawn_magnitude (tau_search_conventional.F90:138-258): gamma =
+// |H_ij| / (p_gen / p_class) of one generated excitation, taken as
+// |H_ij| (1/p_gen) p_class in precision Real.  Singles and uniform doubles
+// count when gamma > 0, parallel and opposite-spin doubles always.
+template <typename Real>
+__device__ inline void tau_log(const DevSys &s, const Excit<Real> &e, TauAcc *acc) {
+    double g;
+    if (sizeof(Real) == 8) g = fabs((double)e.hel) * (double)e.invp * s.tau_fac[e.cls];
+    else g = (double)(fabsf((float)e.hel) * (float)e.invp * s.f_tau_fac[e.cls]);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(g);
+    if (b > acc->g[e.cls]) atomicMax(&acc->g[e.cls], b);
+    const bool counts = (e.cls == TC_PAR || e.cls == TC_OPP) || g > 0.0;
+    if (counts && acc->c[e.cls] <= kTauCntThreshold) atomicAdd(&acc->c[e.cls], 1u);
+}
+
 // attempt_create for a generated excitation: the core -> core filter
 // (is_core_state, semi_stoch_procs.F90:547; those spawns are done by the
-// deterministic projection) and the rounded fixed-point amplitude.
+// deterministic projection), the tau-search log and the rounded fixed-point
+// amplitude.
 template <typename Real>
 __device__ inline long long attempt_create(const DevSys &s, const DevState &st, const IterParams &p, const Parent &P,
-                                           const Excit<Real> &e, Stream &rng, const int32_t *sh_rh2, int &ovf) {
+                                           const Excit<Real> &e, Stream &rng, const int32_t *sh_rh2, int &ovf,
+                                           TauAcc *tacc) {
     if (!e.ok) return 0;
     if (P.core) {
         const long long hs = hash_find(st, e.child, s.W, s.R, neci_hash(e.child, s.W, sh_rh2), st.ctl);
         if (hs >= 0 && is_core_flags(st.dets[hs * s.R + s.W + s.L])) return 0;
     }
+    if (s.tau_search) tau_log<Real>(s, e, tacc);
     return spawn_amplitude<Real>(p, e.hel, e.invp, P.neg, rng, ovf);
 }
 
@@ -522,7 +559,7 @@ __device__ inline void create_particle(const DevSys &s, const DevState &st, long
 // draws are those of an inline single.
 template <typename Real>
 __device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
-                                           unsigned long long w0, const int32_t *sh_rh2, int &ovf) {
+                                           unsigned long long w0, const int32_t *sh_rh2, int &ovf, TauAcc *tacc) {
     Parent P;
     Excit<Real> e;
     e.ok = false;
@@ -534,7 +571,7 @@ __device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, 
         Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
         (void)rng.next64();
         gen_uniform_single<Real>(s, P.d, rng, e);
-        qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf);
+        qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf, tacc);
     }
     create_particle<Real>(s, st, qv, P, e);
 }
@@ -550,12 +587,17 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
     extern __shared__ int32_t sh[];
     __shared__ unsigned long long sq[256];
     __shared__ int sq_n;
+    __shared__ TauAcc tacc;
     int32_t *sh_rh2 = sh;
     int32_t *sh_neigh = sh + (s.nbasis + 1);
     for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
     if (GEN == NECI_EXGEN_RS_HUBBARD)
         for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
     if (threadIdx.x == 0) sq_n = 0;
+    if (threadIdx.x < 4) {
+        tacc.g[threadIdx.x] = 0ull;
+        tacc.c[threadIdx.x] = 0u;
+    }
     __syncthreads();
     const IterParams p = *pp;
     const long long nat = (long long)min(st.ctl->n_att, (unsigned long long)st.max_att);
@@ -584,14 +626,14 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
                 else if (GEN == NECI_EXGEN_UNIFORM) gen_uniform_double<Real>(s, P.d, rng, e);
                 else gen_pchb_double<Real>(s, P.d, rng, e);
             }
-            qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf);
+            qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
         }
         create_particle<Real>(s, st, qv, P, e);
         if (GEN != NECI_EXGEN_RS_HUBBARD) {
             __syncthreads();
             const int n = sq_n;
             if (n >= nb) {
-                spawn_queued_single<Real>(s, st, p, true, sq[n - nb + threadIdx.x], sh_rh2, ovf);
+                spawn_queued_single<Real>(s, st, p, true, sq[n - nb + threadIdx.x], sh_rh2, ovf, &tacc);
                 __syncthreads();
                 if (threadIdx.x == 0) sq_n = n - nb;
                 __syncthreads();
@@ -603,9 +645,16 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
         const int n = sq_n;
         for (int b = 0; b < n; b += nb)
             spawn_queued_single<Real>(s, st, p, b + (int)threadIdx.x < n, b + threadIdx.x < n ? sq[b + threadIdx.x] : 0ull,
-                                      sh_rh2, ovf);
+                                      sh_rh2, ovf, &tacc);
     }
     if (ovf) set_err(st.ctl, NECI_GPU_ERR_OVERFLOW);
+    if (s.tau_search) {
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            if (tacc.g[threadIdx.x]) atomicMax(&st.ctl->tau_gamma[threadIdx.x], tacc.g[threadIdx.x]);
+            if (tacc.c[threadIdx.x]) atomicAdd(&st.ctl->tau_cnt[threadIdx.x], (unsigned long long)tacc.c[threadIdx.x]);
+        }
+    }
 }
 
 // ===========================================================================

@@ -151,6 +151,18 @@ class Engine:
         check(self.lib.neci_gpu_gen_excit(self.ctx, ptr(d), n, seed, it, ptr(child), ptr(pgen), ptr(hel)))
         return child, pgen, hel
 
+    # ------------------------------------------------------------ tau search
+    def set_tau_search(self, on: bool):
+        check(self.lib.neci_gpu_set_tau_search(self.ctx, 1 if on else 0))
+
+    def tau_stats(self, reset: bool = False) -> capi.TauStats:
+        t = capi.TauStats()
+        check(self.lib.neci_gpu_get_tau_stats(self.ctx, C.byref(t), 1 if reset else 0))
+        return t
+
+    def set_excit_biases(self, p_singles: float, p_parallel: float):
+        check(self.lib.neci_gpu_set_excit_biases(self.ctx, p_singles, p_parallel))
+
     # ---------------------------------------------------------------- timing
     def set_profiling(self, on: bool):
         check(self.lib.neci_gpu_set_profiling(self.ctx, 1 if on else 0))

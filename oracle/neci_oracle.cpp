@@ -176,6 +176,20 @@ struct Oracle {
     int nOccAlpha = 0, nOccBeta = 0;
     double p_doubles = 0.0;             // 1 - pSingles
 
+    // conventional tau search (tau/tau_search_conventional.F90:138-258,
+    // tau/tau_main.F90:197-206): class maxima of gamma and max_death_cpt
+    bool tau_search = false;
+    double tau_gamma[4] = {0.0, 0.0, 0.0, 0.0};  // sing, doub, par, opp
+    i64 tau_cnt[4] = {0, 0, 0, 0};
+    double tau_death = 0.0;
+    // factor that unbiases p_gen for class c: gamma = |H| (1/p_gen) factor
+    double tau_factor(int c) const {
+        if (c == 0) return sys.system == NECI_SYS_HUBBARD_REAL_SPACE ? 1.0 : sys.p_singles;  // pSingles = 1 on lattices
+        if (c == 1) return p_doubles;
+        if (c == 2) return p_doubles * sys.p_parallel;
+        return p_doubles * (1.0 - sys.p_parallel);
+    }
+
     // PCHB
     bool pchb_ready = false;
     int nBI = 0;
@@ -1093,6 +1107,19 @@ struct IterRun {
             i64 slot, h;
             if (o.hash_lookup(g.nJ, child.data(), slot, h) && o.is_core(o.row(slot))) return;
         }
+        if (o.tau_search) {
+            // log_spawn_magnitude: the class of the excitation (singles;
+            // uniform doubles; PCHB doubles by the spins of the two sources)
+            int c;
+            if (g.ic == 1) c = 0;
+            else if (o.sys.excitgen == NECI_EXGEN_UNIFORM) c = 1;
+            else c = Oracle::is_beta(g.ex[0][0]) == Oracle::is_beta(g.ex[0][1]) ? 2 : 3;
+            double gam;
+            if (sizeof(Real) == 8) gam = std::fabs((double)g.hel) * (double)g.invp * o.tau_factor(c);
+            else gam = (double)(std::fabs((float)g.hel) * (float)g.invp * (float)o.tau_factor(c));
+            if (gam > o.tau_gamma[c]) o.tau_gamma[c] = gam;
+            if (c >= 2 || gam > 0.0) o.tau_cnt[c] += 1;
+        }
         const i64 q = spawn_amplitude<Real>(g.hel, g.invp, neg, rng, ovf);
         if (q == 0) return;
         // create_particle (fcimc_helper.F90:152-308)
@@ -1314,6 +1341,7 @@ struct IterRun {
         Stream rng(det_key(r, o.W, p.seed), p.iter, P_DEATH, 0, 0);
         for (int k = 0; k < L; ++k) {
             const double fac = p.tau * (Kii - p.diag_sft[k]);
+            if (o.tau_search && Kii - p.diag_sft[k] > o.tau_death) o.tau_death = Kii - p.diag_sft[k];  // log_death_magnitude
             if (fac > 2.0) err = NECI_GPU_ERR_UNSTABLE;
             if (p.t_all_real_coeff) {
                 iDie[k] = fac * std::fabs(sgn[k]);
@@ -1605,6 +1633,35 @@ int32_t orc_set_reference(void *h, const int64_t *ref, double hii) {
     return NECI_GPU_OK;
 }
 int32_t orc_init_pchb(void *h) { return ((Oracle *)h)->init_pchb(); }
+
+int32_t orc_set_excit_biases(void *h, double p_singles, double p_parallel) {
+    Oracle *o = (Oracle *)h;
+    o->p_doubles = 1.0 - p_singles;
+    o->sys.p_singles = o->sys.excitgen == NECI_EXGEN_UNIFORM ? 1.0 - o->p_doubles : p_singles;
+    o->sys.p_parallel = p_parallel;
+    return NECI_GPU_OK;
+}
+int32_t orc_set_tau_search(void *h, int32_t on) {
+    ((Oracle *)h)->tau_search = on != 0;
+    return NECI_GPU_OK;
+}
+int32_t orc_get_tau_stats(void *h, neci_gpu_tau_stats *out, int32_t reset) {
+    Oracle *o = (Oracle *)h;
+    out->gamma_sing = o->tau_gamma[0];
+    out->gamma_doub = o->tau_gamma[1];
+    out->gamma_par = o->tau_gamma[2];
+    out->gamma_opp = o->tau_gamma[3];
+    out->max_death_cpt = o->tau_death;
+    out->cnt_sing = std::min<i64>(o->tau_cnt[0], 51);
+    out->cnt_doub = std::min<i64>(o->tau_cnt[1], 51);
+    out->cnt_par = std::min<i64>(o->tau_cnt[2], 51);
+    out->cnt_opp = std::min<i64>(o->tau_cnt[3], 51);
+    if (reset) {
+        for (int c = 0; c < 4; ++c) { o->tau_gamma[c] = 0.0; o->tau_cnt[c] = 0; }
+        o->tau_death = 0.0;
+    }
+    return NECI_GPU_OK;
+}
 
 int32_t orc_upload_walkers(void *h, const int64_t *ilut, int64_t nrows, const double *dh, const double *odh) {
     Oracle *o = (Oracle *)h;

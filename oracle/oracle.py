@@ -41,6 +41,9 @@ def _load():
         "orc_set_lattice": [_P, _P, C.c_int32],
         "orc_set_reference": [_P, _P, C.c_double],
         "orc_init_pchb": [_P],
+        "orc_set_excit_biases": [_P, C.c_double, C.c_double],
+        "orc_set_tau_search": [_P, C.c_int32],
+        "orc_get_tau_stats": [_P, C.POINTER(capi.TauStats), C.c_int32],
         "orc_upload_walkers": [_P, _P, C.c_int64, _P, _P],
         "orc_download_walkers": [_P, _P, _P, _P, C.c_int64, _P],
         "orc_iterate": [_P, C.POINTER(capi.IterParams), C.POINTER(capi.IterStats)],
@@ -142,6 +145,18 @@ class Oracle:
         n = C.c_int64()
         _ok(lib().orc_download_walkers(self.h, _ptr(rows), _ptr(dh), _ptr(odh), max_rows, C.byref(n)))
         return rows[: n.value], dh[: n.value], odh[: n.value]
+
+    def set_tau_search(self, on: bool):
+        _ok(lib().orc_set_tau_search(self.h, 1 if on else 0))
+
+    def tau_stats(self, reset: bool = False):
+        import neci_stable_gb300.capi as capi
+        t = capi.TauStats()
+        _ok(lib().orc_get_tau_stats(self.h, C.byref(t), 1 if reset else 0))
+        return t
+
+    def set_excit_biases(self, p_singles: float, p_parallel: float):
+        _ok(lib().orc_set_excit_biases(self.h, p_singles, p_parallel))
 
     def iterate(self, params):
         import neci_stable_gb300.capi as capi

@@ -56,6 +56,7 @@ def _c_layout(struct_name):
 
 
 @pytest.mark.parametrize("cls,name", [(capi.System, "neci_gpu_system"), (capi.IterParams, "neci_gpu_iter_params"),
-                                      (capi.IterStats, "neci_gpu_iter_stats")])
+                                      (capi.IterStats, "neci_gpu_iter_stats"),
+                                      (capi.TauStats, "neci_gpu_tau_stats")])
 def test_struct_sizes_match_header(cls, name):
     assert C.sizeof(cls) == _c_layout(name)

@@ -219,3 +219,69 @@ def test_batched_steps_equal_single_steps():
         e.iterate_n(p, 12)
     for a, b, sp in zip(batch, single, specs):
         assert np.array_equal(canonical(a.download()[0], sp.W), canonical(b.download()[0], sp.W))
+
+
+@pytest.mark.parametrize("name,iters,pop,tau,precision", [
+    ("hub10", 15, 50.0, 0.02, capi.PREC_FP64), ("mol24", 12, 200.0, 0.005, capi.PREC_FP64),
+    ("mol24", 10, 200.0, 0.005, capi.PREC_MIXED), ("mol12u", 15, 40.0, 0.02, capi.PREC_FP64)])
+def test_tau_search_log_bit_exact(name, iters, pop, tau, precision):
+    """log_spawn_magnitude / log_death_magnitude: the class maxima of gamma
+    and max_death_cpt match the oracle bit for bit after every step, and a
+    change of pSingles/pParallel (update_tau's new biases) mid-run keeps the
+    walker lists identical."""
+    spec, eng, orc = pair(name, 400_000, 800_000)
+    eng.set_tau_search(True)
+    orc.set_tau_search(True)
+    eng.tau_stats(reset=True)
+    orc.tau_stats(reset=True)
+    try:
+        eng.start_from_reference(initial_part=pop)
+        orc.upload(eng.download()[0])
+        W, L = spec.W, spec.lenof_sign
+        for it in range(1, iters + 1):
+            if it == iters // 2 and spec.kind == capi.SYS_MOLECULAR:
+                ps = 0.05 if spec.generator == capi.EXGEN_PCHB else 0.2
+                eng.set_excit_biases(ps, 0.3)
+                orc.set_excit_biases(ps, 0.3)
+            p = capi.default_params(tau=tau, diag_sft=[-0.5, -0.5], seed=77, iter=it, precision=precision)
+            sg = eng.perform_fcimc_cyc_par(p)
+            sc, rc = orc.iterate(p)
+            assert rc == 0 and sg.err == 0
+            tg, tc = eng.tau_stats().as_dict(), orc.tau_stats().as_dict()
+            assert tg == tc, (it, tg, tc)
+            rg = canonical(eng.download()[0], W)
+            rcpu = canonical(orc.download()[0], W)
+            assert np.array_equal(rg[:, : W + L], rcpu[:, : W + L]), it
+        t = eng.tau_stats(reset=True)
+        assert t.max_death_cpt > 0.0
+        if spec.kind == capi.SYS_HUBBARD_REAL_SPACE:
+            assert t.gamma_sing > 0.0 and t.gamma_doub == 0.0 and t.cnt_sing == 51
+        elif spec.generator == capi.EXGEN_PCHB:
+            assert t.gamma_par > 0.0 and t.gamma_opp > 0.0 and t.cnt_opp == 51
+        else:
+            assert t.gamma_doub > 0.0 and t.cnt_doub == 51
+        z = eng.tau_stats()
+        assert z.gamma_sing == 0.0 and z.max_death_cpt == 0.0 and z.cnt_opp == 0
+    finally:
+        eng.set_tau_search(False)
+        orc.set_tau_search(False)
+        if spec.kind == capi.SYS_MOLECULAR:
+            eng.set_excit_biases(spec.p_singles, spec.p_parallel)
+            orc.set_excit_biases(spec.p_singles, spec.p_parallel)
+
+
+def test_tau_search_run_settles_tau():
+    """A run with the conventional tau search (FciMCPar + update_tau on the
+    device's logs) moves tau to the bloom limit and stops searching when the
+    shift starts to vary."""
+    from neci_stable_gb300.fcimc import CalcParams, FciMCPar
+    spec = molecule(24, 10)
+    eng = Engine(spec, 400_000, 800_000)
+    eng.start_from_reference(initial_part=20.0)
+    drv = FciMCPar(eng, CalcParams(tau=0.05, target_walkers=3000, steps_sft=10, sft_damp=0.1, seed=5,
+                                   tau_search=True))
+    res = drv.run(400)
+    assert res.tau[0] < 0.05 and all(t > 0 for t in res.tau)
+    assert drv.tau_search is None, "the search ends once the shift varies"
+    t_final = res.tau[-1]
+    assert drv.calc.tau == t_final
