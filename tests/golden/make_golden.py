@@ -10,6 +10,12 @@ the fixtures are committed so that the tests do not need it).
   its blocking error that NECI's run recorded ("Total projected energy"),
   plus the core energy after freezing ("ECORE now") and the reference
   energy ("<D0|H|D0>=") that the same run printed.
+* pops_*.npz -- POPSFILEs that NECI wrote in its test suite (text
+  test_suite/neci/tau_search/start_val/from_popsfile/POPSFILE; binary
+  POPSFILEHEAD/POPSFILEBIN of test_suite/neci/serial/Ne_adi_Pops_min_si and
+  test_suite/dneci/rdm/BeH_open_shell_dyn_core): the header text, the
+  records as CurrentDets rows and the SHA-256 of NECI's record bytes, which
+  the writer must reproduce exactly.
 """
 from __future__ import annotations
 
@@ -48,7 +54,27 @@ def save(name, src_dir, pattern, key, extra=None):
     print(name, h.shape, vals, more)
 
 
+def save_pops(name, src_dir, binary):
+    import hashlib
+    from neci_stable_gb300 import popsfile
+    if binary:
+        head = (src_dir / "POPSFILEHEAD").read_text()
+        rec_bytes = (src_dir / "POPSFILEBIN").read_bytes()
+        h, rows = popsfile.read_popsfile(src_dir / "POPSFILE")
+    else:
+        text = (src_dir / "POPSFILE").read_text()
+        end = text.index("\n", text.index("&END")) + 1
+        head, rec_bytes = text[:end], text[end:].encode()
+        h, rows = popsfile.read_popsfile(src_dir / "POPSFILE")
+    np.savez_compressed(HERE / name, header=np.array(head), rows=rows, binary=binary,
+                        sha256=np.array(hashlib.sha256(rec_bytes).hexdigest()))
+    print(name, rows.shape, h.totwalk, h.lenof_sign)
+
+
 if __name__ == "__main__":
+    save_pops("pops_text_li2.npz", REF / "tau_search" / "start_val" / "from_popsfile", binary=False)
+    save_pops("pops_bin_ne.npz", REF / "serial" / "Ne_adi_Pops_min_si", binary=True)
+    save_pops("pops_bin_beh_dneci.npz", REF.parent / "dneci" / "rdm" / "BeH_open_shell_dyn_core", binary=True)
     save("hehe_fcidump.npz", REF / "serial" / "HeHe_Davidson_Direct_CI", r"GROUND E =\s*(-?\d+\.\d+)", "ground_e")
     save("ne_pchb_fcidump.npz", REF / "parallel" / "Ne_FciMCPar_pchb",
          r"Total projected energy\s+(-?\d+\.\d+)\s+\+/-\s+(\d+\.\d+E?-?\d*)", "proje_err",

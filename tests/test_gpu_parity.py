@@ -285,3 +285,38 @@ def test_tau_search_run_settles_tau():
     assert drv.tau_search is None, "the search ends once the shift varies"
     t_final = res.tau[-1]
     assert drv.calc.tau == t_final
+
+
+def test_popsfile_restart_on_the_engine(tmp_path):
+    """Download -> binary POPSFILE -> read -> upload into a fresh context:
+    the restarted run continues bit for bit like the uninterrupted one."""
+    from neci_stable_gb300 import popsfile
+    spec = molecule(24, 10)
+    W, L = spec.W, spec.lenof_sign
+
+    def fresh():
+        e = Engine(spec, 200_000, 400_000)
+        e.start_from_reference(initial_part=300.0)
+        return e
+
+    par = lambda it: capi.default_params(tau=0.005, seed=11, iter=it)  # noqa: E731
+    a = fresh()
+    for it in range(1, 11):
+        a.perform_fcimc_cyc_par(par(it))
+    rows, dh, odh = a.download()
+    hdr = popsfile.PopsHeader(nel=spec.nel, lenof_sign=L, nifd=spec.nifd, cyc=10, tau=0.005,
+                              p_singles=spec.p_singles, p_parallel=spec.p_parallel,
+                              p_doubles=1.0 - spec.p_singles, random_hash=list(map(int, spec.random_hash2)))
+    popsfile.write_popsfile(tmp_path / "POPSFILE", hdr, rows, binary=True)
+    h, back = popsfile.read_popsfile(tmp_path / "POPSFILE")
+    assert back.shape[0] == rows.shape[0] == h.totwalk
+    b = Engine(spec, 200_000, 400_000)
+    b.upload(back)  # diagonal and reference elements recomputed on the device
+    assert np.array_equal(canonical_with(b.download()[0], [b.download()[1]], W)[1][0],
+                          canonical_with(rows, [dh], W)[1][0])
+    for it in range(11, 21):
+        sa = a.perform_fcimc_cyc_par(par(it))
+        sb = b.perform_fcimc_cyc_par(par(it))
+        assert sa.tot_parts[0] == sb.tot_parts[0], it
+    ra, rb = canonical(a.download()[0], W), canonical(b.download()[0], W)
+    assert np.array_equal(ra[:, :W + L], rb[:, :W + L])
