@@ -78,4 +78,35 @@ NECI_HD bool split_count(double c, uint32_t &whole, bool &extra, uint64_t &thres
     return true;
 }
 
+// The spawn amplitude's fixed point: q = llrint(x * 2^32) (round half to
+// even) with the overflow rule !(|x * 2^32| < 9.2e18) -> false.  The product
+// by 2^32 is exact for normal x, so q follows from the bits of x alone: with
+// x = m 2^(E-1075), x 2^32 = m 2^(E-1043), shifted with round-half-even.
+// Subnormal x give 0 (|x 2^32| < 2^-990).  NaN and infinities overflow.
+NECI_HD bool fixed32_from_double(double x, int64_t &q) {
+    const uint64_t b = dbl_bits(x);
+    const uint64_t a = b & 0x7FFFFFFFFFFFFFFFull;
+    // 9.2e18 * 2^-32 is exact, so |x| 2^32 < 9.2e18 <=> |x| < 9.2e18 * 2^-32
+    if (!(a < dbl_bits(9.2e18 * 2.3283064365386962890625e-10))) return false;
+    const int E = (int)(a >> 52);
+    if (E == 0) {
+        q = 0;
+        return true;
+    }
+    const uint64_t m = (a & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = E - 1043;
+    uint64_t v;
+    if (sh >= 0) {
+        v = m << sh;  // |x 2^32| < 2^63 bounds sh by 10
+    } else if (sh <= -54) {
+        v = 0;  // below 1/2
+    } else {
+        const int k = -sh;
+        const uint64_t ip = m >> k, rem = m & ((1ull << k) - 1), half = 1ull << (k - 1);
+        v = ip + ((rem > half || (rem == half && (ip & 1ull))) ? 1ull : 0ull);
+    }
+    q = (b >> 63) ? -(int64_t)v : (int64_t)v;
+    return true;
+}
+
 }  // namespace neci

@@ -327,7 +327,8 @@ int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *u, int64_t len) {
     CK(cudaMemcpyAsync(d32, u32.data(), (size_t)len * sizeof(float), cudaMemcpyHostToDevice, e.stream));
     e.sys.umat = d;
     e.sys.umat32 = d32;
-    // Coulomb and exchange rows of the singles (nBI^3 each, FP64 and FP32)
+    // Coulomb and Coulomb-minus-exchange rows of the singles (nBI^3 each,
+    // FP64 and FP32)
     const size_t n3 = (size_t)e.sys.nBI * e.sys.nBI * e.sys.nBI;
     double *jr = nullptr, *kr = nullptr;
     float *jr32 = nullptr, *kr32 = nullptr;
@@ -339,9 +340,9 @@ int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *u, int64_t len) {
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e.stream));
     e.sys.jrow = jr;
-    e.sys.krow = kr;
+    e.sys.jkrow = kr;
     e.sys.jrow32 = jr32;
-    e.sys.krow32 = kr32;
+    e.sys.jkrow32 = kr32;
     drop_graphs(e);
     return NECI_GPU_OK;
 }
@@ -429,6 +430,26 @@ static void derive_generator_constants(Engine &e) {
     s.tau_fac[TC_PAR] = s.p_doubles * s.p_parallel;
     s.tau_fac[TC_OPP] = s.p_doubles * (1.0 - s.p_parallel);
     for (int k = 0; k < 4; ++k) s.f_tau_fac[k] = (float)s.tau_fac[k];
+    // 1/p_gen of a uniform single by its count of (electron, hole) pairs,
+    // count <= nel * nBI: exactly the products the generator formed inline
+    const int ncount = s.nel * s.nBI + 1;
+    std::vector<double> inv(ncount);
+    std::vector<float> inv32(ncount);
+    for (int c = 0; c < ncount; ++c) {
+        inv[c] = (double)c * s.inv_psingles;
+        inv32[c] = (float)c * s.f_inv_psingles;
+    }
+    if (!e.inv_single) {
+        dalloc(e, &e.inv_single, (size_t)ncount);
+        dalloc(e, &e.inv_single32, (size_t)ncount);
+    }
+    if (e.inv_single && e.inv_single32) {
+        cudaMemcpyAsync(e.inv_single, inv.data(), ncount * sizeof(double), cudaMemcpyHostToDevice, e.stream);
+        cudaMemcpyAsync(e.inv_single32, inv32.data(), ncount * sizeof(float), cudaMemcpyHostToDevice, e.stream);
+        cudaStreamSynchronize(e.stream);
+    }
+    s.inv_single = e.inv_single;
+    s.inv_single32 = e.inv_single32;
 }
 
 int32_t neci_gpu_set_reference(neci_gpu_ctx *ctx, const int64_t *ref, double hii) {

@@ -89,11 +89,16 @@ struct DevSys {
     float f_pgen_par, f_pgen_opp, f_p_doubles, f_p_singles, f_p_elec;
     float f_inv_nalpha;  // 1/nOccAlpha (0 without alpha electrons): pair index -> (alpha, beta) positions
     const float *umat32, *tmat32, *alias_prob32, *pexch32;
-    // Coulomb and exchange rows of the single-excitation elements:
-    // [((i-1) n + (a-1)) n + (k-1)] = <ik|ak> (jrow) and <ik|ka> (krow) for
-    // spatial orbitals i, a, k of n = nBI
-    const double *jrow, *krow;
-    const float *jrow32, *krow32;
+    // Coulomb and Coulomb-minus-exchange rows of the single-excitation
+    // elements: [((i-1) n + (a-1)) n + (k-1)] = <ik|ak> (jrow) and
+    // <ik|ak> - <ik|ka> (jkrow) for spatial orbitals i, a, k of n = nBI;
+    // FP32 copies are the FP64 values rounded once
+    const double *jrow, *jkrow;
+    const float *jrow32, *jkrow32;
+    // 1/p_gen of a uniform single with `count` allowed (electron, hole)
+    // pairs: [count] = count * (1 / pSingles), FP64 and FP32
+    const double *inv_single;
+    const float *inv_single32;
     // reciprocals: the spawn amplitude multiplies by 1/p_gen built from them
     double inv_par, inv_opp, inv_pdoub, inv_psingles;
     float f_inv_par, f_inv_opp, f_inv_pdoub, f_inv_psingles;
@@ -386,32 +391,27 @@ __device__ inline double umat_el(const DevSys &s, int i, int j, int k, int l) {
 __device__ inline int spat(int orb) { return (orb + 1) >> 1; }
 __device__ inline bool beta(int orb) { return orb & 1; }
 
-// sltcnd_1_kernel (sltcnd.fpp:643-679): Coulomb terms over the occupied
-// list, then exchange terms, then the one-electron element.  The terms are
-// read from the Coulomb and exchange rows of (id1, id2): jrow[k] =
-// <id1 k|id2 k>, krow[k] = <id1 k|k id2> (the same UMAT values, summed in
-// the same order).
+// sltcnd_1_kernel (sltcnd.fpp:643-679): over the occupied k != src in
+// ascending order, one add per k of the Coulomb term <ik|ak> or, for k of
+// the source's spin, of the precombined <ik|ak> - <ik|ka>; then h_ia.  The
+// reference adds all Coulomb terms before subtracting the exchange terms;
+// the reassociation moves the element by rounding only.  The terms come from
+// the rows of (id1, id2): jrow[k] = <id1 k|id2 k>, jkrow[k] = jrow[k] -
+// <id1 k|k id2>.
 __device__ inline double sltcnd_1(const DevSys &s, const unsigned long long *d, int src, int tgt) {
     double hel = 0.0;
     const int id1 = spat(src), id2 = spat(tgt);
     if (beta(src) == beta(tgt)) {
         const size_t row = ((size_t)(id1 - 1) * s.nBI + (id2 - 1)) * s.nBI - 1;
-        const double *jr = s.jrow + row, *kr = s.krow + row;
+        const double *jr = s.jrow + row, *jkr = s.jkrow + row;
+        const unsigned long long same = beta(src) ? 0x5555555555555555ull : 0xAAAAAAAAAAAAAAAAull;
         for (int w = 0; w < s.W; ++w) {
             unsigned long long x = d[w];
             while (x) {
-                const int o = w * 64 + __ffsll((long long)x);
+                const int b = __ffsll((long long)x) - 1;
+                const int o = w * 64 + b + 1;
                 x &= x - 1;
-                if (o != src) hel += __ldg(&jr[spat(o)]);
-            }
-        }
-        const unsigned long long same = beta(src) ? 0x5555555555555555ull : 0xAAAAAAAAAAAAAAAAull;
-        for (int w = 0; w < s.W; ++w) {
-            unsigned long long x = d[w] & same;
-            while (x) {
-                const int o = w * 64 + __ffsll((long long)x);
-                x &= x - 1;
-                if (o != src) hel -= __ldg(&kr[spat(o)]);
+                if (o != src) hel += __ldg(((same >> b) & 1ull) ? &jkr[spat(o)] : &jr[spat(o)]);
             }
         }
     }

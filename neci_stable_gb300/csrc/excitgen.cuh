@@ -43,8 +43,8 @@ __device__ inline float umat_r<float>(const DevSys &s, int i, int j, int k, int 
     return __ldg(&s.umat32[umat_ind(i, j, k, l) - 1]);
 }
 
-// sltcnd_1_kernel (sltcnd.fpp:643-679) in precision Real, from the Coulomb
-// and exchange rows of (spat(src), spat(tgt)) in the same summation order.
+// sltcnd_1_kernel (sltcnd.fpp:643-679) in precision Real, summed as the
+// FP64 form (one add per occupied k of jrow[k] or, same spin, jkrow[k]).
 template <typename Real>
 __device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, int src, int tgt) {
     Real hel = 0;
@@ -52,22 +52,15 @@ __device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, 
     if (beta(src) == beta(tgt)) {
         const size_t row = ((size_t)(id1 - 1) * s.nBI + (id2 - 1)) * s.nBI - 1;
         const Real *jr = (sizeof(Real) == 8 ? (const Real *)s.jrow : (const Real *)s.jrow32) + row;
-        const Real *kr = (sizeof(Real) == 8 ? (const Real *)s.krow : (const Real *)s.krow32) + row;
+        const Real *jkr = (sizeof(Real) == 8 ? (const Real *)s.jkrow : (const Real *)s.jkrow32) + row;
+        const unsigned long long same = beta(src) ? kBetaBits : kAlphaBits;
         for (int w = 0; w < s.W; ++w) {
             unsigned long long x = d[w];
             while (x) {
-                const int o = w * 64 + __ffsll((long long)x);
+                const int b = __ffsll((long long)x) - 1;
+                const int o = w * 64 + b + 1;
                 x &= x - 1;
-                if (o != src) hel += __ldg(&jr[spat(o)]);
-            }
-        }
-        const unsigned long long same = beta(src) ? kBetaBits : kAlphaBits;
-        for (int w = 0; w < s.W; ++w) {
-            unsigned long long x = d[w] & same;
-            while (x) {
-                const int o = w * 64 + __ffsll((long long)x);
-                x &= x - 1;
-                if (o != src) hel -= __ldg(&kr[spat(o)]);
+                if (o != src) hel += __ldg(((same >> b) & 1ull) ? &jkr[spat(o)] : &jr[spat(o)]);
             }
         }
     }
@@ -173,10 +166,10 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
     const int count = nexcit * (s.nel - elecs_wno);
     if (sizeof(Real) == 8) {
         e.pgen = (Real)(s.p_singles / (double)count);
-        e.invp = (Real)((double)count * s.inv_psingles);
+        e.invp = (Real)__ldg(&s.inv_single[count]);  // (double)count * (1 / pSingles)
     } else {
         e.pgen = (Real)(s.f_p_singles / (float)count);
-        e.invp = (Real)((float)count * s.f_inv_psingles);
+        e.invp = (Real)__ldg(&s.inv_single32[count]);  // (float)count * (float)(1 / pSingles)
     }
     finish_single<Real>(s, d, src, orb, e);
     e.ok = true;
@@ -275,7 +268,9 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     const Real pholes = dbl ? (Real)__ldg(&s.alias_prob[base + ab - 1]) : (Real)__ldg(&s.alias_prob32[base + ab - 1]);
     const int tp = __ldg(&s.tgt_pair[ab]);
     const int o0 = 2 * (tp >> 16) - spin0, o1 = 2 * (tp & 0xFFFF) - spin1;
-    if (o0 == 0 || o1 == 0 || orb_occ(d, o0) || orb_occ(d, o1) || !(pholes > (Real)1e-10)) { e.pgen = 0; return; }
+    // pholes > 1e-10 (pholes >= 0: compared on the bits in FP64)
+    const bool small = dbl ? !(dbl_bits((double)pholes) > dbl_bits(1e-10)) : !(pholes > (Real)1e-10);
+    if (o0 == 0 || o1 == 0 || orb_occ(d, o0) || orb_occ(d, o1) || small) { e.pgen = 0; return; }
     finish_double<Real>(s, d, src0, src1, o0, o1, e);
     pgen *= pholes;
     e.pgen = pgen * (dbl ? (Real)s.p_doubles : (Real)s.f_p_doubles);

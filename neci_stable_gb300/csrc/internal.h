@@ -40,6 +40,8 @@ struct Engine {
     int max_stats = 0;
     std::vector<void *> allocs;
     bool have_ref = false, have_pchb = false;
+    double *inv_single = nullptr;  // device table of DevSys::inv_single
+    float *inv_single32 = nullptr;
     // CUDA graph of one step per precision (FP64, mixed); `graph` is the one
     // ensure_graph selected for the current parameters
     cudaGraphExec_t graphs[2] = {nullptr, nullptr};
@@ -80,6 +82,6 @@ void launch_core_mark(Engine &e, const long long *core_dets, long long n_core);
 void launch_core_count(Engine &e, const long long *core_dets, long long n_core, long long *counts);
 void launch_core_fill(Engine &e, const long long *core_dets, long long n_core);
 void launch_pchb_build(Engine &e);
-void launch_build_jk(Engine &e, double *jrow, double *krow, float *jrow32, float *krow32);
+void launch_build_jk(Engine &e, double *jrow, double *jkrow, float *jrow32, float *jkrow32);
 
 }  // namespace neci

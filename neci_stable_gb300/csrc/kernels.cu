@@ -446,16 +446,23 @@ __device__ inline Real prm(double d, float f) { return sizeof(Real) == 8 ? (Real
 // RealSpawnCutoff rounding (|n| < cutoff -> +-cutoff with probability
 // |n|/cutoff) or stochastic_round (lib/util_mod.fpp:182) to an integer
 // walker.  Returns 0 for no child.
+// In FP64 the product is formed as ((tau H_ij) (1/p_gen)) (1/AvMCExcits)
+// and its sign applied afterwards: multiplying by -1, by the walker sign and
+// by 1/AvMCExcits = 1 are exact, so the value is the reference order's, with
+// two multiplies where it has five; the scaling by 2^32 and the rounding to
+// an integer are done on the bits (fixed32_from_double).
 template <typename Real>
 __device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real invp, bool neg, Stream &rng, int &ovf) {
-    const Real ww = neg ? (Real)-1 : (Real)1;
-    const Real nsp = -prm<Real>(p.tau, p.f_tau) * hel * ww * invp * prm<Real>(p.inv_av, p.f_inv_av);
     long long q;
     if (sizeof(Real) == 8) {
-        const double sc = (double)nsp * 4294967296.0;
-        if (!(fabs(sc) < 9.2e18)) { ovf = 1; return 0; }
-        q = __double2ll_rn(sc);
+        double v = (p.tau * (double)hel) * (double)invp;
+        if (!p.av_unit) v = v * p.inv_av;
+        int64_t qq;
+        if (!fixed32_from_double(v, qq)) { ovf = 1; return 0; }
+        q = neg ? qq : -qq;  // -tau H sign(C): positive for a negative parent
     } else {
+        const Real ww = neg ? (Real)-1 : (Real)1;
+        const Real nsp = -prm<Real>(p.tau, p.f_tau) * hel * ww * invp * prm<Real>(p.inv_av, p.f_inv_av);
         const float sc = (float)nsp * 4294967296.0f;
         if (!(fabsf(sc) < 9.2e18f)) { ovf = 1; return 0; }
         q = __float2ll_rn(sc);

@@ -241,20 +241,21 @@ __global__ void k_core_fill(DevSys s, DevState st, const long long *core_dets, l
 // init_AliasTable_t (aliasSampling.F90:209-297), probabilities w / sum(w).
 // Uses alias_prob as the weight buffer and `scratch` (2*abMax ints per
 // table) for the over/under-full stacks.
-// Coulomb and exchange rows of the single-excitation elements (the UMAT
-// values sltcnd_1_kernel reads, laid out by (i, a) so that the sum over the
-// occupied orbitals k reads one contiguous row).
-__global__ void k_build_jk(DevSys s, double *jrow, double *krow, float *jrow32, float *krow32) {
+// Coulomb and Coulomb-minus-exchange rows of the single-excitation elements
+// (the UMAT values sltcnd_1_kernel reads, laid out by (i, a) so that the sum
+// over the occupied orbitals k reads one contiguous row).
+__global__ void k_build_jk(DevSys s, double *jrow, double *jkrow, float *jrow32, float *jkrow32) {
     const int n = s.nBI;
     const long long total = (long long)n * n * n;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(t % n) + 1, a = (int)((t / n) % n) + 1, i = (int)(t / ((long long)n * n)) + 1;
         const double j = s.umat[umat_ind(i, k, a, k) - 1], x = s.umat[umat_ind(i, k, k, a) - 1];
+        const double jk = j - x;
         jrow[t] = j;
-        krow[t] = x;
+        jkrow[t] = jk;
         jrow32[t] = (float)j;
-        krow32[t] = (float)x;
+        jkrow32[t] = (float)jk;
     }
 }
 
@@ -383,10 +384,10 @@ void launch_core_count(Engine &e, const long long *core_dets, long long n_core, 
 void launch_core_fill(Engine &e, const long long *core_dets, long long n_core) {
     k_core_fill<<<gsz(e), 128, 0, e.stream>>>(e.sys, e.st, core_dets, n_core);
 }
-void launch_build_jk(Engine &e, double *jrow, double *krow, float *jrow32, float *krow32) {
+void launch_build_jk(Engine &e, double *jrow, double *jkrow, float *jrow32, float *jkrow32) {
     const long long n = e.sys.nBI;
     const int grid = (int)std::min<long long>((n * n * n + 255) / 256, 4096);
-    k_build_jk<<<grid, 256, 0, e.stream>>>(e.sys, jrow, krow, jrow32, krow32);
+    k_build_jk<<<grid, 256, 0, e.stream>>>(e.sys, jrow, jkrow, jrow32, jkrow32);
 }
 
 void launch_pchb_build(Engine &e) {

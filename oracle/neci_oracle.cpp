@@ -400,15 +400,23 @@ struct Oracle {
                     hel_tmp -= get_umat_el(gtID(nI[i]), gtID(nI[j]), gtID(nI[j]), gtID(nI[i]));
         return hel_doub + hel_tmp + hel_sing;
     }
-    // sltcnd_1_kernel (sltcnd.fpp:643-679).
+    // sltcnd_1_kernel (sltcnd.fpp:643-679): the Coulomb terms <ik|ak> over
+    // the occupied k != src, less the exchange terms <ik|ka> over the
+    // same-spin ones, plus h_ia.  The reference sums all Coulomb terms, then
+    // all exchange terms; here each same-spin k contributes the precombined
+    // <ik|ak> - <ik|ka> in one add, in ascending k (a reassociation: the
+    // element moves by rounding only, far inside the 1e-12 relative
+    // tolerance of matrix elements).
+    double coul_exch(int id1, int id2, int o, bool same) const {
+        const double j = get_umat_el(id1, gtID(o), id2, gtID(o));
+        return same ? j - get_umat_el(id1, gtID(o), gtID(o), id2) : j;
+    }
     double sltcnd_1(const std::vector<int> &nI, int src, int tgt) const {
         double hel = 0.0;
         const int id1 = gtID(src), id2 = gtID(tgt);
         if (is_beta(src) == is_beta(tgt)) {
             for (int o : nI)
-                if (o != src) hel += get_umat_el(id1, gtID(o), id2, gtID(o));
-            for (int o : nI)
-                if (o != src && is_beta(src) == is_beta(o)) hel -= get_umat_el(id1, gtID(o), gtID(o), id2);
+                if (o != src) hel += coul_exch(id1, id2, o, is_beta(src) == is_beta(o));
         }
         hel += get_tmat(src, tgt);
         return hel;
@@ -534,9 +542,7 @@ struct Oracle {
         const int id1 = gtID(src), id2 = gtID(tgt);
         if (is_beta(src) == is_beta(tgt)) {
             for (int o : nI)
-                if (o != src) hel += umat_r<Real>(id1, gtID(o), id2, gtID(o));
-            for (int o : nI)
-                if (o != src && is_beta(src) == is_beta(o)) hel -= umat_r<Real>(id1, gtID(o), gtID(o), id2);
+                if (o != src) hel += (Real)coul_exch(id1, id2, o, is_beta(src) == is_beta(o));
         }
         hel += tmat_r<Real>(src, tgt);
         return hel;

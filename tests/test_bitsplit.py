@@ -43,18 +43,32 @@ static int check(double c) {
     if ((c > 0.0) != is_positive(c)) return 1;
     const double bs[] = {1.0, -1.0, -2.3283064365386963e-10, 5e-300, -5e-300, 0.0, -0.0, -4.9e-324, 1e300, -7.5};
     for (double b : bs) if ((c * b < 0.0) != prod_negative(c, b)) return 1;
+    // the spawn amplitude's fixed point: llrint(c 2^32) and its overflow rule
+    for (double x : {c, c * 2.3283064365386963e-10, c * 1e-9, c * 3.0e9}) {
+        const double sc = x * 4294967296.0;
+        const bool ovf = !(std::fabs(sc) < 9.2e18);
+        int64_t q = 12345;
+        const bool ok = fixed32_from_double(x, q);
+        if (ok == ovf) return 1;
+        if (ok && q != (int64_t)std::llrint(sc)) return 1;
+    }
     return 0;
 }
 int main() {
     std::vector<double> v = {0.0, -0.0, 1e-12, -1e-12, std::nextafter(1e-12, 1.0), std::nextafter(1e-12, 0.0),
                              4.9e-324, 2.2e-308, 1.0, -1.0, 2.0, 3.0, 0.5, 0.95, 2147483647.0, 2147483647.5,
                              2147483648.0, -2147483648.0, 1e9, 1e15, 1e300};
+    // (NaN and infinities are appended below for the fixed point only)
     for (int k = 1; k < 40; ++k) {
         const double b = (double)k;
         v.push_back(b + 1e-12); v.push_back(b + 2e-12); v.push_back(b - 1e-13);
         v.push_back(std::nextafter(b, 0.0)); v.push_back(std::nextafter(b, 1e9));
         v.push_back(-(b + 1e-12)); v.push_back(b + 0.5);
     }
+    // ties of the fixed point's rounding: x 2^32 = k + 1/2
+    for (int k = -40; k < 40; ++k) v.push_back(((double)k + 0.5) * 2.3283064365386963e-10);
+    v.push_back(std::nan("")); v.push_back(INFINITY); v.push_back(-INFINITY);
+    v.push_back(2142047537.0); v.push_back(-2142047538.5); v.push_back(4294967296.0);
     std::mt19937_64 g(7);
     std::uniform_real_distribution<double> u(-36.0, 10.0);
     for (int i = 0; i < 2000000; ++i) {
@@ -64,6 +78,11 @@ int main() {
     }
     int bad = 0;
     for (double c : v) {
+        if (!std::isfinite(c)) {
+            int64_t q;
+            if (fixed32_from_double(c, q)) ++bad;
+            continue;
+        }
         const int b = check(c);
         if (b && bad < 5) std::printf("mismatch at %.17g\n", c);
         bad += b;

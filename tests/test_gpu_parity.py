@@ -317,6 +317,9 @@ def test_popsfile_restart_on_the_engine(tmp_path):
     for it in range(11, 21):
         sa = a.perform_fcimc_cyc_par(par(it))
         sb = b.perform_fcimc_cyc_par(par(it))
-        assert sa.tot_parts[0] == sb.tot_parts[0], it
+        # TotParts is a reduction over slots, and the restart compacts the
+        # slots: equal up to the order of the FP64 sum
+        assert abs(sa.tot_parts[0] - sb.tot_parts[0]) <= 1e-12 * sa.tot_parts[0], it
+        assert sa.n_occupied == sb.n_occupied and sa.n_spawned == sb.n_spawned, it
     ra, rb = canonical(a.download()[0], W), canonical(b.download()[0], W)
     assert np.array_equal(ra[:, :W + L], rb[:, :W + L])
