@@ -45,7 +45,12 @@ BLOOM = 3.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of
 # this workload at 1e7 walkers) per unit of work, for roofline.traffic:
 # kernel -> (bytes per unit, step count that is the unit).
-NCU_DRAM_BYTES_PER_UNIT = {}
+NCU_DRAM_BYTES_PER_UNIT = {
+    "spawn": (16.4, "n_attempts"),
+    "sweep": (67.0, "tot_walkers"),
+    "merge_stats": (53.8, "tot_walkers"),
+    "ann_probe": (108.7, "n_spawned"),
+}
 
 
 def workload_spec():
@@ -522,7 +527,7 @@ def main():
     ann = ("ann_probe", "ann_compress", "ann_insert")
     ann_ms = sum(kt[k][0] / kt[k][1] for k in ann if k in kt)
     ann_bytes = sum(algorithmic_bytes(k, r["last"], W, L) for k in ann)
-    launches_per_step = 11 + (1 if r["last"]["n_core"] > 0 else 0)
+    launches_per_step = 16 + (1 if r["last"]["n_core"] > 0 else 0)
     line = {
         "metric": METRIC, "value": updates / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,

@@ -75,8 +75,9 @@ void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
     d.av_unit = p.av_mc_excits == 1.0;
 }
 
-const char *kKernelNames[K_NUM] = {"rehash",    "begin",        "sweep",      "expand",      "spawn", "core",
-                                   "ann_probe", "ann_compress", "ann_insert", "merge_stats", "final"};
+const char *kKernelNames[K_NUM] = {"compact",   "rehash",       "begin",      "sweep",       "expand", "spawn",
+                                   "core",      "ann_probe",    "ann_compress", "ann_insert", "merge_stats",
+                                   "final"};
 
 // Launch one kernel stage, bracketed by events when profiling.
 template <typename F>
@@ -98,6 +99,7 @@ int stage(Engine &e, int id, F &&f) {
 
 // The launch sequence of one PerformFCIMCycPar step.
 void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
+    stage(e, K_COMPACT, [&] { launch_compact(e, e.stream); });
     stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
     stage(e, K_BEGIN, [&] { launch_begin(e, e.stream); });
     stage(e, K_SWEEP, [&] { launch_sweep(e, e.stream); });
@@ -242,6 +244,9 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.rep_bucket, (size_t)st.max_spawned);
     A(st.rep_q, (size_t)st.max_spawned * s.L);
     A(st.rep_cnt, (size_t)st.max_spawned * (s.L + 1));
+    A(st.tile_count, (size_t)st.max_walkers / kCompactTile + 2);
+    A(st.tile_off, (size_t)st.max_walkers / kCompactTile + 2);
+    A(st.hole_at_rank, (size_t)st.max_walkers + 1);
     A(st.ctl, 1);
     A(e.d_params, 1);
     e.max_stats = 4096;

@@ -21,6 +21,7 @@ constexpr int kMaxNeigh = 8;
 constexpr int kBigAttempts = 32;  // parents with more attempts are expanded by k_expand
 constexpr int kHugeAttempts = 1 << 16;  // ... and with more than this by the whole grid
 constexpr int kMaxHuge = 4096;
+constexpr int kCompactTile = 1024;        // slots per block of the compaction scans
 constexpr int kProbeLimit = 1 << 16;
 constexpr uint32_t kEmpty = 0u;
 constexpr uint32_t kTomb = 0xFFFFFFFFu;
@@ -49,6 +50,9 @@ struct Control {
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
     int rehash;                         // rebuild the walker hash at the next step
+    int compact;                        // compact the walker list at the next step
+    unsigned long long compact_k;       // occupied slots kept by the compaction
+    unsigned long long compact_pos_k;   // occupied slots below compact_k
     double nborn[2], ndied[2], nannihil[2], naborted[2], nremoved[2];
     double tot_parts[2], tot_parts_old[2], noat_hf[2], hf_cyc[2], enum_cyc[2], norm[2];
     // tau search (log_spawn_magnitude / log_death_magnitude): kept across
@@ -144,6 +148,10 @@ struct DevState {
     long long n_core;
     int32_t *core_of_slot;         // core index or -1
     long long *core_slot;
+    // compaction of the walker list: occupied slots per tile of kCompactTile,
+    // their exclusive prefix, and the holes below the kept count by rank
+    uint32_t *tile_count, *tile_off;
+    int32_t *hole_at_rank;
     double *core_x, *core_y;
     long long *core_rowptr;
     int32_t *core_col;

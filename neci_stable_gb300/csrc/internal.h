@@ -12,7 +12,8 @@
 namespace neci {
 
 enum KernelId {
-    K_REHASH = 0,
+    K_COMPACT = 0,
+    K_REHASH,
     K_BEGIN,
     K_SWEEP,
     K_EXPAND,
@@ -57,6 +58,7 @@ struct Engine {
 // launchers (kernels.cu)
 void launch_begin(Engine &e, cudaStream_t s);
 void launch_rehash(Engine &e, cudaStream_t s);
+void launch_compact(Engine &e, cudaStream_t s);
 void launch_sweep(Engine &e, cudaStream_t s);
 void launch_expand(Engine &e, cudaStream_t s);
 void launch_spawn(Engine &e, cudaStream_t s);

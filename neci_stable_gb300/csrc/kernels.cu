@@ -223,6 +223,137 @@ __global__ void k_hash_fill(DevSys s, DevState st) {
 }
 
 // ===========================================================================
+// Compaction of the walker list (run at the start of a step when the
+// previous one left more holes than occupied slots).  The K occupied slots
+// (or core slots) keep their order; those at or above K move into the holes
+// below K, the r-th of them into the r-th hole, so that slots 0..K-1 hold the
+// whole list.  TotWalkers becomes K and the walker hash is rebuilt.  Results
+// do not depend on slots: every random stream is keyed by the determinant.
+// ===========================================================================
+__device__ inline bool slot_kept(const DevSys &s, const DevState &st, long long j) {
+    const long long *r = st.dets + j * s.R;
+    if (st.n_core > 0 && is_core_flags(r[s.W + s.L])) return true;
+    for (int k = 0; k < s.L; ++k)
+        if (abs_bits(word_to_double(r[s.W + k])) >= dbl_bits(kEps12)) return true;
+    return false;
+}
+
+// Exclusive position of slot j among the kept slots of its tile, and the
+// tile's count (blockDim.x == kCompactTile).
+__device__ inline unsigned int tile_rank(bool keep, unsigned int &count) {
+    __shared__ unsigned int warp_n[kCompactTile / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned int bal = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_n[wid] = __popc(bal);
+    __syncthreads();
+    unsigned int before = 0, total = 0;
+    for (int w = 0; w < kCompactTile / 32; ++w) {
+        const unsigned int c = warp_n[w];
+        if (w < wid) before += c;
+        total += c;
+    }
+    __syncthreads();
+    count = total;
+    return before + __popc(bal & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(kCompactTile) k_compact_count(DevSys s, DevState st) {
+    if (!st.ctl->compact) return;
+    const long long n = (long long)st.ctl->tot_walkers;
+    const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long j = t * kCompactTile + threadIdx.x;
+        unsigned int count;
+        (void)tile_rank(j < n && slot_kept(s, st, j), count);
+        if (threadIdx.x == 0) st.tile_count[t] = count;
+    }
+}
+
+// One block: exclusive scan of the tile counts; K = the kept total.
+__global__ void __launch_bounds__(kCompactTile) k_compact_scan(DevState st) {
+    if (!st.ctl->compact) return;
+    const long long n = (long long)st.ctl->tot_walkers;
+    const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
+    __shared__ unsigned int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (long long base = 0; base < ntiles; base += kCompactTile) {
+        const long long t = base + threadIdx.x;
+        const unsigned int c = t < ntiles ? st.tile_count[t] : 0u;
+        // block-wide exclusive scan of c
+        __shared__ unsigned int buf[kCompactTile];
+        buf[threadIdx.x] = c;
+        __syncthreads();
+        for (int o = 1; o < kCompactTile; o <<= 1) {
+            const unsigned int v = threadIdx.x >= (unsigned)o ? buf[threadIdx.x - o] : 0u;
+            __syncthreads();
+            buf[threadIdx.x] += v;
+            __syncthreads();
+        }
+        const unsigned int incl = buf[threadIdx.x];
+        if (t < ntiles) st.tile_off[t] = carry + incl - c;
+        __syncthreads();
+        if (threadIdx.x == kCompactTile - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) st.ctl->compact_k = carry;
+}
+
+// Holes below K by rank; the number of kept slots below K.
+__global__ void __launch_bounds__(kCompactTile) k_compact_holes(DevSys s, DevState st) {
+    if (!st.ctl->compact) return;
+    const long long n = (long long)st.ctl->tot_walkers;
+    const long long K = (long long)st.ctl->compact_k;
+    const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const long long j = t * kCompactTile + threadIdx.x;
+        const bool keep = j < n && slot_kept(s, st, j);
+        unsigned int count;
+        const long long pos = (long long)st.tile_off[t] + tile_rank(keep, count);
+        if (j < K && !keep) st.hole_at_rank[j - pos] = (int32_t)j;
+        // the kept position of every slot that will move (the free list is
+        // scratch until the sweep refills it)
+        if (j >= K && keep) st.free_list[j] = (int32_t)pos;
+        if (j == K) st.ctl->compact_pos_k = (unsigned long long)pos;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && K >= n) st.ctl->compact_pos_k = (unsigned long long)K;
+}
+
+// Every kept slot at or above K moves into the hole of its rank.  Only rows
+// at or above K are read, and only holes below K are written.
+__global__ void k_compact_move(DevSys s, DevState st) {
+    if (!st.ctl->compact) return;
+    const long long n = (long long)st.ctl->tot_walkers;
+    const long long K = (long long)st.ctl->compact_k;
+    const long long pos_k = (long long)st.ctl->compact_pos_k;
+    for (long long j = K + blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
+         j += (long long)gridDim.x * blockDim.x) {
+        if (!slot_kept(s, st, j)) continue;
+        const long long to = st.hole_at_rank[st.free_list[j] - pos_k];
+        const long long *src = st.dets + j * s.R;
+        long long *dst = st.dets + to * s.R;
+        for (int w = 0; w < s.R; ++w) dst[w] = src[w];
+        st.diagH[to] = st.diagH[j];
+        st.offdiagH[to] = st.offdiagH[j];
+        if (st.n_core > 0) {
+            const int ci = st.core_of_slot[j];
+            st.core_of_slot[to] = ci;
+            st.core_of_slot[j] = -1;
+            if (ci >= 0) st.core_slot[ci] = to;
+        }
+    }
+}
+
+// Closes the compaction: TotWalkers = K, the hash is rebuilt next.
+__global__ void k_compact_done(DevState st) {
+    Control *c = st.ctl;
+    if (!c->compact) return;
+    c->tot_walkers = c->compact_k;
+    c->rehash = 1;
+    c->compact = 0;
+}
+
+// ===========================================================================
 // k_sweep
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const IterParams *pp) {
@@ -1066,6 +1197,8 @@ __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, i
     // rebuild the walker hash before the next step when live entries plus
     // tombstones pass 70% of the buckets
     c->rehash = (c->n_occupied + c->n_tomb) * 10ull > st.hash_n * 7ull ? 1 : 0;
+    // compact the list before the next step when holes outnumber occupied slots
+    c->compact = (c->tot_walkers > (unsigned long long)(4 * kCompactTile) && c->n_holes * 2ull > c->tot_walkers) ? 1 : 0;
 }
 
 // ===========================================================================
@@ -1084,6 +1217,15 @@ static int grid_for(const Engine &e, int threads) {
 }
 
 void launch_begin(Engine &e, cudaStream_t s) { k_begin<<<1, 32, 0, s>>>(e.st); }
+
+void launch_compact(Engine &e, cudaStream_t s) {
+    const int grid = clamp_grid(e.st.max_walkers / kCompactTile + 1, e.num_sms * 2);
+    k_compact_count<<<grid, kCompactTile, 0, s>>>(e.sys, e.st);
+    k_compact_scan<<<1, kCompactTile, 0, s>>>(e.st);
+    k_compact_holes<<<grid, kCompactTile, 0, s>>>(e.sys, e.st);
+    k_compact_move<<<grid_slots(e), 256, 0, s>>>(e.sys, e.st);
+    k_compact_done<<<1, 32, 0, s>>>(e.st);
+}
 
 void launch_rehash(Engine &e, cudaStream_t s) {
     k_hash_clear<<<grid_for(e, 256), 256, 0, s>>>(e.st);

@@ -323,3 +323,34 @@ def test_popsfile_restart_on_the_engine(tmp_path):
         assert sa.n_occupied == sb.n_occupied and sa.n_spawned == sb.n_spawned, it
     ra, rb = canonical(a.download()[0], W), canonical(b.download()[0], W)
     assert np.array_equal(ra[:, :W + L], rb[:, :W + L])
+
+
+@pytest.mark.parametrize("name", ["mol24", "hub10x2"])
+def test_compaction_keeps_the_run_identical(name):
+    """A list that is mostly holes is compacted at the start of the next step
+    (occupied rows move into the holes below the kept count, TotWalkers
+    shrinks, the walker hash is rebuilt); the walker lists stay identical to
+    the oracle's, which never compacts."""
+    spec, eng, orc = pair(name, 400_000, 800_000)
+    rng = np.random.default_rng(21)
+    W, L = spec.W, spec.lenof_sign
+    rows = random_walkers(spec, 12000, rng)
+    holes = rng.random(rows.shape[0]) < 0.7
+    rows[holes, W:W + L] = 0
+    eng.upload(rows)
+    orc.upload(rows)
+    p = lambda it: capi.default_params(tau=0.005, seed=4, iter=it)  # noqa: E731
+    tw = []
+    for it in range(1, 7):
+        sg = eng.perform_fcimc_cyc_par(p(it))
+        sc, rc = orc.iterate(p(it))
+        assert rc == 0 and sg.err == 0
+        tw.append(sg.tot_walkers)
+        rg, rcpu = canonical(eng.download()[0], W), canonical(orc.download()[0], W)
+        assert np.array_equal(rg[:, :W + L], rcpu[:, :W + L]), it
+        assert np.array_equal(rg[:, -1] & ~1, rcpu[:, -1] & ~1), it
+        np.testing.assert_allclose(sg.tot_parts[:L], sc.tot_parts[:L], rtol=1e-12)
+    # the second step ran on the compacted list (about 30% of the slots, then
+    # its new determinants appended)
+    assert tw[1] < 0.6 * tw[0], tw
+    assert sc.tot_walkers >= rows.shape[0]   # the oracle keeps its holes
