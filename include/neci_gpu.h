@@ -230,6 +230,25 @@ typedef struct {
 int32_t neci_gpu_set_tau_search(neci_gpu_ctx *ctx, int32_t on);
 int32_t neci_gpu_get_tau_stats(neci_gpu_ctx *ctx, neci_gpu_tau_stats *out, int32_t reset);
 
+/* ---- stochastic 2-RDM of a replica pair (lenof_sign == 2) ---------------
+ * While sampling is on, every step adds to a dense spin-orbital 2-RDM
+ *   rdm2[pair(p,q) * npair + pair(r,s)] ~ <Psi_1| a+_p a+_q a_s a_r |Psi_2>,
+ * p < q, r < s, pair(p,q) = (q-1)(q-2)/2 + (p-1) for 1-based spin orbitals,
+ * npair = nBasis (nBasis - 1) / 2:
+ *   off-diagonal: each spawn from D_i (run s) onto D_j that is occupied after
+ *   annihilation adds 1/2 w_i C_j(other run) <D_j|...|D_i>, w_i having
+ *   expectation C_i (DiDj_Found_FillRDM, rdm_filling.F90:423-611, and
+ *   Add_RDM_From_IJ_Pair, :696-767; the parent travels with the spawn as in
+ *   store_parent_with_spawned, rdm_general.fpp:1087);
+ *   diagonal: each occupied D_i adds C_i^1 C_i^2 to Gamma(pq, pq) for its
+ *   occupied pairs (fill_spawn_rdm_diag, rdm_filling.F90:769-789).
+ * The sums are unnormalised and not yet symmetrised (the host takes
+ * (G + G^T) / 2 and divides by the trace, as the reference's output does). */
+int32_t neci_gpu_set_rdm_sampling(neci_gpu_ctx *ctx, int32_t on);
+/* Copies the accumulated 2-RDM (n_elements == npair^2 doubles) and, if reset
+ * != 0, clears it. */
+int32_t neci_gpu_get_rdm(neci_gpu_ctx *ctx, double *rdm2, int64_t n_elements, int32_t reset);
+
 /* ---- annihilation of an injected spawn list -----------------------------
  * CompressSpawnedList (Annihilation.F90:249-515) followed by
  * AnnihilateSpawnedParts + CalcHashTableStats (Annihilation.F90:965-1352,

@@ -128,6 +128,8 @@ _SIGS = {
     "neci_gpu_set_excit_biases": (_i32, [_P, _dbl, _dbl]),
     "neci_gpu_set_tau_search": (_i32, [_P, _i32]),
     "neci_gpu_get_tau_stats": (_i32, [_P, C.POINTER(TauStats), _i32]),
+    "neci_gpu_set_rdm_sampling": (_i32, [_P, _i32]),
+    "neci_gpu_get_rdm": (_i32, [_P, _P, _i64, _i32]),
     "neci_gpu_upload_walkers": (_i32, [_P, _P, _i64, _P, _P]),
     "neci_gpu_download_walkers": (_i32, [_P, _P, _P, _P, _i64, _P]),
     "neci_gpu_iterate": (_i32, [_P, C.POINTER(IterParams), C.POINTER(IterStats)]),

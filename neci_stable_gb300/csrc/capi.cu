@@ -75,9 +75,9 @@ void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
     d.av_unit = p.av_mc_excits == 1.0;
 }
 
-const char *kKernelNames[K_NUM] = {"compact",   "rehash",       "begin",      "sweep",       "expand", "spawn",
+const char *kKernelNames[K_NUM] = {"compact",   "rehash",       "begin",        "sweep",      "expand", "spawn",
                                    "core",      "ann_probe",    "ann_compress", "ann_insert", "merge_stats",
-                                   "final"};
+                                   "rdm",       "final"};
 
 // Launch one kernel stage, bracketed by events when profiling.
 template <typename F>
@@ -110,6 +110,7 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
     stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream); });
     stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, e.st.n_core > 0 ? 1 : 0); });
+    if (e.sys.rdm) stage(e, K_RDM, [&] { launch_rdm(e, e.stream); });
     stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, advance); });
 }
 
@@ -527,6 +528,34 @@ int32_t neci_gpu_get_tau_stats(neci_gpu_ctx *ctx, neci_gpu_tau_stats *out, int32
         CK(cudaMemsetAsync(&e.st.ctl->tau_gamma[0], 0, sizeof(h), e.stream));
         CK(cudaStreamSynchronize(e.stream));
     }
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_rdm_sampling(neci_gpu_ctx *ctx, int32_t on) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (on && e.sys.L != 2) return fail(NECI_GPU_ERR_INVALID, "2-RDM sampling needs a replica pair (lenof_sign 2)");
+    if (on && !e.st.rdm2) {
+        const long long npair = (long long)e.sys.nbasis * (e.sys.nbasis - 1) / 2;
+        if (int r = dalloc(e, &e.st.spawn_par, (size_t)e.st.max_spawned * (e.sys.W + 1))) return r;
+        if (int r = dalloc(e, &e.st.rdm2, (size_t)npair * npair)) return r;
+        CK(cudaStreamSynchronize(e.stream));
+        e.sys.npair = npair;
+    }
+    e.sys.rdm = on ? 1 : 0;
+    drop_graphs(e);
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_get_rdm(neci_gpu_ctx *ctx, double *rdm2, int64_t n_elements, int32_t reset) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!e.st.rdm2) return fail(NECI_GPU_ERR_INVALID, "2-RDM sampling was never enabled");
+    if (!rdm2 || n_elements != e.sys.npair * e.sys.npair)
+        return fail(NECI_GPU_ERR_INVALID, "rdm2 must hold npair^2 doubles, npair = nBasis (nBasis - 1) / 2");
+    CK(cudaMemcpyAsync(rdm2, e.st.rdm2, (size_t)n_elements * sizeof(double), cudaMemcpyDeviceToHost, e.stream));
+    if (reset) CK(cudaMemsetAsync(e.st.rdm2, 0, (size_t)n_elements * sizeof(double), e.stream));
+    CK(cudaStreamSynchronize(e.stream));
     return NECI_GPU_OK;
 }
 

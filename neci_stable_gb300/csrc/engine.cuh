@@ -118,6 +118,10 @@ struct DevSys {
     int tau_search;
     double tau_fac[4];
     float f_tau_fac[4];
+    // stochastic 2-RDM of a replica pair: on/off and the number of spin-orbital
+    // pairs p < q (the 2-RDM is npair x npair)
+    int rdm;
+    long long npair;
 };
 
 // Resident walker state (device pointers).
@@ -152,6 +156,11 @@ struct DevState {
     // their exclusive prefix, and the holes below the kept count by rank
     uint32_t *tile_count, *tile_off;
     int32_t *hole_at_rank;
+    // 2-RDM sampling: the parent of every spawn record (W det words, then the
+    // unbiasing weight as double bits), and the dense 2-RDM
+    // rdm2[pair(p,q) * npair + pair(r,s)] = <a+_p a+_q a_s a_r>, p<q, r<s
+    long long *spawn_par;
+    double *rdm2;
     double *core_x, *core_y;
     long long *core_rowptr;
     int32_t *core_col;

@@ -24,6 +24,7 @@ struct Excit {
     int ic;
     int cls;  // TauClass
     bool ok;
+    unsigned long long aq;  // |amplitude| in fixed point before rounding (2-RDM unbiasing)
 };
 
 template <typename Real>

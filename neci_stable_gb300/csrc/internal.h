@@ -23,6 +23,7 @@ enum KernelId {
     K_ANN_COMPRESS,
     K_ANN_INSERT,
     K_MERGE_STATS,
+    K_RDM,
     K_FINAL,
     K_NUM
 };
@@ -68,6 +69,7 @@ void launch_ann_compress(Engine &e, cudaStream_t s);
 void launch_ann_insert(Engine &e, cudaStream_t s);
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core);
 void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter);
+void launch_rdm(Engine &e, cudaStream_t s);
 
 // utility launchers (util_kernels.cu)
 void launch_util_hash(Engine &e, const long long *dets, long long n, unsigned long long len, long long *out);

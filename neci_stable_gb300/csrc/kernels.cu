@@ -583,7 +583,8 @@ __device__ inline Real prm(double d, float f) { return sizeof(Real) == 8 ? (Real
 // two multiplies where it has five; the scaling by 2^32 and the rounding to
 // an integer are done on the bits (fixed32_from_double).
 template <typename Real>
-__device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real invp, bool neg, Stream &rng, int &ovf) {
+__device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real invp, bool neg, Stream &rng, int &ovf,
+                                            unsigned long long &aq_out) {
     long long q;
     if (sizeof(Real) == 8) {
         double v = (p.tau * (double)hel) * (double)invp;
@@ -599,6 +600,7 @@ __device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real 
         q = __float2ll_rn(sc);
     }
     const unsigned long long aq = (unsigned long long)(q < 0 ? -q : q);
+    aq_out = aq;
     if (p.t_all_real_coeff) {
         if (p.t_real_spawn_cutoff && aq < p.cutoff_q) {
             // keep with probability |q| / cutoff_q
@@ -665,7 +667,7 @@ __device__ inline void tau_log(const DevSys &s, const Excit<Real> &e, TauAcc *ac
 // amplitude.
 template <typename Real>
 __device__ inline long long attempt_create(const DevSys &s, const DevState &st, const IterParams &p, const Parent &P,
-                                           const Excit<Real> &e, Stream &rng, const int32_t *sh_rh2, int &ovf,
+                                           Excit<Real> &e, Stream &rng, const int32_t *sh_rh2, int &ovf,
                                            TauAcc *tacc) {
     if (!e.ok) return 0;
     if (P.core) {
@@ -673,13 +675,32 @@ __device__ inline long long attempt_create(const DevSys &s, const DevState &st, 
         if (hs >= 0 && is_core_flags(st.dets[hs * s.R + s.W + s.L])) return 0;
     }
     if (s.tau_search) tau_log<Real>(s, e, tacc);
-    return spawn_amplitude<Real>(p, e.hel, e.invp, P.neg, rng, ovf);
+    return spawn_amplitude<Real>(p, e.hel, e.invp, P.neg, rng, ovf, e.aq);
+}
+
+// The unbiasing weight of a spawn's parent for the 2-RDM (the role of
+// calc_rdmbiasfac, rdm_general.fpp:1039-1085, for a per-spawn estimator):
+// the expected number of non-zero spawns onto a child per attempt is
+// p_gen P(nz), where P(nz) is min(1, |n| / RealSpawnCutoff) with real
+// coefficients and the cutoff, min(1, |n|) with integer walkers, and 1
+// otherwise; the attempts number |C_i| AvMCExcits on average, so
+// sign(C_i) / (AvMCExcits p_gen P(nz)) has expectation C_i per child.
+// aq is |n| in fixed point before rounding.
+__device__ inline double rdm_parent_weight(const IterParams &p, double invp, unsigned long long aq, bool neg) {
+    double inv_pnz = 1.0;
+    if (p.t_all_real_coeff) {
+        if (p.t_real_spawn_cutoff && aq < p.cutoff_q) inv_pnz = (double)p.cutoff_q / (double)aq;
+    } else if (aq < (1ull << 32)) {
+        inv_pnz = 4294967296.0 / (double)aq;
+    }
+    const double w = (invp * p.inv_av) * inv_pnz;
+    return neg ? -w : w;
 }
 
 // create_particle (fcimc_helper.F90:152-308): append the record; warp-wide.
 template <typename Real>
-__device__ inline void create_particle(const DevSys &s, const DevState &st, long long qv, const Parent &P,
-                                       const Excit<Real> &e) {
+__device__ inline void create_particle(const DevSys &s, const DevState &st, const IterParams &p, long long qv,
+                                       const Parent &P, const Excit<Real> &e) {
     const unsigned long long pos = warp_append(&st.ctl->n_spawned, qv != 0 ? 1u : 0u);
     if (qv == 0) return;
     if (pos >= (unsigned long long)st.max_spawned) {
@@ -690,6 +711,14 @@ __device__ inline void create_particle(const DevSys &s, const DevState &st, long
     for (int w = 0; w < s.W; ++w) o[w] = (long long)e.child[w];
     for (int k2 = 0; k2 < s.L; ++k2) o[s.W + k2] = (k2 == P.run) ? qv : 0ll;
     o[s.W + s.L] = P.pinit ? (1ll << init_flag_bit(P.run)) : 0ll;
+    if (s.rdm) {
+        // the parent and its unbiased sign for the 2-RDM: sign(C_i) divided
+        // by the expected number of non-zero spawns onto this child per unit
+        // of |C_i|, AvMCExcits p_gen P(spawn != 0)
+        long long *par = st.spawn_par + pos * (s.W + 1);
+        for (int w = 0; w < s.W; ++w) par[w] = (long long)P.d[w];
+        par[s.W] = double_to_word(rdm_parent_weight(p, (double)e.invp, e.aq, P.neg));
+    }
 }
 
 // A single excitation parked in the block's queue: the attempt's stream is
@@ -711,7 +740,7 @@ __device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, 
         gen_uniform_single<Real>(s, P.d, rng, e);
         qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf, tacc);
     }
-    create_particle<Real>(s, st, qv, P, e);
+    create_particle<Real>(s, st, p, qv, P, e);
 }
 
 // The spawn attempts (FciMCPar.F90:1600-1745, loop_over_walkers): one
@@ -766,7 +795,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
             }
             qv = attempt_create<Real>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
         }
-        create_particle<Real>(s, st, qv, P, e);
+        create_particle<Real>(s, st, p, qv, P, e);
         if (GEN != NECI_EXGEN_RS_HUBBARD) {
             __syncthreads();
             const int n = sq_n;
@@ -1161,6 +1190,117 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
 }
 
 // ===========================================================================
+// Stochastic 2-RDM of a replica pair (run 1 = bra, run 2 = ket), sampled
+// every step while enabled.  Off-diagonal: each spawn of run s from D_i
+// onto D_j that is occupied after annihilation adds
+//   1/2 w_i C_j^(other run) <D_j| a+_p a+_q a_s a_r |D_i>
+// (DiDj_Found_FillRDM, rdm_filling.F90:423-611, with the instantaneous
+// C_j of the next iteration as there); w_i has expectation C_i per child
+// (rdm_parent_weight).  Diagonal: every occupied D_i adds C_i^1 C_i^2 to
+// Gamma(pq, pq) for its occupied pairs p < q (fill_spawn_rdm_diag,
+// rdm_filling.F90:769-789, with instantaneous rather than averaged signs).
+// The host symmetrises Gamma and normalises it by its trace.
+// ===========================================================================
+__device__ inline long long rdm_pair(int p, int q) { return (long long)(q - 1) * (q - 2) / 2 + (p - 1); }
+
+// Add_RDM_From_IJ_Pair (rdm_filling.F90:696-767) with nI = parent (ket) and
+// nJ = child (bra): a single i -> a adds to Gamma(ka, ki) for every other
+// occupied k of nI (fill_spawn_rdm_singles, :791-817), a double ij -> ab to
+// Gamma(ab, ij); both carry the excitation's fermionic sign.
+__device__ inline void rdm_add_pair(const DevSys &s, const DevState &st, const unsigned long long *par,
+                                    const unsigned long long *chi, double c) {
+    int src[2] = {0, 0}, tgt[2] = {0, 0}, ns = 0, nt = 0;
+    for (int w = 0; w < s.W; ++w) {
+        unsigned long long x = par[w] & ~chi[w], y = chi[w] & ~par[w];
+        while (x) { if (ns < 2) src[ns] = w * 64 + __ffsll((long long)x); ++ns; x &= x - 1; }
+        while (y) { if (nt < 2) tgt[nt] = w * 64 + __ffsll((long long)y); ++nt; y &= y - 1; }
+    }
+    if (ns != nt || ns < 1 || ns > 2) return;
+    if (ns == 1) {
+        const int i = src[0], a = tgt[0];
+        const bool par_odd = occ_between(par, s.W, min(i, a), max(i, a)) & 1;
+        const double full = par_odd ? -c : c;
+        for (int w = 0; w < s.W; ++w) {
+            unsigned long long x = par[w];
+            while (x) {
+                const int k = w * 64 + __ffsll((long long)x);
+                x &= x - 1;
+                if (k == i) continue;
+                const double sg = ((k < a) == (k < i)) ? full : -full;
+                const long long bra = k < a ? rdm_pair(k, a) : rdm_pair(a, k);
+                const long long ket = k < i ? rdm_pair(k, i) : rdm_pair(i, k);
+                atomicAdd(&st.rdm2[bra * s.npair + ket], sg);
+            }
+        }
+        return;
+    }
+    // the parity of i -> a then j -> b (sorted pairing), as successive singles
+    unsigned long long t[kMaxWords];
+    for (int w = 0; w < s.W; ++w) t[w] = par[w];
+    int np = occ_between(t, s.W, min(src[0], tgt[0]), max(src[0], tgt[0]));
+    flip_orb(t, src[0]);
+    flip_orb(t, tgt[0]);
+    np += occ_between(t, s.W, min(src[1], tgt[1]), max(src[1], tgt[1]));
+    atomicAdd(&st.rdm2[rdm_pair(tgt[0], tgt[1]) * s.npair + rdm_pair(src[0], src[1])], (np & 1) ? -c : c);
+}
+
+__global__ void __launch_bounds__(256) k_rdm_offdiag(DevSys s, DevState st) {
+    extern __shared__ int32_t sh_rh2[];
+    load_rh2(s, sh_rh2);
+    Control *c = st.ctl;
+    const long long n = (long long)min(c->n_spawned, (unsigned long long)st.max_spawned);
+    const int W = s.W, L = s.L, R = s.R;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const long long *rec = st.spawn + i * R;
+        const long long *par = st.spawn_par + i * (W + 1);
+        const double w = word_to_double(par[W]);
+        const int run = rec[W] != 0 ? 0 : 1;
+        unsigned long long d[kMaxWords], pd[kMaxWords];
+        for (int k = 0; k < W; ++k) {
+            d[k] = (unsigned long long)rec[k];
+            pd[k] = (unsigned long long)par[k];
+        }
+        const long long slot = hash_find(st, d, W, R, neci_hash(d, W, sh_rh2), c);
+        if (slot < 0) continue;
+        const double cj = word_to_double(st.dets[slot * R + W + (1 - run)]);
+        if (cj == 0.0) continue;
+        rdm_add_pair(s, st, pd, d, 0.5 * w * cj);
+        (void)L;
+    }
+}
+
+// Diagonal terms; per-block sums in shared memory when npair doubles fit.
+__global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use_shared) {
+    extern __shared__ double sh_diag[];
+    const long long npair = s.npair;
+    if (use_shared) {
+        for (long long k = threadIdx.x; k < npair; k += blockDim.x) sh_diag[k] = 0.0;
+        __syncthreads();
+    }
+    const long long n = (long long)min(st.ctl->tot_walkers, (unsigned long long)st.max_walkers);
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        const long long *r = st.dets + j * s.R;
+        const double prod = word_to_double(r[s.W]) * word_to_double(r[s.W + 1]);
+        if (prod == 0.0) continue;
+        uint8_t nI[kMaxNel];
+        unsigned long long d[kMaxWords];
+        for (int w = 0; w < s.W; ++w) d[w] = (unsigned long long)r[w];
+        const int nel = decode(d, s.W, nI);
+        for (int a = 1; a < nel; ++a)
+            for (int b = 0; b < a; ++b) {
+                const long long pq = rdm_pair(nI[b], nI[a]);
+                if (use_shared) atomicAdd(&sh_diag[pq], prod);
+                else atomicAdd(&st.rdm2[pq * npair + pq], prod);
+            }
+    }
+    if (use_shared) {
+        __syncthreads();
+        for (long long k = threadIdx.x; k < npair; k += blockDim.x)
+            if (sh_diag[k] != 0.0) atomicAdd(&st.rdm2[k * npair + k], sh_diag[k]);
+    }
+}
+
+// ===========================================================================
 // k_final: write the step's stats record.
 // ===========================================================================
 __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, int advance_iter, long long n_core) {
@@ -1266,6 +1406,14 @@ void launch_ann_insert(Engine &e, cudaStream_t s) {
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
     k_merge_stats<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params, with_core);
 }
+void launch_rdm(Engine &e, cudaStream_t s) {
+    if (!e.sys.rdm) return;
+    k_rdm_offdiag<<<grid_spawns(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
+    const size_t shm = (size_t)e.sys.npair * sizeof(double);
+    const int use_shared = shm <= 48 * 1024 ? 1 : 0;  // the default dynamic shared-memory limit
+    k_rdm_diag<<<grid_slots(e), 256, use_shared ? shm : 0, s>>>(e.sys, e.st, use_shared);
+}
+
 void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter) {
     k_final<<<1, 32, 0, s>>>(e.st, out, e.d_params, advance_iter, e.st.n_core);
 }

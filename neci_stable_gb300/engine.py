@@ -163,6 +163,18 @@ class Engine:
     def set_excit_biases(self, p_singles: float, p_parallel: float):
         check(self.lib.neci_gpu_set_excit_biases(self.ctx, p_singles, p_parallel))
 
+    # ---------------------------------------------------------------- 2-RDM
+    def set_rdm_sampling(self, on: bool):
+        check(self.lib.neci_gpu_set_rdm_sampling(self.ctx, 1 if on else 0))
+
+    def rdm2(self, reset: bool = False) -> np.ndarray:
+        """The accumulated spin-orbital 2-RDM, npair x npair (unnormalised)."""
+        nb = self.spec.nbasis
+        npair = nb * (nb - 1) // 2
+        out = np.zeros((npair, npair))
+        check(self.lib.neci_gpu_get_rdm(self.ctx, ptr(out), out.size, 1 if reset else 0))
+        return out
+
     # ---------------------------------------------------------------- timing
     def set_profiling(self, on: bool):
         check(self.lib.neci_gpu_set_profiling(self.ctx, 1 if on else 0))

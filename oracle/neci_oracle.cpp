@@ -178,6 +178,12 @@ struct Oracle {
 
     // conventional tau search (tau/tau_search_conventional.F90:138-258,
     // tau/tau_main.F90:197-206): class maxima of gamma and max_death_cpt
+    // stochastic 2-RDM of a replica pair: Gamma[pair(p,q) * npair + pair(r,s)]
+    bool rdm = false;
+    i64 npair = 0;
+    std::vector<double> rdm2;
+    static i64 rdm_pair(int p, int q) { return (i64)(q - 1) * (q - 2) / 2 + (p - 1); }
+
     bool tau_search = false;
     double tau_gamma[4] = {0.0, 0.0, 0.0, 0.0};  // sing, doub, par, opp
     i64 tau_cnt[4] = {0, 0, 0, 0};
@@ -1049,6 +1055,74 @@ struct IterRun {
     std::vector<Oracle::Spawn> spawns;
     std::vector<double> partial;  // core vector (L per core det)
     int err = 0;
+    // spawns whose parents feed the 2-RDM
+    struct RdmEvent {
+        std::vector<i64> child, parent;
+        int run;
+        double w;
+    };
+    std::vector<RdmEvent> rdm_events;
+
+    // The unbiasing weight of a spawn's parent: sign(C_i) / (AvMCExcits p_gen
+    // P(spawn != 0)), the role of calc_rdmbiasfac (rdm_general.fpp:1039) for a
+    // per-spawn estimator; aq is |n| in fixed point before rounding.
+    double rdm_parent_weight(double invp, u64 aq, bool neg) const {
+        double inv_pnz = 1.0;
+        if (p.t_all_real_coeff) {
+            const u64 cutoff_q = (u64)std::llrint(std::ldexp(p.real_spawn_cutoff, NECI_SPAWN_FIXED_BITS));
+            if (p.t_real_spawn_cutoff && aq < cutoff_q) inv_pnz = (double)cutoff_q / (double)aq;
+        } else if (aq < (1ull << 32)) {
+            inv_pnz = 4294967296.0 / (double)aq;
+        }
+        const double w = (invp * (1.0 / p.av_mc_excits)) * inv_pnz;
+        return neg ? -w : w;
+    }
+    // Add_RDM_From_IJ_Pair (rdm_filling.F90:696-767): nI the ket (parent),
+    // nJ the bra (child); singles via fill_spawn_rdm_singles (:791-817).
+    void rdm_add_pair(const std::vector<int> &nI, const std::vector<int> &nJ, double c) {
+        int ex[2][2] = {{0, 0}, {0, 0}};
+        bool tParity = false;
+        const int ic = o.get_excitation(nI, nJ, ex, tParity);
+        const double full = tParity ? -c : c;
+        const i64 np = o.npair;
+        if (ic == 1) {
+            const int i = ex[0][0], a = ex[1][0];
+            for (int k : nI) {
+                if (k < i && k < a) o.rdm2[Oracle::rdm_pair(k, a) * np + Oracle::rdm_pair(k, i)] += full;
+                else if (k < i && k > a) o.rdm2[Oracle::rdm_pair(a, k) * np + Oracle::rdm_pair(k, i)] += -full;
+                else if (k > i && k < a) o.rdm2[Oracle::rdm_pair(k, a) * np + Oracle::rdm_pair(i, k)] += -full;
+                else if (k > i && k > a) o.rdm2[Oracle::rdm_pair(a, k) * np + Oracle::rdm_pair(i, k)] += full;
+            }
+        } else if (ic == 2) {
+            o.rdm2[Oracle::rdm_pair(ex[1][0], ex[1][1]) * np + Oracle::rdm_pair(ex[0][0], ex[0][1])] += full;
+        }
+    }
+    // The step's 2-RDM contributions: spawns onto determinants occupied
+    // after annihilation (DiDj_Found_FillRDM, rdm_filling.F90:423-611), and
+    // the diagonal C_i^1 C_i^2 (fill_spawn_rdm_diag, :769-789).
+    void rdm_fill() {
+        std::vector<int> nI, nJ;
+        for (const RdmEvent &ev : rdm_events) {
+            o.decode_bit_det(ev.child.data(), nJ);
+            i64 slot, h;
+            if (!o.hash_lookup(nJ, ev.child.data(), slot, h)) continue;
+            const double cj = o.get_sign(o.row(slot), 1 - ev.run);
+            if (cj == 0.0) continue;
+            o.decode_bit_det(ev.parent.data(), nI);
+            rdm_add_pair(nI, nJ, 0.5 * ev.w * cj);
+        }
+        for (i64 j = 0; j < o.TotWalkers; ++j) {
+            const i64 *r = o.row(j);
+            const double prod = o.get_sign(r, 0) * o.get_sign(r, 1);
+            if (prod == 0.0) continue;
+            o.decode_bit_det(r, nI);
+            for (size_t a = 1; a < nI.size(); ++a)
+                for (size_t b = 0; b < a; ++b) {
+                    const i64 pq = Oracle::rdm_pair(nI[b], nI[a]);
+                    o.rdm2[pq * o.npair + pq] += prod;
+                }
+        }
+    }
     IterRun(Oracle &o_, const neci_gpu_iter_params &p_, neci_gpu_iter_stats &s_) : o(o_), p(p_), st(s_) {}
 
     // decide_num_to_spawn (fcimc_helper.F90:2160-2174).
@@ -1071,7 +1145,7 @@ struct IterRun {
     // probability |n|/cutoff) or stochastic_round (lib/util_mod.fpp:182-203)
     // then act on the fixed-point value in integer arithmetic.
     template <typename Real>
-    i64 spawn_amplitude(Real hel, Real invp, bool neg, Stream &rng, int &ovf) const {
+    i64 spawn_amplitude(Real hel, Real invp, bool neg, Stream &rng, int &ovf, u64 &aq_out) const {
         const Real ww = neg ? (Real)-1 : (Real)1;
         const Real nsp = -Oracle::prm<Real>(p.tau) * hel * ww * invp * Oracle::prm<Real>(1.0 / p.av_mc_excits);
         i64 q;
@@ -1085,6 +1159,7 @@ struct IterRun {
             q = (i64)std::llrintf(sc);
         }
         const u64 aq = (u64)(q < 0 ? -q : q);
+        aq_out = aq;
         if (p.t_all_real_coeff) {
             const u64 cutoff_q = (u64)std::llrint(std::ldexp(p.real_spawn_cutoff, NECI_SPAWN_FIXED_BITS));
             if (p.t_real_spawn_cutoff && aq < cutoff_q) {
@@ -1126,8 +1201,17 @@ struct IterRun {
             if (gam > o.tau_gamma[c]) o.tau_gamma[c] = gam;
             if (c >= 2 || gam > 0.0) o.tau_cnt[c] += 1;
         }
-        const i64 q = spawn_amplitude<Real>(g.hel, g.invp, neg, rng, ovf);
+        u64 aq = 0;
+        const i64 q = spawn_amplitude<Real>(g.hel, g.invp, neg, rng, ovf, aq);
         if (q == 0) return;
+        if (o.rdm) {
+            RdmEvent ev;
+            ev.child = child;
+            ev.parent.assign(r, r + o.W);
+            ev.run = run;
+            ev.w = rdm_parent_weight((double)g.invp, aq, neg);
+            rdm_events.push_back(ev);
+        }
         // create_particle (fcimc_helper.F90:152-308)
         if ((i64)spawns.size() >= o.sys.max_spawned) { err = NECI_GPU_ERR_SPAWN_FULL; return; }
         Oracle::Spawn s;
@@ -1333,6 +1417,7 @@ struct IterRun {
         st.tot_walkers = o.TotWalkers;
         st.holes_in_list = o.HolesInList;
         st.n_core = (i64)o.core_slots.size();
+        if (o.rdm) rdm_fill();
     }
 
     // walker_death (fcimc_helper.F90:2279-2407) + attempt_die_normal
@@ -1645,6 +1730,23 @@ int32_t orc_set_excit_biases(void *h, double p_singles, double p_parallel) {
     o->p_doubles = 1.0 - p_singles;
     o->sys.p_singles = o->sys.excitgen == NECI_EXGEN_UNIFORM ? 1.0 - o->p_doubles : p_singles;
     o->sys.p_parallel = p_parallel;
+    return NECI_GPU_OK;
+}
+int32_t orc_set_rdm_sampling(void *h, int32_t on) {
+    Oracle *o = (Oracle *)h;
+    if (on && o->L != 2) return NECI_GPU_ERR_INVALID;
+    if (on && o->rdm2.empty()) {
+        o->npair = (i64)o->sys.nbasis * (o->sys.nbasis - 1) / 2;
+        o->rdm2.assign((size_t)(o->npair * o->npair), 0.0);
+    }
+    o->rdm = on != 0;
+    return NECI_GPU_OK;
+}
+int32_t orc_get_rdm(void *h, double *out, int64_t n, int32_t reset) {
+    Oracle *o = (Oracle *)h;
+    if ((int64_t)o->rdm2.size() != n) return NECI_GPU_ERR_INVALID;
+    std::memcpy(out, o->rdm2.data(), (size_t)n * sizeof(double));
+    if (reset) std::fill(o->rdm2.begin(), o->rdm2.end(), 0.0);
     return NECI_GPU_OK;
 }
 int32_t orc_set_tau_search(void *h, int32_t on) {

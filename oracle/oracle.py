@@ -43,6 +43,8 @@ def _load():
         "orc_init_pchb": [_P],
         "orc_set_excit_biases": [_P, C.c_double, C.c_double],
         "orc_set_tau_search": [_P, C.c_int32],
+        "orc_set_rdm_sampling": [_P, C.c_int32],
+        "orc_get_rdm": [_P, _P, C.c_int64, C.c_int32],
         "orc_get_tau_stats": [_P, C.POINTER(capi.TauStats), C.c_int32],
         "orc_upload_walkers": [_P, _P, C.c_int64, _P, _P],
         "orc_download_walkers": [_P, _P, _P, _P, C.c_int64, _P],
@@ -157,6 +159,16 @@ class Oracle:
 
     def set_excit_biases(self, p_singles: float, p_parallel: float):
         _ok(lib().orc_set_excit_biases(self.h, p_singles, p_parallel))
+
+    def set_rdm_sampling(self, on: bool):
+        _ok(lib().orc_set_rdm_sampling(self.h, 1 if on else 0))
+
+    def rdm2(self, reset: bool = False):
+        nb = self.spec.nbasis
+        npair = nb * (nb - 1) // 2
+        out = np.zeros((npair, npair))
+        _ok(lib().orc_get_rdm(self.h, _ptr(out), out.size, 1 if reset else 0))
+        return out
 
     def iterate(self, params):
         import neci_stable_gb300.capi as capi

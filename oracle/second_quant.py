@@ -89,3 +89,32 @@ def hamiltonian(dets_int, nbasis, tmat, eri=None, uhub=None, ecore=0.0):
             if d2 in index:
                 H[index[d2], j] += v
     return H
+
+
+def rdm2_from_vector(dets, vec, nbasis):
+    """Exact spin-orbital 2-RDM of a CI vector by operators:
+    G[pair(p,q), pair(r,s)] = sum_IJ c_I c_J <D_I| a+_p a+_q a_s a_r |D_J>,
+    p < q, r < s, pair(p,q) = (q-1)(q-2)/2 + (p-1); dets are Python ints."""
+    npair = nbasis * (nbasis - 1) // 2
+    G = np.zeros((npair, npair))
+    index = {d: i for i, d in enumerate(dets)}
+    pair = lambda p, q: (q - 1) * (q - 2) // 2 + (p - 1)  # noqa: E731
+    for j, dj in enumerate(dets):
+        cj = vec[j]
+        if cj == 0.0:
+            continue
+        occ = [p for p in range(1, nbasis + 1) if (dj >> (p - 1)) & 1]
+        for ir, r in enumerate(occ):
+            for s in occ[ir + 1:]:
+                d1, s1 = _annihilate(dj, r)
+                d2, s2 = _annihilate(d1, s)  # a_s a_r |D_J>
+                for q in range(2, nbasis + 1):
+                    d3, s3 = _create(d2, q)
+                    if d3 is None:
+                        continue
+                    for p in range(1, q):
+                        d4, s4 = _create(d3, p)  # a+_p a+_q a_s a_r |D_J>
+                        if d4 is None or d4 not in index:
+                            continue
+                        G[pair(p, q), pair(r, s)] += vec[index[d4]] * cj * s1 * s2 * s3 * s4
+    return G

@@ -152,3 +152,37 @@ def test_hehe_mixed_precision_matches_fp64():
     assert abs(e32["proje"] - e64["proje"]) < max(2.0 * comb, 2e-4), (e32, e64)
     assert abs(e32["proje"] - e0) < max(2.5 * e32["proje_err"], 2e-4), (e32, e0)
     assert abs(e32["proje"] - e64["proje"]) < 1e-3
+
+
+def test_rdm_energy_matches_exact_diagonalisation():
+    """Replica-pair FCIQMC on the device with 2-RDM sampling: the energy of
+    the accumulated, normalised 2-RDM agrees with exact diagonalisation."""
+    from neci_stable_gb300 import rdm
+    from oracle import second_quant
+    from oracle.oracle import Oracle, exact_ground_state
+    spec1 = molecule(6, 4)
+    orc = Oracle(spec1, 50_000, 100_000)
+    na = sum(1 for o in spec1.reference if o % 2 == 0)
+    e_exact, dets, vec = exact_ground_state(orc, na, spec1.nel - na)
+    spec = molecule(6, 4, lenof_sign=2)
+    eng = Engine(spec, 200_000, 400_000)
+    eng.start_from_reference(initial_part=5000.0)
+    shift, old, it = [0.0, 0.0], [5000.0, 5000.0], 0
+    for cyc in range(40):
+        st = eng.iterate_n(capi.default_params(tau=0.02, seed=17, iter=it + 1, diag_sft=shift), 10)
+        it += 10
+        for k in range(2):
+            if cyc >= 5:
+                shift[k] -= 0.1 * np.log(st[-1].tot_parts[k] / old[k]) / (0.02 * 10)
+            old[k] = st[-1].tot_parts[k]
+    eng.set_rdm_sampling(True)
+    eng.rdm2(reset=True)
+    A = rdm.antisym_integrals(spec)
+    energies = []
+    for block in range(10):
+        eng.iterate_n(capi.default_params(tau=0.02, seed=17, iter=it + 1, diag_sft=shift), 200)
+        it += 200
+        energies.append(rdm.rdm_energy(eng.rdm2(reset=True), spec, A)["energy"])
+    e = float(np.mean(energies))
+    err = float(np.std(energies, ddof=1) / np.sqrt(len(energies)))
+    assert abs(e - e_exact) < max(3 * err, 5e-4), (e, err, e_exact)
