@@ -59,6 +59,43 @@ def workload_spec():
     return systems.molecular_system(h, eri, ecore, N_EL, seed=SEED + 1, name="synthetic-fcidump-n24-e10")
 
 
+def _ring10():
+    from neci_stable_gb300 import systems
+    return systems.hubbard_system("chain", (10,), 10, u=4.0)
+
+
+def _square6x6():
+    from neci_stable_gb300 import systems
+    return systems.hubbard_system("square", (6, 6), 36, u=4.0)
+
+
+def _fcidump64():
+    from neci_stable_gb300 import systems
+    h, eri, ecore = systems.synthetic_fcidump(64, SEED + 64)
+    return systems.molecular_system(h, eri, ecore, 20, seed=SEED + 65, name="synthetic-fcidump-n64-e20")
+
+
+# The configurations: the spec, target walkers, semistochastic core size,
+# and the buffer sizes as multiples of the walker number (slots, spawn records).
+WORKLOADS = {
+    "n24": dict(spec=workload_spec, walkers=TARGET_WALKERS, core=0, slots=3.0, spawns=4.0,
+                desc="synthetic FCIDUMP n=24 orbitals (48 spin orbitals), 10 electrons, Sz=0, PCHB, initiator "
+                     "FCIQMC, real coefficients"),
+    "ring10": dict(spec=_ring10, walkers=1e4, core=0, slots=10.0, spawns=100.0, start="single_part", sft_damp=0.1,
+                   tau=0.01,
+                   desc="1D Hubbard ring, 10 sites, 10 electrons, Sz=0, periodic, t=1, U=4, real-space, "
+                        "uniform generator"),
+    "hub6x6": dict(spec=_square6x6, walkers=1e8, core=10_000, slots=2.0, spawns=2.0, start="single_part",
+                   sft_damp=0.3, scale_up=20.0, tau=0.003,
+                   desc="2D Hubbard 6x6 periodic real-space lattice, 36 electrons, Sz=0, U/t=4, semistochastic "
+                        "core of the 1e4 most populated determinants"),
+    "n64": dict(spec=_fcidump64, walkers=5e8, core=50_000, slots=0.8, spawns=1.0, sft_damp=0.3, scale_up=20.0,
+                tau=0.002,
+                desc="synthetic FCIDUMP n=64 orbitals (128 spin orbitals, 3 determinant words), 20 electrons, "
+                     "Sz=0, PCHB, semistochastic core of 5e4 determinants"),
+}
+
+
 def estimate_tau(eng, n_samples=200_000):
     """Conventional tau-search value from the excitation statistics of the
     reference and a few of its excitations: tau = bloom / max(|H_ij| / p_gen)."""
@@ -129,7 +166,7 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def algorithmic_bytes(kernel, st, W, L):
+def algorithmic_bytes(kernel, st, W, L, nnz=0):
     """Bytes a kernel must move per launch (per unit counts of the step)."""
     R = 8 * (W + L + 1)
     G = 16
@@ -141,7 +178,12 @@ def algorithmic_bytes(kernel, st, W, L):
     if kernel == "sweep":
         return slots * (R + G) + D * 8 * L + D * 16
     if kernel == "spawn":
-        return S * R + st["n_attempts"] / 16 * (8 * W + 16)
+        # the 8 B attempt entries read and the spawn records written (parent
+        # rows and tables are gathered from L2)
+        return st["n_attempts"] * 8 + S * R
+    if kernel == "core":
+        # CSR column index and FP64 value per element, x gathered and y written
+        return nnz * (4 + 8) + st["n_core"] * 16 * L
     if kernel == "ann_probe":
         return S * R + S * (4 + 8 * W) + (S - (U - N)) * 0 + U * (8 * L + 4)
     if kernel == "ann_compress":
@@ -160,26 +202,68 @@ def run_gpu(args, rank, world):
     from neci_stable_gb300.fcimc import CalcParams, FciMCPar
 
     import torch
-    spec = workload_spec()
-    max_walkers = int(3.0 * args.walkers)
-    max_spawned = int(4.0 * args.walkers)
+    wl = WORKLOADS[args.workload]
+    spec = wl["spec"]()
+    max_walkers = int(max(wl["slots"] * args.walkers, 1e5))
+    max_spawned = int(max(wl["spawns"] * args.walkers, 2e5))
     eng = Engine(spec, max_walkers, max_spawned, device=0)
     # written between timed steps so that no step starts with a warm L2 (129 MB)
     flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda:0")  # 256 MB
-    tau0 = estimate_tau(eng)
+    # a workload with a fixed tau runs without the tau search
+    tau0 = wl["tau"] if "tau" in wl else estimate_tau(eng)
+    # With scale_up, the walker distribution is equilibrated at 1/scale_up of
+    # the target (its overshoot fits the buffers sized for the target) and the
+    # list is then scaled to the target: every sign times the same factor, so
+    # the shape and the shift carry over (a restart from a rescaled POPSFILE).
+    scale = wl.get("scale_up", 1.0)
+    target = args.walkers / scale
     # the conventional tau search runs on the device over the first half of
     # the equilibration (max_iter stop method), starting from tau0
-    calc = CalcParams(tau=tau0, target_walkers=args.walkers, steps_sft=10, sft_damp=0.05,
-                      seed=SEED + 1000 * rank, precision=capi.PREC_FP64, tau_search=True,
+    calc = CalcParams(tau=tau0, target_walkers=target, steps_sft=10, sft_damp=wl.get("sft_damp", 0.05),
+                      seed=SEED + 1000 * rank, precision=capi.PREC_FP64, tau_search="tau" not in wl,
                       tau_search_max_iter=max(args.equil // 2, 20))
     drv = FciMCPar(eng, calc)
-    # start: the population on the reference, shift varying from the start
-    eng.start_from_reference(initial_part=args.walkers)
-    drv.single_part_phase = [False] * eng.L
-    drv.diag_sft = [0.0] * eng.L
+    if wl.get("start") == "single_part":
+        # startsinglepart: a few walkers on the reference and the shift held
+        # at 0 until the population reaches the target, then varied (the
+        # usual start where the reference lies far above the ground state)
+        eng.start_from_reference(initial_part=max(10.0, target * 1e-6))
+    else:
+        # the population on the reference, the shift varying from the start
+        eng.start_from_reference(initial_part=target)
+        drv.single_part_phase = [False] * eng.L
+        drv.diag_sft = [0.0] * eng.L
     equil = drv.run(args.equil)  # untimed equilibration of the walker distribution
+    scale_info = None
+    if scale > 1.0:
+        st0 = eng.iterate_n(drv.params(), 1)[0]
+        drv.iter += 1
+        rows, dh, odh = eng.download(max_rows=int(st0.tot_walkers) + 1)
+        factor = args.walkers / max(st0.tot_parts[0], 1.0)
+        W, L = spec.W, spec.lenof_sign
+        sg = rows[:, W:W + L].view(np.float64) * factor
+        rows[:, W:W + L] = sg.view(np.int64)
+        eng.upload(rows, dh, odh)
+        scale_info = {"equilibrated_walkers": st0.tot_parts[0], "factor": factor}
+        drv.calc.target_walkers = args.walkers
+        drv.run(100)  # re-equilibration at the target population
     tau = drv.calc.tau
     tau_info = {"start": tau0, "final": tau, "cycles_searched": len(equil.tau)}
+    core_info = None
+    if wl["core"] > 0:
+        # pops-core: the most populated determinants become the core space
+        # (semi_stoch_gen.F90:103), its Hamiltonian built on the device
+        t0 = time.perf_counter()
+        st0 = eng.iterate_n(drv.params(), 1)[0]
+        drv.iter += 1
+        rows = eng.download(max_rows=int(st0.tot_walkers) + 1)[0]
+        W, L = spec.W, spec.lenof_sign
+        pop = np.abs(rows[:, W:W + L].view(np.float64)).sum(axis=1)
+        n_core = min(wl["core"], rows.shape[0])
+        core = rows[np.argsort(-pop, kind="stable")[:n_core], :W]
+        eng.set_core_space(core, capi.PREC_FP64)
+        core_info = {"n_core": n_core, "nnz": eng.core_nnz(), "set_up_s": time.perf_counter() - t0}
+        drv.run(20)
     p = drv.params()
     # warm-up steps (untimed)
     eng.iterate_n(p, args.warmup)
@@ -234,6 +318,14 @@ def run_gpu(args, rank, world):
     updates = sum(s.tot_parts_old[0] for s in stats)
     bb_updates = sum(s.tot_parts_old[0] for s in bb_stats)
     mixed_updates = sum(s.tot_parts_old[0] for s in mstats)
+    # E_proj of the FP64 and of the mixed-precision steps (blocks of 10 steps)
+    from neci_stable_gb300 import analysis
+    proje = {}
+    for name, sts in (("fp64", stats), ("mixed", mstats)):
+        num = np.array([sum(x.enum_cyc[0] for x in sts[k:k + 10]) for k in range(0, len(sts), 10)])
+        den = np.array([sum(x.hf_cyc[0] for x in sts[k:k + 10]) for k in range(0, len(sts), 10)])
+        e, err = analysis.projected_energy(num, den, eng.hii) if len(num) >= 2 else (float(num.sum() / den.sum()) + eng.hii, None)
+        proje[name] = {"e_proj": e, "err": err}
     # ---- per-kernel timing pass (events around each kernel; not the timed number)
     eng.set_profiling(True)
     prof_stats = eng.iterate_n(p, 3)
@@ -242,7 +334,9 @@ def run_gpu(args, rank, world):
     eng.set_profiling(False)
     last = prof_stats[-1].as_dict()
     return {
-        "eng": eng, "spec": spec, "tau": tau, "tau_info": tau_info, "updates": updates, "dev_ms": dev_ms, "clk": clk.summary(),
+        "eng": eng, "spec": spec, "tau": tau, "tau_info": tau_info, "core_info": core_info, "proje": proje,
+        "scale_info": scale_info,
+        "updates": updates, "dev_ms": dev_ms, "clk": clk.summary(),
         "e2e_updates": e2e_updates, "e2e_s": e2e_s, "ktimes": ktimes, "last": last, "stats": stats,
         "first": stats[0].as_dict(),
         "equil": equil, "mixed_updates": mixed_updates, "mixed_ms": mixed_ms, "bb_updates": bb_updates,
@@ -461,7 +555,9 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--equil", type=int, default=600, help="untimed equilibration iterations")
-    ap.add_argument("--walkers", type=float, default=TARGET_WALKERS, help="target walker number")
+    ap.add_argument("--walkers", type=float, default=None, help="target walker number (default: the workload's)")
+    ap.add_argument("--workload", default="n24", choices=sorted(WORKLOADS),
+                    help="n24: the headline configuration; ring10, hub6x6, n64: the other single-GPU configurations")
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances measurement")
@@ -470,6 +566,8 @@ def main():
     ap.add_argument("--batch-equil", type=int, default=200)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.walkers is None:
+        args.walkers = WORKLOADS[args.workload]["walkers"]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
@@ -511,7 +609,8 @@ def main():
     kt = {k: v for k, v in r["ktimes"].items() if v[1] > 0}
     top = max(kt, key=lambda k: kt[k][0])
     top_ms = kt[top][0] / kt[top][1]
-    ab = algorithmic_bytes(top, r["last"], W, L)
+    nnz = (r["core_info"] or {}).get("nnz", 0)
+    ab = algorithmic_bytes(top, r["last"], W, L, nnz)
     hbm, peak_kind = peaks()
     achieved = ab / (top_ms / 1e3) / 1e9
     traffic = None
@@ -521,7 +620,7 @@ def main():
     # achieved GB/s of every kernel (algorithmic bytes of the last profiled step)
     kernel_gbs = {}
     for k, (ms, cnt) in kt.items():
-        b = algorithmic_bytes(k, r["last"], W, L)
+        b = algorithmic_bytes(k, r["last"], W, L, nnz)
         if b > 0:
             kernel_gbs[k] = b / (ms / cnt / 1e3) / 1e9
     ann = ("ann_probe", "ann_compress", "ann_insert")
@@ -532,8 +631,8 @@ def main():
         "metric": METRIC, "value": updates / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "synthetic FCIDUMP n=24 orbitals (48 spin orbitals), 10 electrons, Sz=0, PCHB, "
-                               f"initiator FCIQMC, real coefficients, FP64, {args.walkers:.3g} walkers",
+        "config": {"workload": f"{WORKLOADS[args.workload]['desc']}, FP64, {args.walkers:.3g} walkers",
+                   "name": args.workload, "core": r["core_info"], "scaled_up": r["scale_info"],
                    "tau": r["tau"], "tau_search": r["tau_info"], "walkers": r["stats"][-1].tot_parts[0],
                    "determinants": r["stats"][-1].n_occupied,
                    "step_counts": {k: r["last"][k] for k in ("n_attempts", "n_spawned", "n_unique", "n_new",
@@ -557,15 +656,16 @@ def main():
                                   "ms_per_step": ann_ms, "algorithmic_bytes": ann_bytes},
         "kernel_ms_per_step": {k: v[0] / v[1] for k, v in kt.items()},
         "kernel_gbs": kernel_gbs,
+        "proje": r["proje"],
         "mixed_precision": {"value": r["mixed_updates"] / (r["mixed_ms"] / 1000.0), "unit": UNIT,
                             "ms_per_step": r["mixed_ms"] / args.steps,
                             "speedup_vs_fp64": (r["mixed_updates"] / r["mixed_ms"]) / (updates / (dev_s * 1000.0)),
                             "note": "FP32 H_ij, p_gen and spawn amplitude; FP64 death, E_proj and signs; "
                                     "cycles of 10 steps interleaved with the FP64 steps on the same population"},
     }
-    if not args.no_batched and world == 1:
+    if not args.no_batched and world == 1 and args.workload == "n24":
         line["batched"] = run_batched(args)
-    if not args.no_cpu_baseline and world == 1:
+    if not args.no_cpu_baseline and world == 1 and args.workload == "n24":
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))
     eng.close()

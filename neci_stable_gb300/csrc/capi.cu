@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "stage.cuh"
 
 using namespace neci;
 
@@ -226,9 +227,10 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     int32_t *rh2 = nullptr;
     A(rh2, (size_t)s.nbasis + 1);
     s.random_hash2 = rh2;
-    A(st.dets, (size_t)st.max_walkers * s.R);
-    A(st.diagH, (size_t)st.max_walkers);
-    A(st.offdiagH, (size_t)st.max_walkers);
+    // the arrays the sweeps stage by TMA bulk copies are kStagePad slots longer
+    A(st.dets, (size_t)(st.max_walkers + kStagePad) * s.R);
+    A(st.diagH, (size_t)st.max_walkers + kStagePad);
+    A(st.offdiagH, (size_t)st.max_walkers + kStagePad);
     A(st.hash, (size_t)st.hash_n);
     A(st.slot_bucket, (size_t)st.max_walkers);
     A(st.free_list, (size_t)st.max_walkers + 1);
@@ -237,7 +239,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.big, (size_t)st.max_big * 3);
     A(st.huge, (size_t)kMaxHuge * 3);
     A(st.acc, (size_t)st.max_walkers * s.L);
-    A(st.meta, (size_t)st.max_walkers * s.L);
+    A(st.meta, (size_t)(st.max_walkers + kStagePad) * s.L);
     A(st.cand, (size_t)st.max_spawned);
     A(st.cand_h, (size_t)st.max_spawned);
     A(st.spawn_hash, (size_t)st.spawn_hash_n);
@@ -265,6 +267,8 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
         for (int k = 0; k < 2 * K_NUM; ++k) cudaEventCreate(&e.ev[k]);
         if (cudaStreamSynchronize(e.stream) != cudaSuccess) rc = fail(NECI_GPU_ERR_CUDA, "sync after init");
     }
+    if (rc == NECI_GPU_OK && configure_kernels(e) != 0)
+        rc = fail(NECI_GPU_ERR_CUDA, "cudaFuncSetAttribute (shared memory of the staged sweeps) failed");
     if (rc != NECI_GPU_OK) {
         neci_gpu_free(ctx);
         return rc;

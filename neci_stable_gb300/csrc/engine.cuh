@@ -49,6 +49,8 @@ struct Control {
     unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
+    int halted;                         // status of a failed step: later steps do nothing until
+                                        // the walker list is uploaded again
     int rehash;                         // rebuild the walker hash at the next step
     int compact;                        // compact the walker list at the next step
     unsigned long long compact_k;       // occupied slots kept by the compaction
@@ -168,6 +170,14 @@ struct DevState {
     float *core_val32;
     Control *ctl;
 };
+
+// Slots in use, never above the allocation (a step that overflowed the list
+// leaves TotWalkers above it).
+__device__ inline long long slots_in_use(const DevState &st) {
+    const unsigned long long n = st.ctl->tot_walkers;
+    return (long long)(n < (unsigned long long)st.max_walkers ? n : (unsigned long long)st.max_walkers);
+}
+__device__ inline bool halted(const DevState &st) { return st.ctl->halted != 0; }
 
 struct IterParams {
     double tau, diag_sft[2], initiator_walk_no, occupied_thresh, real_spawn_cutoff, av_mc_excits;

@@ -61,6 +61,8 @@ void launch_begin(Engine &e, cudaStream_t s);
 void launch_rehash(Engine &e, cudaStream_t s);
 void launch_compact(Engine &e, cudaStream_t s);
 void launch_sweep(Engine &e, cudaStream_t s);
+// sets the per-kernel launch attributes a context needs (non-zero: failure)
+int configure_kernels(Engine &e);
 void launch_expand(Engine &e, cudaStream_t s);
 void launch_spawn(Engine &e, cudaStream_t s);
 void launch_core(Engine &e, cudaStream_t s);

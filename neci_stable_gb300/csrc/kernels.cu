@@ -35,6 +35,7 @@
 #include "engine.cuh"
 #include "excitgen.cuh"
 #include "internal.h"
+#include "stage.cuh"
 
 namespace neci {
 
@@ -125,10 +126,12 @@ __device__ inline void load_rh2(const DevSys &s, int32_t *sh) {
 }
 
 // Remove slot j from the walker hash (RemoveHashDet, load_balancer.fpp:631).
+// The caller counts the tombstone and adds its count to Control::n_tomb once
+// per block (one atomic per removal would serialise millions of them per
+// step on one address).
 __device__ inline void hash_remove(const DevState &st, long long j) {
     const uint32_t b = st.slot_bucket[j];
     st.hash[b] = kTomb;
-    atomicAdd(&st.ctl->n_tomb, 1ull);
 }
 
 // Look a determinant up: returns slot or -1.
@@ -149,8 +152,9 @@ __device__ inline long long hash_find(const DevState &st, const unsigned long lo
     return -1;
 }
 
-// Insert a determinant known to be absent.
-__device__ inline void hash_insert(const DevState &st, long long slot, unsigned long long h, Control *ctl) {
+// Insert a determinant known to be absent.  Returns 1 if it took a
+// tombstone's bucket (the caller takes one off its tombstone count).
+__device__ inline int hash_insert(const DevState &st, long long slot, unsigned long long h, Control *ctl) {
     const unsigned long long mask = st.hash_n - 1;
     unsigned long long b = hash_mod(h, st.hash_n);
     for (int p = 0; p < kProbeLimit; ++p) {
@@ -158,14 +162,14 @@ __device__ inline void hash_insert(const DevState &st, long long slot, unsigned 
         if (e == kEmpty || e == kTomb) {
             if (atomicCAS(&st.hash[b], e, (uint32_t)(slot + 1)) == e) {
                 st.slot_bucket[slot] = (uint32_t)b;
-                if (e == kTomb) atomicAdd(&ctl->n_tomb, ~0ull);  // -1
-                return;
+                return e == kTomb ? 1 : 0;
             }
             continue;  // lost the race for this bucket: look at it again
         }
         b = (b + 1) & mask;
     }
     set_err(ctl, NECI_GPU_ERR_HASH_FULL);
+    return 0;
 }
 
 // TestInitiator_explicit (fcimc_helper.F90:1142-1240) without ADI, senior
@@ -182,7 +186,7 @@ __device__ inline bool test_initiator(const IterParams &p, bool was, double sgn,
 // ===========================================================================
 __global__ void k_begin(DevState st) {
     Control *c = st.ctl;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && !c->halted) {
         c->n_free = 0; c->free_taken = 0; c->n_att = 0; c->n_spawned = 0; c->n_cand = 0;
         c->n_reps = 0; c->n_new = 0; c->n_attempts = 0; c->n_occupied = 0; c->n_holes = 0; c->n_found = 0;
         c->n_big = 0;
@@ -200,6 +204,7 @@ __global__ void k_begin(DevState st) {
 // Rehash: clear every bucket, then reinsert live slots (run only when the
 // tombstone share is high; the flag is decided on the host from n_tomb).
 __global__ void k_hash_clear(DevState st) {
+    if (halted(st)) return;
     if (!st.ctl->rehash) return;
     for (unsigned long long b = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; b < st.hash_n;
          b += (unsigned long long)gridDim.x * blockDim.x)
@@ -207,10 +212,11 @@ __global__ void k_hash_clear(DevState st) {
     if (blockIdx.x == 0 && threadIdx.x == 0) st.ctl->n_tomb = 0;
 }
 __global__ void k_hash_fill(DevSys s, DevState st) {
+    if (halted(st)) return;
     if (!st.ctl->rehash) return;
     extern __shared__ int32_t sh_rh2[];
     load_rh2(s, sh_rh2);
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
         const long long *r = st.dets + j * s.R;
         bool occ = is_core_flags(r[s.W + s.L]);
@@ -258,8 +264,9 @@ __device__ inline unsigned int tile_rank(bool keep, unsigned int &count) {
 }
 
 __global__ void __launch_bounds__(kCompactTile) k_compact_count(DevSys s, DevState st) {
+    if (halted(st)) return;
     if (!st.ctl->compact) return;
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const long long j = t * kCompactTile + threadIdx.x;
@@ -271,8 +278,9 @@ __global__ void __launch_bounds__(kCompactTile) k_compact_count(DevSys s, DevSta
 
 // One block: exclusive scan of the tile counts; K = the kept total.
 __global__ void __launch_bounds__(kCompactTile) k_compact_scan(DevState st) {
+    if (halted(st)) return;
     if (!st.ctl->compact) return;
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
     __shared__ unsigned int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -301,8 +309,9 @@ __global__ void __launch_bounds__(kCompactTile) k_compact_scan(DevState st) {
 
 // Holes below K by rank; the number of kept slots below K.
 __global__ void __launch_bounds__(kCompactTile) k_compact_holes(DevSys s, DevState st) {
+    if (halted(st)) return;
     if (!st.ctl->compact) return;
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     const long long K = (long long)st.ctl->compact_k;
     const long long ntiles = (n + kCompactTile - 1) / kCompactTile;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -322,8 +331,9 @@ __global__ void __launch_bounds__(kCompactTile) k_compact_holes(DevSys s, DevSta
 // Every kept slot at or above K moves into the hole of its rank.  Only rows
 // at or above K are read, and only holes below K are written.
 __global__ void k_compact_move(DevSys s, DevState st) {
+    if (halted(st)) return;
     if (!st.ctl->compact) return;
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     const long long K = (long long)st.ctl->compact_k;
     const long long pos_k = (long long)st.ctl->compact_pos_k;
     for (long long j = K + blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n;
@@ -346,6 +356,7 @@ __global__ void k_compact_move(DevSys s, DevState st) {
 
 // Closes the compaction: TotWalkers = K, the hash is rebuilt next.
 __global__ void k_compact_done(DevState st) {
+    if (halted(st)) return;
     Control *c = st.ctl;
     if (!c->compact) return;
     c->tot_walkers = c->compact_k;
@@ -357,27 +368,75 @@ __global__ void k_compact_done(DevState st) {
 // k_sweep
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const IterParams *pp) {
+    if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
-    const long long n = (long long)c->tot_walkers;
+    const long long n = slots_in_use(st);
     const int W = s.W, L = s.L, R = s.R;
     double acc_old[2] = {0.0, 0.0}, acc_hf[2] = {0.0, 0.0}, acc_en[2] = {0.0, 0.0};
     double acc_died[2] = {0.0, 0.0}, acc_born[2] = {0.0, 0.0}, acc_ab[2] = {0.0, 0.0};
     double death_max = 0.0;  // max_death_cpt of this thread's determinants (tau search)
-    unsigned long long acc_att = 0;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    const long long nround = ((n + stride - 1) / stride) * stride;  // all lanes iterate together
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < nround; j += stride) {
+    unsigned long long acc_att = 0, acc_tomb = 0;
+    // Tiles of kStageTile slots (one per block and round) are staged into
+    // shared memory by TMA bulk copies, the next tile's while this one is
+    // processed: rows, diagH and offdiagH of the tile.  Writes go to global.
+    extern __shared__ __align__(16) unsigned char sweep_smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int stage_ok;
+    const size_t stage_bytes = (size_t)kStageTile * (R + 2) * 8;
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const long long nrounds = (n + (long long)gridDim.x * kStageTile - 1) / ((long long)gridDim.x * kStageTile);
+    auto issue = [&](long long k) {  // thread 0: the copies of round k's tile
+        const long long tile = blockIdx.x + k * gridDim.x;
+        const int rows = stage_rows(tile, n);
+        if (rows == 0) return;
+        unsigned char *base = sweep_smem + (k & 1) * stage_bytes;
+        const uint32_t br = (uint32_t)rows * R * 8, bd = (uint32_t)rows * 8;
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bars[k & 1], br + 2 * bd);
+        bulk_g2s(base, st.dets + tile * kStageTile * R, br, &bars[k & 1]);
+        bulk_g2s(base + (size_t)kStageTile * R * 8, st.diagH + tile * kStageTile, bd, &bars[k & 1]);
+        bulk_g2s(base + (size_t)kStageTile * (R + 1) * 8, st.offdiagH + tile * kStageTile, bd, &bars[k & 1]);
+    };
+    if (threadIdx.x == 0 && nrounds > 0) issue(0);
+    for (long long kr = 0; kr < nrounds; ++kr) {
+        const long long tile = blockIdx.x + kr * gridDim.x;
+        const unsigned char *sbase = sweep_smem + (kr & 1) * stage_bytes;
+        if (threadIdx.x == 0 && kr + 1 < nrounds) issue(kr + 1);
+        if (stage_rows(tile, n) > 0) {
+            if (threadIdx.x == 0) stage_ok = mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1)) ? 1 : 0;
+            __syncthreads();
+            if (!stage_ok) {
+                // a copy that never completed: report it, give the copies in
+                // flight a last bounded wait, and leave
+                if (threadIdx.x == 0) {
+                    set_err(c, NECI_GPU_ERR_TIMEOUT);
+                    (void)mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1));
+                    if (kr + 1 < nrounds) (void)mbar_wait_bounded(&bars[(kr + 1) & 1], (uint32_t)(((kr + 1) >> 1) & 1));
+                }
+                __syncthreads();
+                return;
+            }
+        }
+        const long long j = tile * kStageTile + threadIdx.x;
         bool live = j < n;
-        long long *r = st.dets + (live ? j : 0) * R;
+        long long *r = st.dets + (live ? j : 0) * R;  // the global row (writes)
+        const long long *sr = (const long long *)sbase + (size_t)threadIdx.x * R;  // its staged copy (reads)
+        const double *sdiag = (const double *)(sbase + (size_t)kStageTile * R * 8);
+        const double *soffd = (const double *)(sbase + (size_t)kStageTile * (R + 1) * 8);
         unsigned long long d[kMaxWords];
         double C[2] = {0.0, 0.0};
         long long flags = 0;
         bool core = false, occ = false;
         if (live) {
-            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
-            for (int k = 0; k < L; ++k) C[k] = word_to_double(r[W + k]);
-            flags = r[W + L];
+            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)sr[w];
+            for (int k = 0; k < L; ++k) C[k] = word_to_double(sr[W + k]);
+            flags = sr[W + L];
             core = st.n_core > 0 && is_core_flags(flags);
             for (int k = 0; k < L; ++k) {
                 acc_old[k] += fabs(C[k]);
@@ -392,6 +451,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
         const bool hole = live && !occ && !core;
         unsigned int nsp[2] = {0, 0};
         bool neg[2] = {false, false};
+        bool out_zero = true;
         if (live && occ) {
             const int exl = excit_level(s.ilut_ref, d, W);
             const bool is_ref = exl == 0;
@@ -404,7 +464,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 }
                 if (nf != flags) { r[W + L] = nf; flags = nf; }
             }
-            const double odh = st.offdiagH[j];
+            const double odh = soffd[threadIdx.x];
             for (int k = 0; k < L; ++k) {
                 if (is_ref) acc_hf[k] += C[k];
                 acc_en[k] += odh * C[k];
@@ -434,7 +494,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             // walker_death + attempt_die_normal (fcimc_helper.F90:2279-2407,
             // fcimc_pointed_fns.F90:573-705)
             Stream rd(dkey, p.iter, P_DEATH, 0, 0);
-            const double Kii = st.diagH[j];
+            const double Kii = sdiag[threadIdx.x];
             double cp[2] = {0.0, 0.0};
             bool any = false;
             for (int k = 0; k < L; ++k) {
@@ -464,15 +524,19 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 for (int k = 0; k < L; ++k) if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
             }
             if (any || core) {
-                for (int k = 0; k < L; ++k) r[W + k] = double_to_word(cp[k]);
+                for (int k = 0; k < L; ++k) {
+                    r[W + k] = double_to_word(cp[k]);
+                    out_zero = out_zero && abs_bits(cp[k]) == 0;
+                }
             } else {
                 hash_remove(st, j);
+                ++acc_tomb;
                 r[W + L] = flags | 1ll;  // flag_removed
                 for (int k = 0; k < L; ++k) r[W + k] = double_to_word(0.0);
             }
         }
-        const bool freed = live && occ && !core && abs_bits(word_to_double(r[W])) == 0 &&
-                           (L == 1 || abs_bits(word_to_double(r[W + 1])) == 0);
+        // the signs just written are all zero
+        const bool freed = live && occ && !core && out_zero;
         // append free slots
         {
             const unsigned int want = (hole || freed) ? 1u : 0u;
@@ -520,6 +584,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 }
             }
         }
+        __syncthreads();  // this round's stage is refilled two rounds on
     }
     const double v[12] = {acc_old[0], acc_old[1], acc_hf[0], acc_hf[1], acc_en[0], acc_en[1], acc_died[0],
                           acc_died[1], acc_born[0], acc_born[1], acc_ab[0], acc_ab[1]};
@@ -527,9 +592,9 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                              &c->enum_cyc[0], &c->enum_cyc[1], &c->ndied[0], &c->ndied[1],
                              &c->nborn[0], &c->nborn[1], &c->naborted[0], &c->naborted[1]};
     block_add<12>(v, dst, L);
-    unsigned long long u[1] = {acc_att};
-    unsigned long long *const du[1] = {&c->n_attempts};
-    block_add_u<1>(u, du);
+    unsigned long long u[2] = {acc_att, acc_tomb};
+    unsigned long long *const du[2] = {&c->n_attempts, &c->n_tomb};
+    block_add_u<2>(u, du);
     if (s.tau_search) {
         // non-negative doubles order like their bit patterns
         unsigned long long b = (unsigned long long)__double_as_longlong(death_max);
@@ -546,6 +611,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
 // k_expand: attempt entries of heavily populated parents, one block per parent.
 // ===========================================================================
 __global__ void k_expand(DevState st) {
+    if (halted(st)) return;
     // parents with more than kHugeAttempts attempts: the whole grid per parent
     const unsigned long long nh = min(st.ctl->n_huge, (unsigned long long)kMaxHuge);
     for (unsigned long long b = 0; b < nh; ++b) {
@@ -751,6 +817,7 @@ __device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, 
 // long: run inline they would stall the doubles of their warp).
 template <typename Real, int GEN>
 __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp) {
+    if (halted(st)) return;
     extern __shared__ int32_t sh[];
     __shared__ unsigned long long sq[256];
     __shared__ int sq_n;
@@ -829,6 +896,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
 // FP32 hi/lo accumulation and an FP64 final sum)
 // ===========================================================================
 __global__ void k_core(DevSys s, DevState st, const IterParams *pp) {
+    if (halted(st)) return;
     const int L = s.L;
     const double tau = pp->tau;
     const bool mixed = pp->precision == NECI_PREC_MIXED;
@@ -862,6 +930,7 @@ __global__ void k_core(DevSys s, DevState st, const IterParams *pp) {
 // Annihilation pass 1: probe the walker hash with every spawn record.
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
+    if (halted(st)) return;
     extern __shared__ int32_t sh_rh2[];
     load_rh2(s, sh_rh2);
     Control *c = st.ctl;
@@ -911,6 +980,7 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
 // Annihilation pass 2: merge candidates per determinant.
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
+    if (halted(st)) return;
     Control *c = st.ctl;
     const long long n = (long long)c->n_cand;
     const int W = s.W, L = s.L, R = s.R;
@@ -960,6 +1030,7 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
 // Annihilation pass 3: unique new determinants -> CurrentDets.
 // ===========================================================================
 __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const IterParams *pp) {
+    if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
     const long long n = (long long)c->n_reps;
@@ -968,8 +1039,12 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
     unsigned long long a_s[2] = {0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
+    long long a_tomb = 0;  // tombstones taken over by the insertions (a negative count)
     for (long long ri = blockIdx.x * (long long)blockDim.x + threadIdx.x; ri < nround; ri += stride) {
-        bool inserted = false;
+        bool inserted = false, want = false;
+        unsigned long long wd[kMaxWords];
+        double ws[2] = {0.0, 0.0};
+        long long wflags = 0, wci = 0;
         if (ri < n) {
             const long long ci = st.reps[ri];
             st.spawn_hash[st.rep_bucket[ri]] = kEmpty;  // leave the table clean
@@ -1027,28 +1102,53 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
                     for (int k = 0; k < L; ++k) if (fabs(ss[k]) >= kEps12) unocc = false;
                 }
                 if (!unocc) {
-                    // AddNewHashDet (load_balancer.fpp:514-629)
-                    long long slot;
-                    const unsigned long long t = atomicAdd(&c->free_taken, 1ull);
-                    if (t < c->n_free) {
-                        slot = st.free_list[t];
-                    } else {
-                        slot = (long long)atomicAdd(&c->tot_walkers, 1ull);
-                    }
-                    if (slot + 1 >= st.max_walkers) {
-                        set_err(c, NECI_GPU_ERR_LIST_FULL);
-                    } else {
-                        long long *o = st.dets + slot * R;
-                        for (int w = 0; w < W; ++w) o[w] = (long long)d[w];
-                        for (int k = 0; k < L; ++k) o[W + k] = double_to_word(ss[k]);
-                        o[W + L] = flags & ~1ll;
-                        st.diagH[slot] = diag_helement(s, d) - s.hii;
-                        const int ic = excit_level(s.ilut_ref, d, W);
-                        st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
-                        if (st.n_core > 0) st.core_of_slot[slot] = -1;
-                        hash_insert(st, slot, st.cand_h[ci], c);
-                        inserted = true;
-                    }
+                    // AddNewHashDet (load_balancer.fpp:514-629): a slot below
+                    want = true;
+                    for (int w = 0; w < W; ++w) wd[w] = d[w];
+                    ws[0] = ss[0];
+                    ws[1] = ss[1];
+                    wflags = flags;
+                    wci = ci;
+                }
+            }
+        }
+        // Slots for the new determinants of the warp: the next holes of the
+        // free list (one atomic on its cursor), then fresh slots at the end
+        // of the list (one atomic on TotWalkers) when the holes run out.
+        {
+            const int lane = threadIdx.x & 31;
+            const unsigned int ballot = __ballot_sync(0xffffffffu, want);
+            const unsigned int nwant = __popc(ballot);
+            const unsigned int rank = __popc(ballot & ((1u << lane) - 1u));
+            unsigned long long t0 = 0, f0 = 0;
+            const unsigned long long nfree = c->n_free;
+            if (nwant) {
+                const int leader = __ffs(ballot) - 1;
+                if (lane == leader) {
+                    t0 = atomicAdd(&c->free_taken, (unsigned long long)nwant);
+                    const unsigned long long from_free = t0 >= nfree ? 0ull : min(nfree - t0, (unsigned long long)nwant);
+                    if (nwant > from_free) f0 = atomicAdd(&c->tot_walkers, (unsigned long long)(nwant - from_free));
+                }
+                t0 = __shfl_sync(0xffffffffu, t0, leader);
+                f0 = __shfl_sync(0xffffffffu, f0, leader);
+            }
+            if (want) {
+                const unsigned long long t = t0 + rank;
+                const unsigned long long first_fresh = t0 >= nfree ? t0 : nfree;  // the first t that gets a fresh slot
+                const long long slot = t < nfree ? (long long)st.free_list[t] : (long long)(f0 + (t - first_fresh));
+                if (slot + 1 >= st.max_walkers) {
+                    set_err(c, NECI_GPU_ERR_LIST_FULL);
+                } else {
+                    long long *o = st.dets + slot * R;
+                    for (int w = 0; w < W; ++w) o[w] = (long long)wd[w];
+                    for (int k = 0; k < L; ++k) o[W + k] = double_to_word(ws[k]);
+                    o[W + L] = wflags & ~1ll;
+                    st.diagH[slot] = diag_helement(s, wd) - s.hii;
+                    const int ic = excit_level(s.ilut_ref, wd, W);
+                    st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, wd, ic) : 0.0;
+                    if (st.n_core > 0) st.core_of_slot[slot] = -1;
+                    a_tomb -= hash_insert(st, slot, st.cand_h[wci], c);
+                    inserted = true;
                 }
             }
         }
@@ -1059,8 +1159,9 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                             &c->nborn[0], &c->nborn[1]};
     block_add<6>(v, dst, s.L);
-    unsigned long long *const du[2] = {&c->abs_s[0], &c->abs_s[1]};
-    block_add_u<2>(a_s, du);
+    unsigned long long u[3] = {a_s[0], a_s[1], (unsigned long long)a_tomb};  // two's complement for -count
+    unsigned long long *const du[3] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb};
+    block_add_u<3>(u, du);
 }
 
 // ===========================================================================
@@ -1068,19 +1169,45 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
 // CalcHashTableStats in one sweep.
 // ===========================================================================
 __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core) {
+    if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
     const long long n = (long long)min(c->tot_walkers, (unsigned long long)st.max_walkers);
     const int W = s.W, L = s.L, R = s.R;
     double a_born[2] = {0, 0}, a_ann[2] = {0, 0}, a_ab[2] = {0, 0}, a_rm[2] = {0, 0};
     double a_tp[2] = {0, 0}, a_norm[2] = {0, 0};
-    unsigned long long a_s[2] = {0, 0}, a_occ = 0, a_holes = 0, a_found = 0;
-    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+    unsigned long long a_s[2] = {0, 0}, a_occ = 0, a_holes = 0, a_found = 0, a_tomb = 0;
+    // Tiles staged into shared memory by TMA bulk copies as in k_sweep: the
+    // rows and the per-slot spawn counts (meta) of the tile.
+    extern __shared__ __align__(16) unsigned char merge_smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int stage_ok;
+    const size_t stage_bytes = (size_t)kStageTile * (R * 8 + L * 4);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const long long nrounds = (n + (long long)gridDim.x * kStageTile - 1) / ((long long)gridDim.x * kStageTile);
+    auto issue = [&](long long k) {  // thread 0: the copies of round k's tile
+        const long long tile = blockIdx.x + k * gridDim.x;
+        const int rows = stage_rows(tile, n);
+        if (rows == 0) return;
+        unsigned char *base = merge_smem + (k & 1) * stage_bytes;
+        const uint32_t br = (uint32_t)rows * R * 8, bm = (uint32_t)rows * L * 4;
+        fence_proxy_async_smem();
+        mbar_expect_tx(&bars[k & 1], br + bm);
+        bulk_g2s(base, st.dets + tile * kStageTile * R, br, &bars[k & 1]);
+        bulk_g2s(base + (size_t)kStageTile * R * 8, st.meta + tile * kStageTile * L, bm, &bars[k & 1]);
+    };
+    // one slot: its row (global, for writes), staged row and staged meta
+    auto body = [&](long long j, const long long *sr, const uint32_t *sm) {
         long long *r = st.dets + j * R;
-        const long long flags = r[W + L];
+        const long long flags = sr[W + L];
         const bool core = st.n_core > 0 && is_core_flags(flags);
         double C[2] = {0.0, 0.0};
-        for (int k = 0; k < L; ++k) C[k] = word_to_double(r[W + k]);
+        for (int k = 0; k < L; ++k) C[k] = word_to_double(sr[W + k]);
         bool changed = false;
         // deterministic_annihilation (Annihilation.F90:930-963)
         if (core && with_core) {
@@ -1097,7 +1224,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         uint32_t m[2] = {0, 0};
         bool has = false;
         for (int k = 0; k < L; ++k) {
-            m[k] = st.meta[j * L + k];
+            m[k] = sm[k];
             if (m[k]) has = true;
         }
         if (has) {
@@ -1125,6 +1252,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                 for (int k = 0; k < L; ++k) if (abs_bits(C[k]) >= dbl_bits(kEps12)) unocc = false;
                 if (unocc) {
                     hash_remove(st, j);
+                    ++a_tomb;
                     r[W + L] = flags | 1ll;
                 }
             }
@@ -1135,14 +1263,14 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         if (!occ && !core) {
             if (changed) for (int k = 0; k < L; ++k) r[W + k] = double_to_word(C[k]);
             ++a_holes;
-            continue;
+            return;
         }
         if (!core) {
             for (int k = 0; k < L; ++k) {
                 const double a = fabs(C[k]);
                 if (abs_bits(a) > dbl_bits(kEps12) && abs_bits(a) < dbl_bits(p.occupied_thresh)) {
                     unsigned long long d[kMaxWords];
-                    for (int w = 0; w < W; ++w) d[w] = (unsigned long long)r[w];
+                    for (int w = 0; w < W; ++w) d[w] = (unsigned long long)sr[w];
                     Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
                     const double pRemove = (p.occupied_thresh - a) / p.occupied_thresh;
                     if (bern(rng, pRemove)) {
@@ -1152,6 +1280,7 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                         for (int k2 = 0; k2 < L; ++k2) if (abs_bits(C[k2]) >= dbl_bits(kEps12)) unocc = false;
                         if (unocc) {
                             hash_remove(st, j);
+                            ++a_tomb;
                             r[W + L] = flags | 1ll;
                         }
                     } else {
@@ -1172,11 +1301,35 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         if (occ || core) {
             ++a_occ;
             bool is_ref = true;
-            for (int w = 0; w < W; ++w) if ((unsigned long long)r[w] != s.ilut_ref[w]) is_ref = false;
+            for (int w = 0; w < W; ++w) if ((unsigned long long)sr[w] != s.ilut_ref[w]) is_ref = false;
             if (is_ref) for (int k = 0; k < L; ++k) c->noat_hf[k] = C[k];
         } else {
             ++a_holes;
         }
+        };
+    if (threadIdx.x == 0 && nrounds > 0) issue(0);
+    for (long long kr = 0; kr < nrounds; ++kr) {
+        const long long tile = blockIdx.x + kr * gridDim.x;
+        const unsigned char *sbase = merge_smem + (kr & 1) * stage_bytes;
+        if (threadIdx.x == 0 && kr + 1 < nrounds) issue(kr + 1);
+        if (stage_rows(tile, n) > 0) {
+            if (threadIdx.x == 0) stage_ok = mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1)) ? 1 : 0;
+            __syncthreads();
+            if (!stage_ok) {
+                if (threadIdx.x == 0) {
+                    set_err(c, NECI_GPU_ERR_TIMEOUT);
+                    (void)mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1));
+                    if (kr + 1 < nrounds) (void)mbar_wait_bounded(&bars[(kr + 1) & 1], (uint32_t)(((kr + 1) >> 1) & 1));
+                }
+                __syncthreads();
+                return;
+            }
+        }
+        const long long j = tile * kStageTile + threadIdx.x;
+        if (j < n)
+            body(j, (const long long *)sbase + (size_t)threadIdx.x * R,
+                 (const uint32_t *)(sbase + (size_t)kStageTile * R * 8) + (size_t)threadIdx.x * L);
+        __syncthreads();  // this round's stage is refilled two rounds on
     }
     double v[12] = {a_born[0], a_born[1], a_ann[0], a_ann[1], a_ab[0], a_ab[1], a_rm[0], a_rm[1],
                     a_tp[0], a_tp[1], a_norm[0], a_norm[1]};
@@ -1184,9 +1337,10 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                              &c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                              &c->tot_parts[0], &c->tot_parts[1], &c->norm[0], &c->norm[1]};
     block_add<12>(v, dst, L);
-    unsigned long long u[5] = {a_s[0], a_s[1], a_occ, a_holes, a_found};
-    unsigned long long *const du[5] = {&c->abs_s[0], &c->abs_s[1], &c->n_occupied, &c->n_holes, &c->n_found};
-    block_add_u<5>(u, du);
+    unsigned long long u[6] = {a_s[0], a_s[1], a_occ, a_holes, a_found, a_tomb};
+    unsigned long long *const du[6] = {&c->abs_s[0], &c->abs_s[1], &c->n_occupied, &c->n_holes, &c->n_found,
+                                       &c->n_tomb};
+    block_add_u<6>(u, du);
 }
 
 // ===========================================================================
@@ -1245,6 +1399,7 @@ __device__ inline void rdm_add_pair(const DevSys &s, const DevState &st, const u
 }
 
 __global__ void __launch_bounds__(256) k_rdm_offdiag(DevSys s, DevState st) {
+    if (halted(st)) return;
     extern __shared__ int32_t sh_rh2[];
     load_rh2(s, sh_rh2);
     Control *c = st.ctl;
@@ -1271,6 +1426,7 @@ __global__ void __launch_bounds__(256) k_rdm_offdiag(DevSys s, DevState st) {
 
 // Diagonal terms; per-block sums in shared memory when npair doubles fit.
 __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use_shared) {
+    if (halted(st)) return;
     extern __shared__ double sh_diag[];
     const long long npair = s.npair;
     if (use_shared) {
@@ -1306,6 +1462,14 @@ __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use
 __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, int advance_iter, long long n_core) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     Control *c = st.ctl;
+    if (c->halted) {
+        // a previous step failed: report its status again, change nothing
+        neci_gpu_iter_stats r{};
+        r.err = c->halted;
+        *out = r;
+        return;
+    }
+    if (c->tot_walkers > (unsigned long long)st.max_walkers) c->tot_walkers = (unsigned long long)st.max_walkers;
     neci_gpu_iter_stats r;
     for (int k = 0; k < 2; ++k) {
         r.nborn[k] = c->nborn[k];
@@ -1339,6 +1503,8 @@ __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, i
     c->rehash = (c->n_occupied + c->n_tomb) * 10ull > st.hash_n * 7ull ? 1 : 0;
     // compact the list before the next step when holes outnumber occupied slots
     c->compact = (c->tot_walkers > (unsigned long long)(4 * kCompactTile) && c->n_holes * 2ull > c->tot_walkers) ? 1 : 0;
+    // a failed step halts the ones after it (in the same graph batch)
+    if (c->err) c->halted = c->err;
 }
 
 // ===========================================================================
@@ -1372,8 +1538,27 @@ void launch_rehash(Engine &e, cudaStream_t s) {
     k_hash_fill<<<grid_for(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
 }
 
+// Dynamic shared memory of the staged sweeps: two stages of a tile.
+static size_t sweep_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R + 2) * 8; }
+static size_t merge_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R * 8 + e.sys.L * 4); }
+
+int configure_kernels(Engine &e) {
+    // The stages and the block reductions' shared arrays pass the default
+    // 48 KB per block.  The limit is an attribute of the kernel for the whole
+    // process, so it is raised to the largest row any context can have
+    // (kMaxWords det words, two signs, a flag word), never lowered.
+    (void)e;
+    const int rmax = kMaxWords + 2 + 1;
+    const int sweep_max = 2 * kStageTile * (rmax + 2) * 8;
+    const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 4);
+    if (cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(k_merge_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
+        return 1;
+    return 0;
+}
+
 void launch_sweep(Engine &e, cudaStream_t s) {
-    k_sweep<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
+    k_sweep<<<grid_for(e, 256), kStageTile, sweep_smem_bytes(e), s>>>(e.sys, e.st, e.d_params);
 }
 void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256), 256, 0, s>>>(e.st); }
 void launch_spawn(Engine &e, cudaStream_t s) {
@@ -1404,7 +1589,7 @@ void launch_ann_insert(Engine &e, cudaStream_t s) {
     k_ann_insert<<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
-    k_merge_stats<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params, with_core);
+    k_merge_stats<<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core);
 }
 void launch_rdm(Engine &e, cudaStream_t s) {
     if (!e.sys.rdm) return;

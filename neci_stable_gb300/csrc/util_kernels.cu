@@ -79,7 +79,7 @@ __global__ void k_upload_fix(DevSys s, DevState st, long long nrows, int compute
 // Holes of the current list -> free list (the sweep's FreeSlot pass) for an
 // injected annihilation; also resets the step counters.
 __global__ void k_collect_holes(DevSys s, DevState st) {
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
         const long long *r = st.dets + j * s.R;
         bool occ = false;
@@ -90,7 +90,7 @@ __global__ void k_collect_holes(DevSys s, DevState st) {
     }
 }
 __global__ void k_tot_parts_old(DevSys s, DevState st) {
-    const long long n = (long long)st.ctl->tot_walkers;
+    const long long n = slots_in_use(st);
     double a[2] = {0.0, 0.0};
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
         for (int k = 0; k < s.L; ++k) a[k] += fabs(word_to_double(st.dets[j * s.R + s.W + k]));

@@ -193,6 +193,22 @@ def test_errors_are_reported_not_faulted():
     assert st.err == 0
 
 
+def test_list_overflow_inside_a_batch_halts_the_batch():
+    """CurrentDets overflowing in the middle of a batch of graph-launched
+    steps: the step reports NECI_GPU_ERR_LIST_FULL, the steps after it in the
+    batch do nothing (no slot beyond the allocation is touched), and an
+    upload makes the context usable again."""
+    spec = hubbard10()
+    eng = Engine(spec, max_walkers=4096, max_spawned=1 << 20)
+    eng.start_from_reference(initial_part=3000.0)
+    with pytest.raises(capi.NeciGpuError) as ei:
+        eng.iterate_n(capi.default_params(tau=0.05, seed=2, iter=1), 20)
+    assert ei.value.code == capi.ERR_LIST_FULL
+    eng.start_from_reference(initial_part=5.0)
+    st = eng.iterate_n(capi.default_params(tau=0.01, seed=2, iter=1), 5)
+    assert all(s.err == 0 for s in st) and st[-1].tot_walkers <= 4096
+
+
 def test_batched_steps_equal_single_steps():
     """neci_gpu_iterate_batch changes only concurrency: every instance ends
     with the walker list it has when stepped alone."""
