@@ -18,7 +18,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libneci_gpu.so"
-SOURCES = ["kernels.cu", "util_kernels.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["kernels.cu", "spawn_fp64.cu", "spawn_fp32.cu", "util_kernels.cu", "capi.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "--expt-relaxed-constexpr"]

@@ -16,6 +16,8 @@
 namespace neci {
 
 constexpr int kMaxWords = 4;      // nBasis <= 255 (NIfD <= 3)
+// A loop over the words 0..W-1 of a determinant, unrolled over kMaxWords.
+#define NECI_FOR_WORDS(w, W) _Pragma("unroll") for (int w = 0; w < kMaxWords; ++w) if (w < (W))
 constexpr int kMaxNel = 64;
 constexpr int kMaxNeigh = 8;
 constexpr int kBigAttempts = 32;  // parents with more attempts are expanded by k_expand
@@ -221,9 +223,12 @@ __host__ __device__ inline unsigned long long splitmix64(unsigned long long x) {
     return z ^ (z >> 31);
 }
 
-__host__ __device__ inline unsigned long long det_key(const unsigned long long *det, int W, unsigned long long seed) {
+// Key of a determinant's random streams.  Words at or above nset (those
+// past the last orbital) are zero and are not read.
+__host__ __device__ inline unsigned long long det_key(const unsigned long long *det, int W, unsigned long long seed,
+                                                      int nset = kMaxWords) {
     unsigned long long h = seed ^ 0x6A09E667F3BCC909ull;
-    for (int i = 0; i < W; ++i) h = splitmix64(h ^ det[i]);
+    NECI_FOR_WORDS(i, W) h = splitmix64(h ^ (i < nset ? det[i] : 0ull));
     return h;
 }
 
@@ -303,24 +308,47 @@ __device__ inline bool is_core_flags(long long f) { return test_bit(f, NECI_FLAG
 // ---------------------------------------------------------------------------
 // Bit strings.
 // ---------------------------------------------------------------------------
+// The loops over determinant words run over kMaxWords with a guard and are
+// unrolled, and a word is picked by orbital through selects, never by a
+// run-time index: a determinant copied into a thread's array then stays in
+// registers (an array indexed at run time is placed in local memory).
 __device__ inline int excit_level(const unsigned long long *a, const unsigned long long *b, int W) {
     int ic = 0;
-    for (int i = 0; i < W; ++i) ic += __popcll(a[i] & ~b[i]);
+#pragma unroll
+    for (int i = 0; i < kMaxWords; ++i)
+        if (i < W) ic += __popcll(a[i] & ~b[i]);
     return ic;
 }
 __device__ inline bool det_eq(const unsigned long long *a, const long long *b, int W) {
-    for (int i = 0; i < W; ++i)
-        if ((long long)a[i] != b[i]) return false;
-    return true;
+    bool eq = true;
+#pragma unroll
+    for (int i = 0; i < kMaxWords; ++i)
+        if (i < W) eq = eq && (long long)a[i] == b[i];
+    return eq;
 }
-__device__ inline bool orb_occ(const unsigned long long *d, int orb) {
-    return (d[(orb - 1) >> 6] >> ((orb - 1) & 63)) & 1ull;
+// The word holding orbital orb (1-based).
+__device__ inline unsigned long long orb_word(const unsigned long long *d, int orb) {
+    const int w = (orb - 1) >> 6;
+    unsigned long long r = 0;
+#pragma unroll
+    for (int k = 0; k < kMaxWords; ++k)
+        if (w == k) r = d[k];
+    return r;
 }
-__device__ inline void flip_orb(unsigned long long *d, int orb) { d[(orb - 1) >> 6] ^= 1ull << ((orb - 1) & 63); }
+__device__ inline bool orb_occ(const unsigned long long *d, int orb) { return (orb_word(d, orb) >> ((orb - 1) & 63)) & 1ull; }
+__device__ inline void flip_orb(unsigned long long *d, int orb) {
+    const int w = (orb - 1) >> 6;
+    const unsigned long long m = 1ull << ((orb - 1) & 63);
+#pragma unroll
+    for (int k = 0; k < kMaxWords; ++k)
+        if (w == k) d[k] ^= m;
+}
 // Occupied orbitals strictly between orbitals lo < hi.
 __device__ inline int occ_between(const unsigned long long *d, int W, int lo, int hi) {
     int n = 0;
-    for (int w = 0; w < W; ++w) {
+#pragma unroll
+    for (int w = 0; w < kMaxWords; ++w) {
+        if (w >= W) break;
         const int base = w * 64;  // orbital base+1 is bit 0
         // bits for orbitals lo+1 .. hi-1 -> bit positions lo .. hi-2
         const int b0 = lo - base, b1 = hi - 2 - base;  // inclusive range in this word
@@ -332,29 +360,41 @@ __device__ inline int occ_between(const unsigned long long *d, int W, int lo, in
     }
     return n;
 }
+// Bit position (0-based) of the (k+1)-th set bit of x, k < popcount(x).
+__device__ inline int select_bit(unsigned long long x, int k) {
+    int pos = 0;
+    int t = __popc((unsigned int)x);
+    if (k >= t) { k -= t; x >>= 32; pos += 32; }
+    t = __popc((unsigned int)(x & 0xFFFFull));
+    if (k >= t) { k -= t; x >>= 16; pos += 16; }
+    t = __popc((unsigned int)(x & 0xFFull));
+    if (k >= t) { k -= t; x >>= 8; pos += 8; }
+    t = __popc((unsigned int)(x & 0xFull));
+    if (k >= t) { k -= t; x >>= 4; pos += 4; }
+    t = __popc((unsigned int)(x & 0x3ull));
+    if (k >= t) { k -= t; x >>= 2; pos += 2; }
+    t = (int)(x & 1ull);
+    if (k >= t) { pos += 1; }
+    return pos;
+}
 // Orbital (1-based) of the n-th (1-based) set bit of (d & pattern), counting
-// from orbital 1 upwards: the n-th electron of that spin class in nI order.
+// from orbital 1 upwards: the n-th electron of that spin class in nI order;
+// 0 if there are fewer.  The word is found first, so a single bit select
+// runs.
 __device__ inline int nth_orbital(const unsigned long long *d, int W, unsigned long long pattern, int n) {
-    for (int w = 0; w < W; ++w) {
-        unsigned long long x = d[w] & pattern;
-        const int c = __popcll(x);
-        if (n > c) { n -= c; continue; }
-        int k = n - 1, pos = 0;
-        int t = __popc((unsigned int)x);
-        if (k >= t) { k -= t; x >>= 32; pos += 32; }
-        t = __popc((unsigned int)(x & 0xFFFFull));
-        if (k >= t) { k -= t; x >>= 16; pos += 16; }
-        t = __popc((unsigned int)(x & 0xFFull));
-        if (k >= t) { k -= t; x >>= 8; pos += 8; }
-        t = __popc((unsigned int)(x & 0xFull));
-        if (k >= t) { k -= t; x >>= 4; pos += 4; }
-        t = __popc((unsigned int)(x & 0x3ull));
-        if (k >= t) { k -= t; x >>= 2; pos += 2; }
-        t = (int)(x & 1ull);
-        if (k >= t) { pos += 1; }
-        return w * 64 + pos + 1;
+    unsigned long long x = 0;
+    int wsel = -1;
+#pragma unroll
+    for (int w = 0; w < kMaxWords; ++w) {
+        if (w < W && wsel < 0) {
+            const unsigned long long y = d[w] & pattern;
+            const int c = __popcll(y);
+            if (n <= c) { x = y; wsel = w; }
+            else n -= c;
+        }
     }
-    return 0;
+    if (wsel < 0) return 0;
+    return wsel * 64 + select_bit(x, n - 1) + 1;
 }
 constexpr unsigned long long kAllBits = ~0ull;
 constexpr unsigned long long kAlphaBits = 0xAAAAAAAAAAAAAAAAull;  // even orbitals
@@ -363,7 +403,9 @@ constexpr unsigned long long kBetaBits = 0x5555555555555555ull;   // odd orbital
 // decode_bit_det: ascending occupied orbitals.
 __device__ inline int decode(const unsigned long long *d, int W, uint8_t *nI) {
     int n = 0;
-    for (int w = 0; w < W; ++w) {
+#pragma unroll
+    for (int w = 0; w < kMaxWords; ++w) {
+        if (w >= W) break;
         unsigned long long x = d[w];
         while (x) {
             const int b = __ffsll((long long)x) - 1;
@@ -378,7 +420,9 @@ __device__ inline int decode(const unsigned long long *d, int W, uint8_t *nI) {
 __device__ inline unsigned long long neci_hash(const unsigned long long *d, int W, const int32_t *rh2) {
     unsigned long long hash = 0;
     int i = 0;
-    for (int w = 0; w < W; ++w) {
+#pragma unroll
+    for (int w = 0; w < kMaxWords; ++w) {
+        if (w >= W) break;
         unsigned long long x = d[w];
         while (x) {
             const int b = __ffsll((long long)x) - 1;
@@ -432,7 +476,7 @@ __device__ inline double sltcnd_1(const DevSys &s, const unsigned long long *d, 
         const size_t row = ((size_t)(id1 - 1) * s.nBI + (id2 - 1)) * s.nBI - 1;
         const double *jr = s.jrow + row, *jkr = s.jkrow + row;
         const unsigned long long same = beta(src) ? 0x5555555555555555ull : 0xAAAAAAAAAAAAAAAAull;
-        for (int w = 0; w < s.W; ++w) {
+        NECI_FOR_WORDS(w, s.W) {
             unsigned long long x = d[w];
             while (x) {
                 const int b = __ffsll((long long)x) - 1;
@@ -473,7 +517,7 @@ __device__ inline double diag_helement(const DevSys &s, const unsigned long long
     if (s.system == NECI_SYS_HUBBARD_REAL_SPACE) {
         // U * number of doubly occupied sites: beta bit 2k and alpha bit 2k+1.
         int n = 0;
-        for (int w = 0; w < s.W; ++w) n += __popcll(d[w] & (d[w] >> 1) & 0x5555555555555555ull);
+        NECI_FOR_WORDS(w, s.W) n += __popcll(d[w] & (d[w] >> 1) & 0x5555555555555555ull);
         return s.uhub * n;
     }
     uint8_t nI[kMaxNel];
@@ -485,7 +529,7 @@ __device__ inline double diag_helement(const DevSys &s, const unsigned long long
 __device__ inline double offdiag_helement(const DevSys &s, const unsigned long long *a, const unsigned long long *b, int ic) {
     if (ic == 1) {
         int src = 0, tgt = 0;
-        for (int w = 0; w < s.W; ++w) {
+        NECI_FOR_WORDS(w, s.W) {
             const unsigned long long x = a[w] & ~b[w], y = b[w] & ~a[w];
             if (x) src = w * 64 + __ffsll((long long)x);
             if (y) tgt = w * 64 + __ffsll((long long)y);
@@ -497,14 +541,14 @@ __device__ inline double offdiag_helement(const DevSys &s, const unsigned long l
     }
     if (ic == 2 && s.system == NECI_SYS_MOLECULAR) {
         int src[2], tgt[2], ns = 0, nt = 0;
-        for (int w = 0; w < s.W; ++w) {
+        NECI_FOR_WORDS(w, s.W) {
             unsigned long long x = a[w] & ~b[w], y = b[w] & ~a[w];
             while (x) { src[ns++] = w * 64 + __ffsll((long long)x); x &= x - 1; }
             while (y) { tgt[nt++] = w * 64 + __ffsll((long long)y); y &= y - 1; }
         }
         // parity of i->a then j->b (sorted pairing), as successive singles
         unsigned long long t[kMaxWords];
-        for (int w = 0; w < s.W; ++w) t[w] = a[w];
+        NECI_FOR_WORDS(w, s.W) t[w] = a[w];
         int lo = min(src[0], tgt[0]), hi = max(src[0], tgt[0]);
         int np = occ_between(t, s.W, lo, hi);
         flip_orb(t, src[0]);

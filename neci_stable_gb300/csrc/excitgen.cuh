@@ -27,6 +27,12 @@ struct Excit {
     unsigned long long aq;  // |amplitude| in fixed point before rounding (2-RDM unbiasing)
 };
 
+// Words of a determinant: NW where a kernel is instantiated for that count
+// (its loops then have fixed trip counts and unused words need no
+// registers), else the system's W.
+template <int NW>
+__device__ inline int nwords(const DevSys &s) { return NW > 0 ? NW : s.W; }
+
 template <typename Real>
 __device__ inline Real tmat_r(const DevSys &s, int i, int j);
 template <>
@@ -46,7 +52,7 @@ __device__ inline float umat_r<float>(const DevSys &s, int i, int j, int k, int 
 
 // sltcnd_1_kernel (sltcnd.fpp:643-679) in precision Real, summed as the
 // FP64 form (one add per occupied k of jrow[k] or, same spin, jkrow[k]).
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, int src, int tgt) {
     Real hel = 0;
     const int id1 = spat(src), id2 = spat(tgt);
@@ -55,7 +61,7 @@ __device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, 
         const Real *jr = (sizeof(Real) == 8 ? (const Real *)s.jrow : (const Real *)s.jrow32) + row;
         const Real *jkr = (sizeof(Real) == 8 ? (const Real *)s.jkrow : (const Real *)s.jkrow32) + row;
         const unsigned long long same = beta(src) ? kBetaBits : kAlphaBits;
-        for (int w = 0; w < s.W; ++w) {
+        NECI_FOR_WORDS(w, nwords<NW>(s)) {
             unsigned long long x = d[w];
             while (x) {
                 const int b = __ffsll((long long)x) - 1;
@@ -78,69 +84,75 @@ __device__ inline Real sltcnd_2_r(const DevSys &s, int i, int j, int a, int b) {
 }
 
 // Child determinant and H_ij of a single src -> tgt.
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void finish_single(const DevSys &s, const unsigned long long *d, int src, int tgt, Excit<Real> &e) {
-    for (int w = 0; w < s.W; ++w) e.child[w] = d[w];
+    NECI_FOR_WORDS(w, nwords<NW>(s)) e.child[w] = d[w];
     flip_orb(e.child, src);
     flip_orb(e.child, tgt);
     const int lo = min(src, tgt), hi = max(src, tgt);
-    const bool par = occ_between(d, s.W, lo, hi) & 1;  // make_single tParity
-    const Real hel = (s.system == NECI_SYS_HUBBARD_REAL_SPACE) ? tmat_r<Real>(s, src, tgt) : sltcnd_1_r<Real>(s, d, src, tgt);
+    const bool par = occ_between(d, nwords<NW>(s), lo, hi) & 1;  // make_single tParity
+    const Real hel = (s.system == NECI_SYS_HUBBARD_REAL_SPACE) ? tmat_r<Real>(s, src, tgt) : sltcnd_1_r<Real, NW>(s, d, src, tgt);
     e.hel = par ? -hel : hel;
 }
 
 // gen_excit_rs_hubbard (real_space_hubbard.F90:1938-2030),
 // create_cum_list_rs_hubbard (:2080) and pick_from_cum_list
 // (lattice_models_utils.F90:150).  The cumulative pick stays in FP64.
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long *d,
                                       const int32_t *neigh, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
     e.cls = TC_SING;
     e.ok = false;
     const int elec = 1 + (int)uniform_index(rng, (unsigned)s.nel);
-    const int src = nth_orbital(d, s.W, kAllBits, elec);  // nI(elec)
+    const int src = nth_orbital(d, nwords<NW>(s), kAllBits, elec);  // nI(elec)
     const int site = spat(src);
-    int orbs[kMaxNeigh];
-    double cum[kMaxNeigh];
-    int nn = 0;
+    const int32_t *nb = neigh + (site - 1) * s.max_neigh;
+    // The cumulative list is walked twice (its total, then the pick) instead
+    // of being stored: the running sums are the same additions in the same
+    // order, so the pick and its probability are those of the stored list.
     double cum_sum = 0.0;
     for (int k = 0; k < s.max_neigh; ++k) {
-        const int n = neigh[(site - 1) * s.max_neigh + k];
+        const int n = nb[k];
         if (n <= 0) continue;
         const int orb = beta(src) ? 2 * n - 1 : 2 * n;
-        double elem = 0.0;
-        if (!orb_occ(d, orb)) elem = fabs(tmat_el(s, src, orb));
-        cum_sum += elem;
-        orbs[nn] = orb;
-        cum[nn] = cum_sum;
-        ++nn;
+        cum_sum += orb_occ(d, orb) ? 0.0 : fabs(tmat_el(s, src, orb));
     }
     if (cum_sum < 1e-10) { e.pgen = 0; return; }
     const double r = rng.next() * cum_sum;
-    int ind = nn;
-    for (int k = 0; k < nn; ++k)
-        if (cum[k] >= r) { ind = k + 1; break; }
-    const double p_orb = (ind == 1) ? cum[0] / cum_sum : (cum[ind - 1] - cum[ind - 2]) / cum_sum;
-    const int orb = orbs[ind - 1];
+    // the first entry with cum >= r, else the last one
+    double c = 0.0, c_at = 0.0, c_before = 0.0;
+    int orb = 0;
+    bool found = false;
+    for (int k = 0; k < s.max_neigh && !found; ++k) {
+        const int n = nb[k];
+        if (n <= 0) continue;
+        const int o = beta(src) ? 2 * n - 1 : 2 * n;
+        c_before = c;
+        c += orb_occ(d, o) ? 0.0 : fabs(tmat_el(s, src, o));
+        c_at = c;
+        orb = o;
+        found = c >= r;
+    }
+    const double p_orb = (c_at - c_before) / cum_sum;
     const double pg = s.p_elec * p_orb;
     e.pgen = (Real)pg;
     e.invp = (Real)(1.0 / pg);
-    finish_single<Real>(s, d, src, orb, e);
+    finish_single<Real, NW>(s, d, src, orb, e);
     e.ok = true;
 }
 
 // CreateSingleExcit (GenRandSymExcitNUMod.F90:1118-1243), C1 symmetry,
 // tCycleOrbs = .false. (rejection for the electron and for the hole).
 // Returns the full single pgen, pSingles / (NExcit * (nel - ElecsWNoExcits)).
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 1;
     e.cls = TC_SING;
     e.ok = false;
     const int norbs = s.nbasis / 2;
     int nalpha = 0, nbeta = 0;
-    for (int w = 0; w < s.W; ++w) {
+    NECI_FOR_WORDS(w, nwords<NW>(s)) {
         nalpha += __popcll(d[w] & 0xAAAAAAAAAAAAAAAAull);
         nbeta += __popcll(d[w] & 0x5555555555555555ull);
     }
@@ -150,7 +162,7 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
     int eleci = 0, ispn = 0, nexcit = 0, src = 0;
     for (int attempts = 0; attempts <= 250; ++attempts) {
         eleci = (int)uniform_index(rng, (unsigned)s.nel) + 1;
-        src = nth_orbital(d, s.W, kAllBits, eleci);  // nI(eleci)
+        src = nth_orbital(d, nwords<NW>(s), kAllBits, eleci);  // nI(eleci)
         ispn = beta(src) ? 2 : 1;
         nexcit = (ispn == 1) ? nun_a : nun_b;
         if (nexcit != 0) break;
@@ -172,22 +184,22 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
         e.pgen = (Real)(s.f_p_singles / (float)count);
         e.invp = (Real)__ldg(&s.inv_single32[count]);  // (float)count * (float)(1 / pSingles)
     }
-    finish_single<Real>(s, d, src, orb, e);
+    finish_single<Real, NW>(s, d, src, orb, e);
     e.ok = true;
 }
 
 // Child determinant and H_ij of the double src0 < src1 -> {o0, o1}:
 // make_double (excit_parity.F90:78) pairs the sources with the sorted
 // targets, the parity counts the occupied orbitals each move passes.
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void finish_double(const DevSys &s, const unsigned long long *d, int src0, int src1, int o0, int o1,
                                      Excit<Real> &e) {
     const int ta = min(o0, o1), tb = max(o0, o1);
-    for (int w = 0; w < s.W; ++w) e.child[w] = d[w];
-    int np = occ_between(e.child, s.W, min(src0, ta), max(src0, ta));
+    NECI_FOR_WORDS(w, nwords<NW>(s)) e.child[w] = d[w];
+    int np = occ_between(e.child, nwords<NW>(s), min(src0, ta), max(src0, ta));
     flip_orb(e.child, src0);
     flip_orb(e.child, ta);
-    np += occ_between(e.child, s.W, min(src1, tb), max(src1, tb));
+    np += occ_between(e.child, nwords<NW>(s), min(src1, tb), max(src1, tb));
     flip_orb(e.child, src1);
     flip_orb(e.child, tb);
     const Real hel = sltcnd_2_r<Real>(s, src0, src1, ta, tb);
@@ -210,7 +222,7 @@ __device__ inline void tri_pair(int idx, int &a1, int &a2) {
 // with UNIF_UNIF particles = pick_biased_elecs
 // (excit_gens_int_weighted.F90:722-830).  Returns the full double pgen
 // (times pDoubles).
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 2;
     e.ok = false;
@@ -232,8 +244,8 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     qb += ((qb + 1) * s.nOccAlpha <= idx);
     const int ra = idx - qb * s.nOccAlpha;
     const unsigned long long spin_mask = alpha_pair ? kAlphaBits : kBetaBits;
-    const int o_a = nth_orbital(d, s.W, par ? spin_mask : kAlphaBits, par ? a2 : 1 + ra);
-    const int o_b = nth_orbital(d, s.W, par ? spin_mask : kBetaBits, par ? a1 : 1 + qb);
+    const int o_a = nth_orbital(d, nwords<NW>(s), par ? spin_mask : kAlphaBits, par ? a2 : 1 + ra);
+    const int o_b = nth_orbital(d, nwords<NW>(s), par ? spin_mask : kBetaBits, par ? a1 : 1 + qb);
     Real pgen = par ? (dbl ? (Real)s.pgen_par : (Real)s.f_pgen_par) : (dbl ? (Real)s.pgen_opp : (Real)s.f_pgen_opp);
     Real invp = par ? (dbl ? (Real)s.inv_par : (Real)s.f_inv_par) : (dbl ? (Real)s.inv_opp : (Real)s.f_inv_opp);
     // the exchange draw is taken for every pair and used for opposite spins
@@ -272,7 +284,7 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     // pholes > 1e-10 (pholes >= 0: compared on the bits in FP64)
     const bool small = dbl ? !(dbl_bits((double)pholes) > dbl_bits(1e-10)) : !(pholes > (Real)1e-10);
     if (o0 == 0 || o1 == 0 || orb_occ(d, o0) || orb_occ(d, o1) || small) { e.pgen = 0; return; }
-    finish_double<Real>(s, d, src0, src1, o0, o1, e);
+    finish_double<Real, NW>(s, d, src0, src1, o0, o1, e);
     pgen *= pholes;
     e.pgen = pgen * (dbl ? (Real)s.p_doubles : (Real)s.f_p_doubles);
     invp *= dbl ? (Real)__ldg(&s.alias_inv[base + ab - 1]) : (Real)__ldg(&s.alias_inv32[base + ab - 1]);
@@ -281,14 +293,15 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
 }
 
 // The c-th (1-based) unoccupied spin orbital among those of `pattern`, 0 if none.
+template <int NW = 0>
 __device__ inline int nth_unoccupied(const DevSys &s, const unsigned long long *d, unsigned long long pattern, int c) {
     unsigned long long u[kMaxWords];
-    for (int w = 0; w < s.W; ++w) {
+    NECI_FOR_WORDS(w, nwords<NW>(s)) {
         const int lo = 64 * w;
         const unsigned long long valid = s.nbasis >= lo + 64 ? ~0ull : (s.nbasis > lo ? (1ull << (s.nbasis - lo)) - 1 : 0ull);
         u[w] = ~d[w] & valid;
     }
-    return nth_orbital(u, s.W, pattern, c);
+    return nth_orbital(u, nwords<NW>(s), pattern, c);
 }
 
 // CreateDoubExcit (GenRandSymExcitNUMod.F90:155-205) without spatial
@@ -303,7 +316,7 @@ __device__ inline int nth_unoccupied(const DevSys &s, const unsigned long long *
 //                        taken from the host's table of the three cases.
 // NECI stops the run where a rejection loop exceeds its limit; here the
 // attempt produces no child.
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void gen_uniform_double(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
     e.ic = 2;
     e.cls = TC_DOUB;
@@ -316,8 +329,8 @@ __device__ inline void gen_uniform_double(const DevSys &s, const unsigned long l
     int K = (int)((sqrtf(8.0f * (float)X + 1.0f) - 1.0f) * 0.5f);
     while (K > 0 && K * (K + 1) / 2 > X) --K;
     while ((K + 1) * (K + 2) / 2 <= X) ++K;
-    const int src0 = nth_orbital(d, s.W, kAllBits, nel - 1 - K);
-    const int src1 = nth_orbital(d, s.W, kAllBits, nel - X + K * (K + 1) / 2);
+    const int src0 = nth_orbital(d, nwords<NW>(s), kAllBits, nel - 1 - K);
+    const int src1 = nth_orbital(d, nwords<NW>(s), kAllBits, nel - X + K * (K + 1) / 2);
     if (src0 == 0 || src1 == 0) return;
     const int ispn = beta(src0) != beta(src1) ? 2 : (beta(src0) ? 1 : 3);
     const int nua = s.nBI - s.nOccAlpha, nub = s.nBI - s.nOccBeta;
@@ -339,7 +352,7 @@ __device__ inline void gen_uniform_double(const DevSys &s, const unsigned long l
     if (na == forbidden) return;
     int orbA = 0;
     if (na - forbidden <= 3) {
-        orbA = nth_unoccupied(s, d, allowed, (int)uniform_index(rng, (unsigned)(na - forbidden)) + 1);
+        orbA = nth_unoccupied<NW>(s, d, allowed, (int)uniform_index(rng, (unsigned)(na - forbidden)) + 1);
     } else {
         const unsigned n_draw = ispn == 2 ? (unsigned)s.nbasis : (unsigned)s.nBI;
         bool found = false;
@@ -366,7 +379,7 @@ __device__ inline void gen_uniform_double(const DevSys &s, const unsigned long l
         if (!orb_occ(d, o) && o != orbA) { orbB = o; break; }
     }
     if (orbB == 0) return;
-    finish_double<Real>(s, d, src0, src1, orbA, orbB, e);
+    finish_double<Real, NW>(s, d, src0, src1, orbA, orbB, e);
     const bool dbl = sizeof(Real) == 8;
     e.pgen = dbl ? (Real)s.pgen_unif[ispn - 1] : (Real)s.f_pgen_unif[ispn - 1];
     e.invp = dbl ? (Real)s.inv_unif[ispn - 1] : (Real)s.f_inv_unif[ispn - 1];
@@ -374,21 +387,21 @@ __device__ inline void gen_uniform_double(const DevSys &s, const unsigned long l
 }
 
 // gen_exc_sd (excitation_generators.F90:110-133): singles with pSingles.
-template <typename Real>
+template <typename Real, int NW = 0>
 __device__ inline void generate_excitation(const DevSys &s, const unsigned long long *d, const int32_t *neigh,
                                            Stream &rng, Excit<Real> &e) {
     if (s.excitgen == NECI_EXGEN_RS_HUBBARD) {
-        gen_rs_hubbard<Real>(s, d, neigh, rng, e);
+        gen_rs_hubbard<Real, NW>(s, d, neigh, rng, e);
         return;
     }
     if (s.excitgen == NECI_EXGEN_UNIFORM) {
         // gen_rand_excit (GenRandSymExcitNUMod.F90:120-147): r < pDoubles -> double
-        if (rng.next64() < s.thr_doubles) gen_uniform_double<Real>(s, d, rng, e);
-        else gen_uniform_single<Real>(s, d, rng, e);
+        if (rng.next64() < s.thr_doubles) gen_uniform_double<Real, NW>(s, d, rng, e);
+        else gen_uniform_single<Real, NW>(s, d, rng, e);
         return;
     }
-    if (rng.next64() < s.thr_singles) gen_uniform_single<Real>(s, d, rng, e);
-    else gen_pchb_double<Real>(s, d, rng, e);
+    if (rng.next64() < s.thr_singles) gen_uniform_single<Real, NW>(s, d, rng, e);
+    else gen_pchb_double<Real, NW>(s, d, rng, e);
 }
 
 }  // namespace neci

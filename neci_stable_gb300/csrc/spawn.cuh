@@ -1,0 +1,315 @@
+// spawn.cuh -- the spawn attempts of a step (FciMCPar.F90:1600-1745,
+// loop_over_walkers): generate_excitation, attempt_create and
+// create_particle for every attempt entry the sweep wrote, one attempt per
+// thread per round.  Instantiated per precision of the amplitude (one
+// translation unit each: spawn_fp64.cu, spawn_fp32.cu), excitation generator
+// and number of determinant words.
+#pragma once
+
+#include "common.cuh"
+#include "excitgen.cuh"
+#include "internal.h"
+
+namespace neci {
+
+// ===========================================================================
+// k_spawn
+// ===========================================================================
+template <typename Real>
+__device__ inline Real prm(double d, float f) { return sizeof(Real) == 8 ? (Real)d : (Real)f; }
+
+// attempt_create_normal (fcimc_pointed_fns.F90:178-494) for one generated
+// excitation: the child amplitude -tau H_ij sign(C) / (p_gen AvMCExcits),
+// taken as -tau H_ij sign(C) (1/p_gen) (1/AvMCExcits) in precision Real and
+// converted to fixed point, then rounded there in integer arithmetic:
+// RealSpawnCutoff rounding (|n| < cutoff -> +-cutoff with probability
+// |n|/cutoff) or stochastic_round (lib/util_mod.fpp:182) to an integer
+// walker.  Returns 0 for no child.
+// In FP64 the product is formed as ((tau H_ij) (1/p_gen)) (1/AvMCExcits)
+// and its sign applied afterwards: multiplying by -1, by the walker sign and
+// by 1/AvMCExcits = 1 are exact, so the value is the reference order's, with
+// two multiplies where it has five; the scaling by 2^32 and the rounding to
+// an integer are done on the bits (fixed32_from_double).
+template <typename Real>
+__device__ inline long long spawn_amplitude(const IterParams &p, Real hel, Real invp, bool neg, Stream &rng, int &ovf,
+                                            unsigned long long &aq_out) {
+    long long q;
+    if (sizeof(Real) == 8) {
+        double v = (p.tau * (double)hel) * (double)invp;
+        if (!p.av_unit) v = v * p.inv_av;
+        int64_t qq;
+        if (!fixed32_from_double(v, qq)) { ovf = 1; return 0; }
+        q = neg ? qq : -qq;  // -tau H sign(C): positive for a negative parent
+    } else {
+        const Real ww = neg ? (Real)-1 : (Real)1;
+        const Real nsp = -prm<Real>(p.tau, p.f_tau) * hel * ww * invp * prm<Real>(p.inv_av, p.f_inv_av);
+        const float sc = (float)nsp * 4294967296.0f;
+        if (!(fabsf(sc) < 9.2e18f)) { ovf = 1; return 0; }
+        q = __float2ll_rn(sc);
+    }
+    const unsigned long long aq = (unsigned long long)(q < 0 ? -q : q);
+    aq_out = aq;
+    if (p.t_all_real_coeff) {
+        if (p.t_real_spawn_cutoff && aq < p.cutoff_q) {
+            // keep with probability |q| / cutoff_q
+            const bool keep = __umul64hi(rng.next64(), p.cutoff_q) < aq;
+            return keep ? (q < 0 ? -(long long)p.cutoff_q : (long long)p.cutoff_q) : 0ll;
+        }
+        return q;
+    }
+    const unsigned long long whole = aq >> 32, frac = aq & 0xFFFFFFFFull;
+    unsigned long long m = whole;
+    if (frac != 0 && (rng.next64() >> 32) < frac) m += 1;
+    const long long v = (long long)(m << 32);
+    return q < 0 ? -v : v;
+}
+
+// One spawn attempt's parent, unpacked from its 8-byte attempt entry
+// (slot | run << 32 | sign bit << 33 | attempt index << 34).
+struct Parent {
+    unsigned long long d[kMaxWords];
+    unsigned long long key;
+    unsigned int k;
+    int run;
+    bool neg, core, pinit;
+};
+// Words of a CurrentDets row (NIfD + 1): RW where the kernel is instantiated
+// for that count, else the system's W.
+template <int RW>
+__device__ inline int rwords(const DevSys &s) { return RW > 0 ? RW : s.W; }
+
+template <int NW, int RW>
+__device__ inline void load_parent(const DevSys &s, const DevState &st, const IterParams &p, unsigned long long w0,
+                                   Parent &P) {
+    const long long j = (long long)(w0 & 0xFFFFFFFFull);
+    P.run = (int)((w0 >> 32) & 1ull);
+    P.neg = (w0 >> 33) & 1ull;
+    P.k = (unsigned int)(w0 >> 34);
+    const long long *r = st.dets + j * s.R;
+    NECI_FOR_WORDS(w, nwords<NW>(s)) P.d[w] = (unsigned long long)r[w];
+    const long long flags = r[rwords<RW>(s) + s.L];
+    P.core = st.n_core > 0 && is_core_flags(flags);
+    P.pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(P.run));
+    P.key = det_key(P.d, rwords<RW>(s), p.seed, nwords<NW>(s));
+}
+
+// Block-local tau-search log of k_spawn: per TauClass the largest gamma (as
+// bits) and the logged count, capped near the reference's threshold.
+struct TauAcc {
+    unsigned long long g[4];
+    unsigned int c[4];
+};
+
+// log_spawn_magnitude (tau_search_conventional.F90:138-258): gamma =
+// |H_ij| / (p_gen / p_class) of one generated excitation, taken as
+// |H_ij| (1/p_gen) p_class in precision Real.  Singles and uniform doubles
+// count when gamma > 0, parallel and opposite-spin doubles always.
+template <typename Real>
+__device__ inline void tau_log(const DevSys &s, const Excit<Real> &e, TauAcc *acc) {
+    double g;
+    if (sizeof(Real) == 8) g = fabs((double)e.hel) * (double)e.invp * s.tau_fac[e.cls];
+    else g = (double)(fabsf((float)e.hel) * (float)e.invp * s.f_tau_fac[e.cls]);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(g);
+    if (b > acc->g[e.cls]) atomicMax(&acc->g[e.cls], b);
+    const bool counts = (e.cls == TC_PAR || e.cls == TC_OPP) || g > 0.0;
+    if (counts && acc->c[e.cls] <= kTauCntThreshold) atomicAdd(&acc->c[e.cls], 1u);
+}
+
+// attempt_create for a generated excitation: the core -> core filter
+// (is_core_state, semi_stoch_procs.F90:547; those spawns are done by the
+// deterministic projection), the tau-search log and the rounded fixed-point
+// amplitude.
+template <typename Real, int NW, int RW>
+__device__ inline long long attempt_create(const DevSys &s, const DevState &st, const IterParams &p, const Parent &P,
+                                           Excit<Real> &e, Stream &rng, const int32_t *sh_rh2, int &ovf,
+                                           TauAcc *tacc) {
+    if (!e.ok) return 0;
+    if (P.core) {
+        const long long hs = hash_find(st, e.child, nwords<NW>(s), s.R, neci_hash(e.child, nwords<NW>(s), sh_rh2), st.ctl);
+        if (hs >= 0 && is_core_flags(st.dets[hs * s.R + rwords<RW>(s) + s.L])) return 0;
+    }
+    if (s.tau_search) tau_log<Real>(s, e, tacc);
+    return spawn_amplitude<Real>(p, e.hel, e.invp, P.neg, rng, ovf, e.aq);
+}
+
+// The unbiasing weight of a spawn's parent for the 2-RDM (the role of
+// calc_rdmbiasfac, rdm_general.fpp:1039-1085, for a per-spawn estimator):
+// the expected number of non-zero spawns onto a child per attempt is
+// p_gen P(nz), where P(nz) is min(1, |n| / RealSpawnCutoff) with real
+// coefficients and the cutoff, min(1, |n|) with integer walkers, and 1
+// otherwise; the attempts number |C_i| AvMCExcits on average, so
+// sign(C_i) / (AvMCExcits p_gen P(nz)) has expectation C_i per child.
+// aq is |n| in fixed point before rounding.
+__device__ inline double rdm_parent_weight(const IterParams &p, double invp, unsigned long long aq, bool neg) {
+    double inv_pnz = 1.0;
+    if (p.t_all_real_coeff) {
+        if (p.t_real_spawn_cutoff && aq < p.cutoff_q) inv_pnz = (double)p.cutoff_q / (double)aq;
+    } else if (aq < (1ull << 32)) {
+        inv_pnz = 4294967296.0 / (double)aq;
+    }
+    const double w = (invp * p.inv_av) * inv_pnz;
+    return neg ? -w : w;
+}
+
+// create_particle (fcimc_helper.F90:152-308): append the record; warp-wide.
+template <typename Real, int NW, int RW>
+__device__ inline void create_particle(const DevSys &s, const DevState &st, const IterParams &p, long long qv,
+                                       const Parent &P, const Excit<Real> &e) {
+    const unsigned long long pos = warp_append(&st.ctl->n_spawned, qv != 0 ? 1u : 0u);
+    if (qv == 0) return;
+    if (pos >= (unsigned long long)st.max_spawned) {
+        set_err(st.ctl, NECI_GPU_ERR_SPAWN_FULL);
+        return;
+    }
+    long long *o = st.spawn + pos * s.R;
+    NECI_FOR_WORDS(w, rwords<RW>(s)) o[w] = w < nwords<NW>(s) ? (long long)e.child[w] : 0ll;
+    for (int k2 = 0; k2 < s.L; ++k2) o[rwords<RW>(s) + k2] = (k2 == P.run) ? qv : 0ll;
+    o[rwords<RW>(s) + s.L] = P.pinit ? (1ll << init_flag_bit(P.run)) : 0ll;
+    if (s.rdm) {
+        // the parent and its unbiased sign for the 2-RDM: sign(C_i) divided
+        // by the expected number of non-zero spawns onto this child per unit
+        // of |C_i|, AvMCExcits p_gen P(spawn != 0)
+        long long *par = st.spawn_par + pos * (rwords<RW>(s) + 1);
+        NECI_FOR_WORDS(w, rwords<RW>(s)) par[w] = w < nwords<NW>(s) ? (long long)P.d[w] : 0ll;
+        par[rwords<RW>(s)] = double_to_word(rdm_parent_weight(p, (double)e.invp, e.aq, P.neg));
+    }
+}
+
+// A single excitation parked in the block's queue: the attempt's stream is
+// rebuilt and its first draw (the singles/doubles choice) skipped, so the
+// draws are those of an inline single.
+template <typename Real, int NW, int RW>
+__device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
+                                           unsigned long long w0, const int32_t *sh_rh2, int &ovf, TauAcc *tacc) {
+    Parent P;
+    Excit<Real> e;
+    e.ok = false;
+    long long qv = 0;
+    P.run = 0;
+    P.pinit = false;
+    if (valid) {
+        load_parent<NW, RW>(s, st, p, w0, P);
+        Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
+        (void)rng.next64();
+        gen_uniform_single<Real, NW>(s, P.d, rng, e);
+        qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, tacc);
+    }
+    create_particle<Real, NW, RW>(s, st, p, qv, P, e);
+}
+
+// The spawn attempts (FciMCPar.F90:1600-1745, loop_over_walkers): one
+// attempt per thread per round; every lane runs the same number of rounds so
+// that the record append is warp-wide.  For molecular systems an attempt
+// that draws a single excitation is parked in a block-local queue; once the
+// queue holds a block's worth, every thread takes one (singles are rare and
+// long: run inline they would stall the doubles of their warp).
+//
+// NW is the number of words that can hold orbitals, ceil(nBasis/64), and RW
+// the row's W = nBasis/64 + 1 words (NIfD + 1): one more, always zero, when
+// nBasis is a multiple of 64.  Excitations are generated on NW words; the
+// determinant key, the records and the row offsets use all RW.  NW = RW = 0
+// is the instance for any size, with the counts read from the system.
+template <typename Real, int GEN, int NW, int RW>
+__global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp) {
+    if (halted(st)) return;
+    extern __shared__ int32_t sh[];
+    __shared__ unsigned long long sq[256];
+    __shared__ int sq_n;
+    __shared__ TauAcc tacc;
+    int32_t *sh_rh2 = sh;
+    int32_t *sh_neigh = sh + (s.nbasis + 1);
+    for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
+    if (GEN == NECI_EXGEN_RS_HUBBARD)
+        for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
+    if (threadIdx.x == 0) sq_n = 0;
+    if (threadIdx.x < 4) {
+        tacc.g[threadIdx.x] = 0ull;
+        tacc.c[threadIdx.x] = 0u;
+    }
+    __syncthreads();
+    const IterParams p = *pp;
+    const long long nat = (long long)min(st.ctl->n_att, (unsigned long long)st.max_att);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((nat + stride - 1) / stride) * stride;
+    const int nb = blockDim.x;  // 128: the queue holds at most two rounds
+    int ovf = 0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
+        long long qv = 0;
+        Parent P;
+        P.run = 0;
+        P.pinit = false;
+        Excit<Real> e;
+        e.ok = false;
+        if (q < nat) {
+            const unsigned long long w0 = st.att[q];
+            load_parent<NW, RW>(s, st, p, w0, P);
+            Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
+            if (GEN == NECI_EXGEN_RS_HUBBARD) {
+                gen_rs_hubbard<Real, NW>(s, P.d, sh_neigh, rng, e);
+            } else {
+                // gen_exc_sd: r < pSingles is a single; gen_rand_excit: r < pDoubles is a double
+                const unsigned long long r0 = rng.next64();
+                const bool single = GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles;
+                if (single) sq[atomicAdd(&sq_n, 1)] = w0;
+                else if (GEN == NECI_EXGEN_UNIFORM) gen_uniform_double<Real, NW>(s, P.d, rng, e);
+                else gen_pchb_double<Real, NW>(s, P.d, rng, e);
+            }
+            qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
+        }
+        create_particle<Real, NW, RW>(s, st, p, qv, P, e);
+        if (GEN != NECI_EXGEN_RS_HUBBARD) {
+            __syncthreads();
+            const int n = sq_n;
+            if (n >= nb) {
+                spawn_queued_single<Real, NW, RW>(s, st, p, true, sq[n - nb + threadIdx.x], sh_rh2, ovf, &tacc);
+                __syncthreads();
+                if (threadIdx.x == 0) sq_n = n - nb;
+                __syncthreads();
+            }
+        }
+    }
+    if (GEN != NECI_EXGEN_RS_HUBBARD) {
+        __syncthreads();
+        const int n = sq_n;
+        for (int b = 0; b < n; b += nb)
+            spawn_queued_single<Real, NW, RW>(s, st, p, b + (int)threadIdx.x < n, b + threadIdx.x < n ? sq[b + threadIdx.x] : 0ull,
+                                      sh_rh2, ovf, &tacc);
+    }
+    if (ovf) set_err(st.ctl, NECI_GPU_ERR_OVERFLOW);
+    if (s.tau_search) {
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            if (tacc.g[threadIdx.x]) atomicMax(&st.ctl->tau_gamma[threadIdx.x], tacc.g[threadIdx.x]);
+            if (tacc.c[threadIdx.x]) atomicAdd(&st.ctl->tau_cnt[threadIdx.x], (unsigned long long)tacc.c[threadIdx.x]);
+        }
+    }
+}
+
+// Grids are sized to the context's capacity (as in kernels.cu).
+inline int spawn_grid(const Engine &e, int threads) {
+    const long long want = e.st.max_spawned / (threads * 4) + 1, hi = e.num_sms * (threads == 128 ? 8 : 4);
+    return (int)(want < 8 ? 8 : (want > hi ? hi : want));
+}
+
+template <typename Real, int GEN>
+void launch_spawn_gen(Engine &e, cudaStream_t s, int grid, size_t shm) {
+    const int rw = e.sys.W, nw = (e.sys.nbasis + 63) / 64;
+    if (rw == 1) k_spawn<Real, GEN, 1, 1><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 2) k_spawn<Real, GEN, 2, 2><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 3) k_spawn<Real, GEN, 3, 3><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else k_spawn<Real, GEN, 0, 0><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+}
+
+// The spawn kernel for amplitudes in precision Real.
+template <typename Real>
+void launch_spawn_real(Engine &e, cudaStream_t s) {
+    const size_t shm = (size_t)(e.sys.nbasis + 1 + e.sys.nsites * e.sys.max_neigh) * sizeof(int32_t);
+    const int grid = spawn_grid(e, 128);
+    if (e.sys.excitgen == NECI_EXGEN_RS_HUBBARD) launch_spawn_gen<Real, NECI_EXGEN_RS_HUBBARD>(e, s, grid, shm);
+    else if (e.sys.excitgen == NECI_EXGEN_UNIFORM) launch_spawn_gen<Real, NECI_EXGEN_UNIFORM>(e, s, grid, shm);
+    else launch_spawn_gen<Real, NECI_EXGEN_PCHB>(e, s, grid, shm);
+}
+
+}  // namespace neci
