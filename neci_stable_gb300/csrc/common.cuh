@@ -36,8 +36,9 @@ __device__ inline void block_add(const double (&v)[NV], double *const (&dst)[NV]
     for (int m = 0; m < NV; ++m)
         if ((m & 1) < L) red[m][t] = v[m];
     __syncthreads();
-    for (int m = wid; m < NV; m += nw) {
-        if ((m & 1) >= L) continue;
+#pragma unroll
+    for (int m = 0; m < NV; ++m) {  // value m is summed by warp m mod nw
+        if (m % nw != wid || (m & 1) >= L) continue;
         double s = 0.0;
         for (int i = lane; i < (int)blockDim.x; i += 32) s += red[m][i];
         s = warp_sum(s);

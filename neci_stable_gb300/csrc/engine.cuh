@@ -18,6 +18,10 @@ namespace neci {
 constexpr int kMaxWords = 4;      // nBasis <= 255 (NIfD <= 3)
 // A loop over the words 0..W-1 of a determinant, unrolled over kMaxWords.
 #define NECI_FOR_WORDS(w, W) _Pragma("unroll") for (int w = 0; w < kMaxWords; ++w) if (w < (W))
+constexpr int kMaxRuns = 2;  // lenof_sign: one run or a replica pair
+// A loop over the runs 0..L-1, unrolled over kMaxRuns: per-run arrays
+// indexed by it stay in registers.
+#define NECI_FOR_RUNS(k, L) _Pragma("unroll") for (int k = 0; k < kMaxRuns; ++k) if (k < (L))
 constexpr int kMaxNel = 64;
 constexpr int kMaxNeigh = 8;
 constexpr int kBigAttempts = 32;  // parents with more attempts are expanded by k_expand
@@ -496,20 +500,41 @@ __device__ inline double sltcnd_2(const DevSys &s, int i, int j, int a, int b) {
     if (beta(i) == beta(b) && beta(j) == beta(a)) hel -= umat_el(s, spat(i), spat(j), spat(b), spat(a));
     return hel;
 }
-// sltcnd_0_base (sltcnd.fpp:585-622) + ECore, same summation order as NECI.
-__device__ inline double sltcnd_0(const DevSys &s, const uint8_t *nI, int nel) {
+// sltcnd_0_base (sltcnd.fpp:585-622), same summation order as NECI, taken
+// over the occupied bits in ascending order (nI order) instead of a decoded
+// nI array: the one-electron sum, then for each electron i the Coulomb sum
+// over j > i added to hel_doub, while the exchange terms of the same pairs,
+// in the same (i, j) order, go to their own sum.
+__device__ inline double sltcnd_0(const DevSys &s, const unsigned long long *d, int W) {
     double hel_sing = 0.0;
-    for (int i = 0; i < nel; ++i) hel_sing += tmat_el(s, nI[i], nI[i]);
-    double hel_doub = 0.0;
-    for (int i = 0; i < nel - 1; ++i) {
-        double t = 0.0;
-        for (int j = i + 1; j < nel; ++j) t += umat_el(s, spat(nI[i]), spat(nI[j]), spat(nI[i]), spat(nI[j]));
-        hel_doub += t;
+    NECI_FOR_WORDS(w, W) {
+        unsigned long long x = d[w];
+        while (x) {
+            const int o = w * 64 + __ffsll((long long)x);
+            x &= x - 1;
+            hel_sing += tmat_el(s, o, o);
+        }
     }
-    double hel_tmp = 0.0;
-    for (int i = 0; i < nel - 1; ++i)
-        for (int j = i + 1; j < nel; ++j)
-            if (beta(nI[i]) == beta(nI[j])) hel_tmp -= umat_el(s, spat(nI[i]), spat(nI[j]), spat(nI[j]), spat(nI[i]));
+    double hel_doub = 0.0, hel_tmp = 0.0;
+    NECI_FOR_WORDS(wi, W) {
+        unsigned long long xi = d[wi];
+        while (xi) {
+            const int oi = wi * 64 + __ffsll((long long)xi);
+            xi &= xi - 1;
+            double t = 0.0;
+            NECI_FOR_WORDS(wj, W) {
+                if (wj < wi) continue;
+                unsigned long long xj = wj == wi ? xi : d[wj];  // the electrons after i
+                while (xj) {
+                    const int oj = wj * 64 + __ffsll((long long)xj);
+                    xj &= xj - 1;
+                    t += umat_el(s, spat(oi), spat(oj), spat(oi), spat(oj));
+                    if (beta(oi) == beta(oj)) hel_tmp -= umat_el(s, spat(oi), spat(oj), spat(oj), spat(oi));
+                }
+            }
+            hel_doub += t;  // the last electron adds t = 0
+        }
+    }
     return hel_doub + hel_tmp + hel_sing;
 }
 
@@ -520,9 +545,7 @@ __device__ inline double diag_helement(const DevSys &s, const unsigned long long
         NECI_FOR_WORDS(w, s.W) n += __popcll(d[w] & (d[w] >> 1) & 0x5555555555555555ull);
         return s.uhub * n;
     }
-    uint8_t nI[kMaxNel];
-    const int nel = decode(d, s.W, nI);
-    return sltcnd_0(s, nI, nel) + s.ecore;
+    return sltcnd_0(s, d, s.W) + s.ecore;
 }
 
 // <D_a|H|D_b> for a != b, given the excitation level.

@@ -78,10 +78,10 @@ __global__ void k_hash_fill(DevSys s, DevState st) {
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
         const long long *r = st.dets + j * s.R;
         bool occ = is_core_flags(r[s.W + s.L]);
-        for (int k = 0; k < s.L; ++k) occ = occ || fabs(word_to_double(r[s.W + k])) >= kEps12;
+        NECI_FOR_RUNS(k, s.L) occ = occ || fabs(word_to_double(r[s.W + k])) >= kEps12;
         if (!occ) continue;
         unsigned long long d[kMaxWords];
-        for (int w = 0; w < s.W; ++w) d[w] = (unsigned long long)r[w];
+        NECI_FOR_WORDS(w, s.W) d[w] = (unsigned long long)r[w];
         hash_insert(st, j, neci_hash(d, s.W, sh_rh2), st.ctl);
     }
 }
@@ -97,7 +97,7 @@ __global__ void k_hash_fill(DevSys s, DevState st) {
 __device__ inline bool slot_kept(const DevSys &s, const DevState &st, long long j) {
     const long long *r = st.dets + j * s.R;
     if (st.n_core > 0 && is_core_flags(r[s.W + s.L])) return true;
-    for (int k = 0; k < s.L; ++k)
+    NECI_FOR_RUNS(k, s.L)
         if (abs_bits(word_to_double(r[s.W + k])) >= dbl_bits(kEps12)) return true;
     return false;
 }
@@ -225,7 +225,7 @@ __global__ void k_compact_done(DevState st) {
 // ===========================================================================
 // k_sweep
 // ===========================================================================
-__global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const IterParams *pp) {
+__global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
@@ -292,17 +292,17 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
         long long flags = 0;
         bool core = false, occ = false;
         if (live) {
-            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)sr[w];
-            for (int k = 0; k < L; ++k) C[k] = word_to_double(sr[W + k]);
+            NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)sr[w];
+            NECI_FOR_RUNS(k, L) C[k] = word_to_double(sr[W + k]);
             flags = sr[W + L];
             core = st.n_core > 0 && is_core_flags(flags);
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 acc_old[k] += fabs(C[k]);
                 if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
             }
             if (core) {
                 const int ci = st.core_of_slot[j];
-                for (int k = 0; k < L; ++k) st.core_x[(long long)ci * L + k] = C[k];
+                NECI_FOR_RUNS(k, L) st.core_x[(long long)ci * L + k] = C[k];
             }
         }
         // holes go to the free list (FciMCPar.F90:1415-1427)
@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             const bool is_ref = exl == 0;
             if (p.t_trunc_initiator) {
                 long long nf = flags;
-                for (int k = 0; k < L; ++k) {
+                NECI_FOR_RUNS(k, L) {
                     const int b = init_flag_bit(k);
                     const bool now = test_initiator(p, test_bit(flags, b), C[k], is_ref, core);
                     if (now) nf |= (1ll << b); else nf &= ~(1ll << b);
@@ -323,12 +323,12 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 if (nf != flags) { r[W + L] = nf; flags = nf; }
             }
             const double odh = soffd[threadIdx.x];
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 if (is_ref) acc_hf[k] += C[k];
                 acc_en[k] += odh * C[k];
             }
             const unsigned long long dkey = det_key(d, W, p.seed);
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 // decide_num_to_spawn (fcimc_helper.F90:2160-2174)
                 Stream rs(dkey, p.iter, P_NSPAWN, k, 0);
                 uint32_t whole;
@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
             const double Kii = sdiag[threadIdx.x];
             double cp[2] = {0.0, 0.0};
             bool any = false;
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 const double fac = p.tau * (Kii - p.diag_sft[k]);
                 if (s.tau_search) death_max = fmax(death_max, Kii - p.diag_sft[k]);  // log_death_magnitude
                 if (fac > 2.0) set_err(c, NECI_GPU_ERR_UNSTABLE);
@@ -376,13 +376,13 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
             }
             if (p.t_trunc_initiator && any) {
-                for (int k = 0; k < L; ++k)
+                NECI_FOR_RUNS(k, L)
                     if (is_positive(cp[k]) != is_positive(C[k])) { acc_ab[k] += fabs(cp[k]); cp[k] = 0.0; }
                 any = false;
-                for (int k = 0; k < L; ++k) if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
+                NECI_FOR_RUNS(k, L) if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
             }
             if (any || core) {
-                for (int k = 0; k < L; ++k) {
+                NECI_FOR_RUNS(k, L) {
                     r[W + k] = double_to_word(cp[k]);
                     out_zero = out_zero && abs_bits(cp[k]) == 0;
                 }
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
                 hash_remove(st, j);
                 ++acc_tomb;
                 r[W + L] = flags | 1ll;  // flag_removed
-                for (int k = 0; k < L; ++k) r[W + k] = double_to_word(0.0);
+                NECI_FOR_RUNS(k, L) r[W + k] = double_to_word(0.0);
             }
         }
         // the signs just written are all zero
@@ -406,14 +406,14 @@ __global__ void __launch_bounds__(256) k_sweep(DevSys s, DevState st, const Iter
         // entries with a whole block
         {
             unsigned int nat = 0;
-            for (int k = 0; k < L; ++k) nat += nsp[k];
+            NECI_FOR_RUNS(k, L) nat += nsp[k];
             const unsigned long long base = warp_append(&c->n_att, nat);
             if (nat) {
                 if (base + nat > (unsigned long long)st.max_att) {
                     set_err(c, NECI_GPU_ERR_SPAWN_FULL);
                 } else {
                     unsigned long long q = base;
-                    for (int k = 0; k < L; ++k) {
+                    NECI_FOR_RUNS(k, L) {
                         const unsigned long long head = (unsigned long long)j | ((unsigned long long)k << 32) |
                                                         ((unsigned long long)neg[k] << 33);
                         if (nsp[k] > (unsigned int)kHugeAttempts) {
@@ -502,7 +502,7 @@ __global__ void k_core(DevSys s, DevState st, const IterParams *pp) {
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
     for (long long i = warp; i < st.n_core; i += nwarps) {
         const long long e0 = st.core_rowptr[i], e1 = st.core_rowptr[i + 1];
-        for (int k = 0; k < L; ++k) {
+        NECI_FOR_RUNS(k, L) {
             double acc = 0.0;
             if (!mixed) {
                 for (long long e = e0 + lane; e < e1; e += 32)
@@ -542,9 +542,9 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
         if (i < n) {
             const long long *rec = st.spawn + i * R;
             unsigned long long d[kMaxWords];
-            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)rec[w];
+            NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
             long long q[2] = {0, 0};
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 q[k] = rec[W + k];
                 aq[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
             }
@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
             h = neci_hash(d, W, sh_rh2);
             const long long slot = hash_find(st, d, W, R, h, c);
             if (slot >= 0) {
-                for (int k = 0; k < L; ++k) {
+                NECI_FOR_RUNS(k, L) {
                     if (q[k] == 0) continue;
                     atomicAdd((unsigned long long *)&st.acc[slot * L + k], (unsigned long long)q[k]);
                     const uint32_t add = 1u;
@@ -591,7 +591,7 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
             const long long i = st.cand[ci];
             const long long *rec = st.spawn + i * R;
             unsigned long long d[kMaxWords];
-            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)rec[w];
+            NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
             unsigned long long b = splitmix64(st.cand_h[ci]) & mask;
             long long owner = -1;
             for (int p = 0; p < kProbeLimit; ++p) {
@@ -606,7 +606,7 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
             } else {
                 const long long fl = rec[W + L];
                 atomicAdd(&st.rep_cnt[owner * (L + 1) + L], 1u);  // records in the block
-                for (int k = 0; k < L; ++k) {
+                NECI_FOR_RUNS(k, L) {
                     const long long q = rec[W + k];
                     if (q == 0) continue;
                     atomicAdd((unsigned long long *)&st.rep_q[owner * L + k], (unsigned long long)q);
@@ -626,7 +626,7 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
 // ===========================================================================
 // Annihilation pass 3: unique new determinants -> CurrentDets.
 // ===========================================================================
-__global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const IterParams *pp) {
+__global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
@@ -648,10 +648,10 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
             const long long i = st.cand[ci];
             const long long *rec = st.spawn + i * R;
             unsigned long long d[kMaxWords];
-            for (int w = 0; w < W; ++w) d[w] = (unsigned long long)rec[w];
+            NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
             long long q[2] = {0, 0};
             uint32_t cnt[2] = {0, 0};
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 q[k] = st.rep_q[ci * L + k];
                 cnt[k] = st.rep_cnt[ci * (L + 1) + k];
                 st.rep_q[ci * L + k] = 0;
@@ -666,26 +666,26 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
             } else {
                 flags = 0;
                 if (p.t_trunc_initiator)
-                    for (int k = 0; k < L; ++k) {
+                    NECI_FOR_RUNS(k, L) {
                         const bool coh = p.t_init_coherent_rule && (cnt[k] & 0x7FFFFFFFu) >= 2u;
                         if (coh || (cnt[k] & 0x80000000u)) flags |= 1ll << init_flag_bit(k);
                     }
             }
             bool zero = true;
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 if (q[k] != 0) zero = false;
                 a_s[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
             }
             if (!zero) {
                 double ss[2] = {from_fixed(q[0]), from_fixed(q[1])};
                 if (p.t_trunc_initiator)
-                    for (int k = 0; k < L; ++k)
+                    NECI_FOR_RUNS(k, L)
                         if (!test_bit(flags, init_flag_bit(k))) { a_ab[k] += fabs(ss[k]); ss[k] = 0.0; }
                 bool unocc = true;
-                for (int k = 0; k < L; ++k) if (fabs(ss[k]) >= kEps12) unocc = false;
+                NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) unocc = false;
                 if (!unocc) {
                     const unsigned long long dkey = det_key(d, W, p.seed);
-                    for (int k = 0; k < L; ++k) {
+                    NECI_FOR_RUNS(k, L) {
                         // stochRoundSpawn (Annihilation.F90:1354-1418)
                         const double a = fabs(ss[k]);
                         if (a > kEps12 && a < p.occupied_thresh) {
@@ -696,12 +696,12 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
                         }
                     }
                     unocc = true;
-                    for (int k = 0; k < L; ++k) if (fabs(ss[k]) >= kEps12) unocc = false;
+                    NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) unocc = false;
                 }
                 if (!unocc) {
                     // AddNewHashDet (load_balancer.fpp:514-629): a slot below
                     want = true;
-                    for (int w = 0; w < W; ++w) wd[w] = d[w];
+                    NECI_FOR_WORDS(w, W) wd[w] = d[w];
                     ws[0] = ss[0];
                     ws[1] = ss[1];
                     wflags = flags;
@@ -737,8 +737,8 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
                     set_err(c, NECI_GPU_ERR_LIST_FULL);
                 } else {
                     long long *o = st.dets + slot * R;
-                    for (int w = 0; w < W; ++w) o[w] = (long long)wd[w];
-                    for (int k = 0; k < L; ++k) o[W + k] = double_to_word(ws[k]);
+                    NECI_FOR_WORDS(w, W) o[w] = (long long)wd[w];
+                    NECI_FOR_RUNS(k, L) o[W + k] = double_to_word(ws[k]);
                     o[W + L] = wflags & ~1ll;
                     st.diagH[slot] = diag_helement(s, wd) - s.hii;
                     const int ic = excit_level(s.ilut_ref, wd, W);
@@ -765,7 +765,7 @@ __global__ void __launch_bounds__(128) k_ann_insert(DevSys s, DevState st, const
 // k_merge_stats: deterministic annihilation, found-branch merge and
 // CalcHashTableStats in one sweep.
 // ===========================================================================
-__global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core) {
+__global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
@@ -804,12 +804,12 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         const long long flags = sr[W + L];
         const bool core = st.n_core > 0 && is_core_flags(flags);
         double C[2] = {0.0, 0.0};
-        for (int k = 0; k < L; ++k) C[k] = word_to_double(sr[W + k]);
+        NECI_FOR_RUNS(k, L) C[k] = word_to_double(sr[W + k]);
         bool changed = false;
         // deterministic_annihilation (Annihilation.F90:930-963)
         if (core && with_core) {
             const int ci = st.core_of_slot[j];
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 const double y = st.core_y[(long long)ci * L + k];
                 a_born[k] += fabs(y);
                 if (prod_negative(C[k], y)) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(y));
@@ -820,21 +820,21 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         // AnnihilateSpawnedParts, found branch (Annihilation.F90:1000-1140)
         uint32_t m[2] = {0, 0};
         bool has = false;
-        for (int k = 0; k < L; ++k) {
+        NECI_FOR_RUNS(k, L) {
             m[k] = sm[k];
             if (m[k]) has = true;
         }
         if (has) {
             ++a_found;
             double S[2] = {0.0, 0.0};
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 const long long q = st.acc[j * L + k];
                 st.acc[j * L + k] = 0;
                 st.meta[j * L + k] = 0;
                 a_s[k] += (unsigned long long)(q < 0 ? -q : q);
                 S[k] = from_fixed(q);
             }
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 if (abs_bits(C[k]) < dbl_bits(kEps12) && p.t_trunc_initiator) {
                     const bool sp_init = (m[k] & 0x80000000u) ||
                                          (p.t_init_coherent_rule && (m[k] & 0x7FFFFFFFu) >= 2u);
@@ -842,11 +842,11 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                 }
                 if (prod_negative(C[k], S[k])) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(S[k]));
             }
-            for (int k = 0; k < L; ++k) C[k] = S[k] + C[k];
+            NECI_FOR_RUNS(k, L) C[k] = S[k] + C[k];
             changed = true;
             if (!core) {
                 bool unocc = true;
-                for (int k = 0; k < L; ++k) if (abs_bits(C[k]) >= dbl_bits(kEps12)) unocc = false;
+                NECI_FOR_RUNS(k, L) if (abs_bits(C[k]) >= dbl_bits(kEps12)) unocc = false;
                 if (unocc) {
                     hash_remove(st, j);
                     ++a_tomb;
@@ -856,25 +856,25 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         }
         // CalcHashTableStats (load_balancer.fpp:646-806)
         bool occ = false;
-        for (int k = 0; k < L; ++k) if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
+        NECI_FOR_RUNS(k, L) if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
         if (!occ && !core) {
-            if (changed) for (int k = 0; k < L; ++k) r[W + k] = double_to_word(C[k]);
+            if (changed) NECI_FOR_RUNS(k, L) r[W + k] = double_to_word(C[k]);
             ++a_holes;
             return;
         }
         if (!core) {
-            for (int k = 0; k < L; ++k) {
+            NECI_FOR_RUNS(k, L) {
                 const double a = fabs(C[k]);
                 if (abs_bits(a) > dbl_bits(kEps12) && abs_bits(a) < dbl_bits(p.occupied_thresh)) {
                     unsigned long long d[kMaxWords];
-                    for (int w = 0; w < W; ++w) d[w] = (unsigned long long)sr[w];
+                    NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)sr[w];
                     Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
                     const double pRemove = (p.occupied_thresh - a) / p.occupied_thresh;
                     if (bern(rng, pRemove)) {
                         a_rm[k] += a;
                         C[k] = 0.0;
                         bool unocc = true;
-                        for (int k2 = 0; k2 < L; ++k2) if (abs_bits(C[k2]) >= dbl_bits(kEps12)) unocc = false;
+                        NECI_FOR_RUNS(k2, L) if (abs_bits(C[k2]) >= dbl_bits(kEps12)) unocc = false;
                         if (unocc) {
                             hash_remove(st, j);
                             ++a_tomb;
@@ -888,9 +888,9 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
                 }
             }
         }
-        if (changed) for (int k = 0; k < L; ++k) r[W + k] = double_to_word(C[k]);
+        if (changed) NECI_FOR_RUNS(k, L) r[W + k] = double_to_word(C[k]);
         occ = false;
-        for (int k = 0; k < L; ++k) {
+        NECI_FOR_RUNS(k, L) {
             a_tp[k] += fabs(C[k]);
             a_norm[k] += C[k] * C[k];
             if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
@@ -898,8 +898,8 @@ __global__ void __launch_bounds__(256) k_merge_stats(DevSys s, DevState st, cons
         if (occ || core) {
             ++a_occ;
             bool is_ref = true;
-            for (int w = 0; w < W; ++w) if ((unsigned long long)sr[w] != s.ilut_ref[w]) is_ref = false;
-            if (is_ref) for (int k = 0; k < L; ++k) c->noat_hf[k] = C[k];
+            NECI_FOR_WORDS(w, W) if ((unsigned long long)sr[w] != s.ilut_ref[w]) is_ref = false;
+            if (is_ref) NECI_FOR_RUNS(k, L) c->noat_hf[k] = C[k];
         } else {
             ++a_holes;
         }
@@ -961,7 +961,7 @@ __device__ inline long long rdm_pair(int p, int q) { return (long long)(q - 1) *
 __device__ inline void rdm_add_pair(const DevSys &s, const DevState &st, const unsigned long long *par,
                                     const unsigned long long *chi, double c) {
     int src[2] = {0, 0}, tgt[2] = {0, 0}, ns = 0, nt = 0;
-    for (int w = 0; w < s.W; ++w) {
+    NECI_FOR_WORDS(w, s.W) {
         unsigned long long x = par[w] & ~chi[w], y = chi[w] & ~par[w];
         while (x) { if (ns < 2) src[ns] = w * 64 + __ffsll((long long)x); ++ns; x &= x - 1; }
         while (y) { if (nt < 2) tgt[nt] = w * 64 + __ffsll((long long)y); ++nt; y &= y - 1; }
@@ -971,7 +971,7 @@ __device__ inline void rdm_add_pair(const DevSys &s, const DevState &st, const u
         const int i = src[0], a = tgt[0];
         const bool par_odd = occ_between(par, s.W, min(i, a), max(i, a)) & 1;
         const double full = par_odd ? -c : c;
-        for (int w = 0; w < s.W; ++w) {
+        NECI_FOR_WORDS(w, s.W) {
             unsigned long long x = par[w];
             while (x) {
                 const int k = w * 64 + __ffsll((long long)x);
@@ -987,7 +987,7 @@ __device__ inline void rdm_add_pair(const DevSys &s, const DevState &st, const u
     }
     // the parity of i -> a then j -> b (sorted pairing), as successive singles
     unsigned long long t[kMaxWords];
-    for (int w = 0; w < s.W; ++w) t[w] = par[w];
+    NECI_FOR_WORDS(w, s.W) t[w] = par[w];
     int np = occ_between(t, s.W, min(src[0], tgt[0]), max(src[0], tgt[0]));
     flip_orb(t, src[0]);
     flip_orb(t, tgt[0]);
@@ -1008,7 +1008,7 @@ __global__ void __launch_bounds__(256) k_rdm_offdiag(DevSys s, DevState st) {
         const double w = word_to_double(par[W]);
         const int run = rec[W] != 0 ? 0 : 1;
         unsigned long long d[kMaxWords], pd[kMaxWords];
-        for (int k = 0; k < W; ++k) {
+        NECI_FOR_WORDS(k, W) {
             d[k] = (unsigned long long)rec[k];
             pd[k] = (unsigned long long)par[k];
         }
@@ -1037,7 +1037,7 @@ __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use
         if (prod == 0.0) continue;
         uint8_t nI[kMaxNel];
         unsigned long long d[kMaxWords];
-        for (int w = 0; w < s.W; ++w) d[w] = (unsigned long long)r[w];
+        NECI_FOR_WORDS(w, s.W) d[w] = (unsigned long long)r[w];
         const int nel = decode(d, s.W, nI);
         for (int a = 1; a < nel; ++a)
             for (int b = 0; b < a; ++b) {
