@@ -109,4 +109,34 @@ NECI_HD bool fixed32_from_double(double x, int64_t &q) {
     return true;
 }
 
+// prob_thresh(p) = floor(p 2^64) as a 64-bit threshold (0 for p <= 0 or
+// NaN, all ones for p >= 1), from the bits of p: the product by 2^64 is
+// exact, so for p = m 2^(E-1075) in (0, 1) it is m shifted by E - 1011
+// (at most 11 places left) and truncated.  Subnormal p give 0.
+NECI_HD uint64_t prob_thresh_bits(double p) {
+    const uint64_t b = dbl_bits(p);
+    if ((b >> 63) || b == 0) return 0ull;
+    if (b >= 0x3FF0000000000000ull) return b > 0x7FF0000000000000ull ? 0ull : ~0ull;
+    const int E = (int)(b >> 52);
+    if (E == 0) return 0ull;
+    const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = E - 1011;
+    return sh >= 0 ? m << sh : (sh > -64 ? m >> -sh : 0ull);
+}
+
+// a <= b for finite a and b >= 0 (b not -0.0 unless a is negative or zero):
+// a negative or -0.0 is below any b >= 0; non-negative doubles order like
+// their bit patterns.
+NECI_HD bool le_nonneg(double a, double b) {
+    const uint64_t x = dbl_bits(a);
+    return (x >> 63) || x <= dbl_bits(b);
+}
+
+// a > b for b > 0 finite: a positive and above b in bit order (NaN with the
+// sign bit clear counts as above).
+NECI_HD bool gt_pos(double a, double b) {
+    const uint64_t x = dbl_bits(a);
+    return !(x >> 63) && x > dbl_bits(b);
+}
+
 }  // namespace neci

@@ -270,15 +270,15 @@ struct Stream {
 };
 
 // Probability p as a 64-bit threshold: draw r < thresh(p)  <=>  r/2^64 < p.
-__host__ __device__ inline unsigned long long prob_thresh(double p) {
-    if (!(p > 0.0)) return 0ull;
-    if (p >= 1.0) return ~0ull;
-    return (unsigned long long)(p * 18446744073709551616.0);
-}
-// Bernoulli(p) from one draw (p >= 1 is always true).
+// (unsigned long long)(p * 2^64) for 0 < p < 1, 0 for p <= 0, all ones for
+// p >= 1; taken on the bits of p (prob_thresh_bits), no FP64 instructions.
+__host__ __device__ inline unsigned long long prob_thresh(double p) { return prob_thresh_bits(p); }
+// Bernoulli(p) from one draw (p >= 1 is always true: the threshold is all
+// ones only then).
 __device__ inline bool bern(Stream &r, double p) {
     const unsigned long long x = r.next64();
-    return p >= 1.0 || x < prob_thresh(p);
+    const unsigned long long t = prob_thresh_bits(p);
+    return t == ~0ull || x < t;
 }
 // Bernoulli(p) for a float p from the top 32 bits of one draw.
 __device__ inline bool bern_f(Stream &r, float p) {

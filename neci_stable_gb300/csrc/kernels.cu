@@ -225,12 +225,15 @@ __global__ void k_compact_done(DevState st) {
 // ===========================================================================
 // k_sweep
 // ===========================================================================
+// LR: lenof_sign of the instance (1, or 2 for a replica pair).
+template <int LR>
 __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
     const long long n = slots_in_use(st);
-    const int W = s.W, L = s.L, R = s.R;
+    const int W = s.W, R = s.R;
+    constexpr int L = LR;
     double acc_old[2] = {0.0, 0.0}, acc_hf[2] = {0.0, 0.0}, acc_en[2] = {0.0, 0.0};
     double acc_died[2] = {0.0, 0.0}, acc_born[2] = {0.0, 0.0}, acc_ab[2] = {0.0, 0.0};
     double death_max = 0.0;  // max_death_cpt of this thread's determinants (tau search)
@@ -322,10 +325,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                 }
                 if (nf != flags) { r[W + L] = nf; flags = nf; }
             }
+            // offdiagH is zero beyond the double excitations of the
+            // reference; adding that +-0 product changes no sum, so it is
+            // skipped (GB300 runs FP64 at 1/64 of the FP32 rate)
             const double odh = soffd[threadIdx.x];
+            const bool has_odh = abs_bits(odh) != 0;
             NECI_FOR_RUNS(k, L) {
                 if (is_ref) acc_hf[k] += C[k];
-                acc_en[k] += odh * C[k];
+                if (has_odh) acc_en[k] += odh * C[k];
             }
             const unsigned long long dkey = det_key(d, W, p.seed);
             NECI_FOR_RUNS(k, L) {
@@ -358,7 +365,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
             NECI_FOR_RUNS(k, L) {
                 const double fac = p.tau * (Kii - p.diag_sft[k]);
                 if (s.tau_search) death_max = fmax(death_max, Kii - p.diag_sft[k]);  // log_death_magnitude
-                if (fac > 2.0) set_err(c, NECI_GPU_ERR_UNSTABLE);
+                if (gt_pos(fac, 2.0)) set_err(c, NECI_GPU_ERR_UNSTABLE);
                 double idie;
                 if (p.t_all_real_coeff) {
                     idie = fac * fabs(C[k]);
@@ -368,8 +375,15 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                     rat -= idie;
                     if (bern(rd, fabs(rat))) idie += nearbyint(fsign(1.0, rat));
                 }
-                acc_died[k] += fmin(idie, fabs(C[k]));
-                acc_born[k] += fmax(idie - fabs(C[k]), 0.0);
+                // fmin(idie, |C|) to the died and fmax(idie - |C|, 0) to the
+                // born, with the compare in integers (a zero added to the
+                // born changes nothing)
+                if (le_nonneg(idie, fabs(C[k]))) {
+                    acc_died[k] += idie;
+                } else {
+                    acc_died[k] += fabs(C[k]);
+                    acc_born[k] += idie - fabs(C[k]);
+                }
                 // C - idie * sign(1, C) with Fortran's sign (+1 for C = -0.0); both products are exact
                 const bool nonneg = !(dbl_bits(C[k]) >> 63) || abs_bits(C[k]) == 0;
                 cp[k] = C[k] - (nonneg ? idie : -idie);
@@ -526,13 +540,16 @@ __global__ void k_core(DevSys s, DevState st, const IterParams *pp) {
 // ===========================================================================
 // Annihilation pass 1: probe the walker hash with every spawn record.
 // ===========================================================================
+// LR: lenof_sign of the instance (1, or 2 for a replica pair).
+template <int LR>
 __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
     if (halted(st)) return;
     extern __shared__ int32_t sh_rh2[];
     load_rh2(s, sh_rh2);
     Control *c = st.ctl;
     const long long n = (long long)min(c->n_spawned, (unsigned long long)st.max_spawned);
-    const int W = s.W, L = s.L, R = s.R;
+    const int W = s.W, R = s.R;
+    constexpr int L = LR;
     unsigned long long aq[2] = {0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
@@ -576,11 +593,14 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
 // ===========================================================================
 // Annihilation pass 2: merge candidates per determinant.
 // ===========================================================================
+// LR: lenof_sign of the instance (1, or 2 for a replica pair).
+template <int LR>
 __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
     if (halted(st)) return;
     Control *c = st.ctl;
     const long long n = (long long)c->n_cand;
-    const int W = s.W, L = s.L, R = s.R;
+    const int W = s.W, R = s.R;
+    constexpr int L = LR;
     const unsigned long long mask = st.spawn_hash_n - 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
@@ -626,12 +646,15 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
 // ===========================================================================
 // Annihilation pass 3: unique new determinants -> CurrentDets.
 // ===========================================================================
+// LR: lenof_sign of the instance (1, or 2 for a replica pair).
+template <int LR>
 __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
     const long long n = (long long)c->n_reps;
-    const int W = s.W, L = s.L, R = s.R;
+    const int W = s.W, R = s.R;
+    constexpr int L = LR;
     double a_ab[2] = {0, 0}, a_rm[2] = {0, 0}, a_born[2] = {0, 0};
     unsigned long long a_s[2] = {0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -690,7 +713,8 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                         const double a = fabs(ss[k]);
                         if (a > kEps12 && a < p.occupied_thresh) {
                             Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
-                            const double pRemove = 1.0 - a / p.occupied_thresh;
+                            const double pRemove =
+                                1.0 - (dbl_bits(p.occupied_thresh) == dbl_bits(1.0) ? a : a / p.occupied_thresh);
                             if (bern(rng, pRemove)) { a_rm[k] += a; ss[k] = 0.0; }
                             else { a_born[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
                         }
@@ -755,7 +779,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
     double v[6] = {a_ab[0], a_ab[1], a_rm[0], a_rm[1], a_born[0], a_born[1]};
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                             &c->nborn[0], &c->nborn[1]};
-    block_add<6>(v, dst, s.L);
+    block_add<6>(v, dst, L);
     unsigned long long u[3] = {a_s[0], a_s[1], (unsigned long long)a_tomb};  // two's complement for -count
     unsigned long long *const du[3] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb};
     block_add_u<3>(u, du);
@@ -765,12 +789,15 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
 // k_merge_stats: deterministic annihilation, found-branch merge and
 // CalcHashTableStats in one sweep.
 // ===========================================================================
+// LR: lenof_sign of the instance (1, or 2 for a replica pair).
+template <int LR>
 __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
     const long long n = (long long)min(c->tot_walkers, (unsigned long long)st.max_walkers);
-    const int W = s.W, L = s.L, R = s.R;
+    const int W = s.W, R = s.R;
+    constexpr int L = LR;
     double a_born[2] = {0, 0}, a_ann[2] = {0, 0}, a_ab[2] = {0, 0}, a_rm[2] = {0, 0};
     double a_tp[2] = {0, 0}, a_norm[2] = {0, 0};
     unsigned long long a_s[2] = {0, 0}, a_occ = 0, a_holes = 0, a_found = 0, a_tomb = 0;
@@ -869,7 +896,10 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
                     unsigned long long d[kMaxWords];
                     NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)sr[w];
                     Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
-                    const double pRemove = (p.occupied_thresh - a) / p.occupied_thresh;
+                    // (T - a) / T; a division by T = 1 (the default) is exact and skipped
+                    const double pRemove = dbl_bits(p.occupied_thresh) == dbl_bits(1.0)
+                                               ? 1.0 - a
+                                               : (p.occupied_thresh - a) / p.occupied_thresh;
                     if (bern(rng, pRemove)) {
                         a_rm[k] += a;
                         C[k] = 0.0;
@@ -1148,30 +1178,41 @@ int configure_kernels(Engine &e) {
     const int rmax = kMaxWords + 2 + 1;
     const int sweep_max = 2 * kStageTile * (rmax + 2) * 8;
     const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 4);
-    if (cudaFuncSetAttribute(k_sweep, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess) return 1;
-    if (cudaFuncSetAttribute(k_merge_stats, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(k_sweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(k_merge_stats<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
+        return 1;
+    if (cudaFuncSetAttribute(k_merge_stats<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
         return 1;
     return 0;
 }
 
 void launch_sweep(Engine &e, cudaStream_t s) {
-    k_sweep<<<grid_for(e, 256), kStageTile, sweep_smem_bytes(e), s>>>(e.sys, e.st, e.d_params);
+    if (e.sys.L == 2) k_sweep<2><<<grid_for(e, 256), kStageTile, sweep_smem_bytes(e), s>>>(e.sys, e.st, e.d_params);
+    else k_sweep<1><<<grid_for(e, 256), kStageTile, sweep_smem_bytes(e), s>>>(e.sys, e.st, e.d_params);
 }
 void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256), 256, 0, s>>>(e.st); }
 void launch_core(Engine &e, cudaStream_t s) {
     if (e.st.n_core > 0) k_core<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_ann_probe(Engine &e, cudaStream_t s) {
-    k_ann_probe<<<grid_spawns(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
+    const size_t shm = (e.sys.nbasis + 1) * sizeof(int32_t);
+    if (e.sys.L == 2) k_ann_probe<2><<<grid_spawns(e, 256), 256, shm, s>>>(e.sys, e.st);
+    else k_ann_probe<1><<<grid_spawns(e, 256), 256, shm, s>>>(e.sys, e.st);
 }
 void launch_ann_compress(Engine &e, cudaStream_t s) {
-    k_ann_compress<<<grid_spawns(e, 256), 256, 0, s>>>(e.sys, e.st);
+    if (e.sys.L == 2) k_ann_compress<2><<<grid_spawns(e, 256), 256, 0, s>>>(e.sys, e.st);
+    else k_ann_compress<1><<<grid_spawns(e, 256), 256, 0, s>>>(e.sys, e.st);
 }
 void launch_ann_insert(Engine &e, cudaStream_t s) {
-    k_ann_insert<<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
+    if (e.sys.L == 2) k_ann_insert<2><<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
+    else k_ann_insert<1><<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
-    k_merge_stats<<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core);
+    if (e.sys.L == 2)
+        k_merge_stats<2><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core);
+    else
+        k_merge_stats<1><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core);
 }
 void launch_rdm(Engine &e, cudaStream_t s) {
     if (!e.sys.rdm) return;

@@ -1,5 +1,6 @@
 """The bit-level helpers of csrc/bitsplit.h return what the FP64 expressions
-they replace return (decide_num_to_spawn's split, threshold tests on |C|),
+they replace return (decide_num_to_spawn's split, threshold tests on |C|,
+the Bernoulli threshold floor(p 2^64) and the compares of the death step),
 for random signs over many magnitudes and for the edge cases: integers,
 values just above and below integers and 1e-12, signed zeros, tiny and
 subnormal values, and the 2^31 limit."""
@@ -43,6 +44,15 @@ static int check(double c) {
     if ((c > 0.0) != is_positive(c)) return 1;
     const double bs[] = {1.0, -1.0, -2.3283064365386963e-10, 5e-300, -5e-300, 0.0, -0.0, -4.9e-324, 1e300, -7.5};
     for (double b : bs) if ((c * b < 0.0) != prod_negative(c, b)) return 1;
+    // Bernoulli thresholds (bern) and the compares of the death step
+    for (double pp : {c, std::fabs(c), std::fabs(c) - std::floor(std::fabs(c)), 1.0 - std::fabs(c), c * 1e-3,
+                      std::fabs(c) * 0.5})
+        if (prob_thresh_bits(pp) != prob_thresh(pp)) return 1;
+    for (double b : {std::fabs(c), 0.0, 1.0, 0.5, 3.0, 1e-300})
+        for (double a : {c, -c, c * 0.999, c * 1.001, 0.0, -0.0})
+            if ((a <= b) != le_nonneg(a, b)) return 1;
+    for (double y : {2.0, 1.0, 1e-12})
+        if ((c > y) != gt_pos(c, y)) return 1;
     // the spawn amplitude's fixed point: llrint(c 2^32) and its overflow rule
     for (double x : {c, c * 2.3283064365386963e-10, c * 1e-9, c * 3.0e9}) {
         const double sc = x * 4294967296.0;
@@ -81,6 +91,7 @@ int main() {
         if (!std::isfinite(c)) {
             int64_t q;
             if (fixed32_from_double(c, q)) ++bad;
+            if (prob_thresh_bits(c) != prob_thresh(c) || prob_thresh_bits(-c) != prob_thresh(-c)) ++bad;
             continue;
         }
         const int b = check(c);
