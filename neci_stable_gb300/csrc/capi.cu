@@ -130,7 +130,8 @@ void drop_graphs(Engine &e) {
 int ensure_graph(Engine &e) {
     const bool core = e.st.n_core > 0;
     const int k = e.h_params->precision == NECI_PREC_MIXED ? 1 : 0;
-    if (e.graphs[k] && e.graph_core[k] != core) {
+    const bool fast = sweep_fast(*e.h_params);
+    if (e.graphs[k] && (e.graph_core[k] != core || e.graph_fast[k] != fast)) {
         cudaGraphExecDestroy(e.graphs[k]);
         e.graphs[k] = nullptr;
     }
@@ -142,6 +143,7 @@ int ensure_graph(Engine &e) {
         CK(cudaGraphInstantiate(&e.graphs[k], g, 0));
         cudaGraphDestroy(g);
         e.graph_core[k] = core;
+        e.graph_fast[k] = fast;
     }
     e.graph = e.graphs[k];
     return NECI_GPU_OK;

@@ -197,6 +197,10 @@ struct IterParams {
     int av_unit;                  // AvMCExcits == 1: the spawn count is split in integers
 };
 
+// The sweep's fast instance serves steps with real coefficients and
+// AvMCExcits = 1, the instance for any parameters the others.
+__host__ __device__ inline bool sweep_fast(const IterParams &p) { return p.t_all_real_coeff && p.av_unit; }
+
 // ---------------------------------------------------------------------------
 // Philox-4x32-10 (Salmon et al., SC11) and the per-determinant stream.
 // ---------------------------------------------------------------------------
@@ -267,6 +271,13 @@ struct Stream {
     }
     // genrand_real2 equivalent: a double in [0, 1) from 53 bits
     __device__ inline double next() { return (double)(next64() >> 11) * 0x1.0p-53; }
+    // The state after the stream's first draw, given its second draw (the
+    // rest of the first Philox block): the next draw returns `second`.
+    __device__ inline void resume_second(unsigned long long second) {
+        ctr[1] = 1;
+        buf[1] = second;
+        have = 1;
+    }
 };
 
 // Probability p as a 64-bit threshold: draw r < thresh(p)  <=>  r/2^64 < p.
@@ -303,7 +314,14 @@ __device__ inline long long to_fixed(double x, int *overflow) {
 __device__ inline double from_fixed(long long q) { return __ll2double_rn(q) * 0x1.0p-32; }
 __device__ inline double word_to_double(long long w) { return __longlong_as_double(w); }
 __device__ inline long long double_to_word(double d) { return __double_as_longlong(d); }
-__device__ inline double fsign(double a, double b) { return b >= 0.0 ? fabs(a) : -fabs(a); }
+// |x| and -x on the high word, in integer instructions: materialised as FP64
+// operations they would take a slot of GB300's 1/64-rate FP64 pipe each.
+__device__ inline double abs_dbl(double x) { return __hiloint2double(__double2hiint(x) & 0x7FFFFFFF, __double2loint(x)); }
+__device__ inline double neg_dbl(double x) {
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
+// Fortran sign(a, b): |a| for b >= 0 (and for b = -0.0), else -|a|.
+__device__ inline double fsign(double a, double b) { return is_negative(b) ? neg_dbl(abs_dbl(a)) : abs_dbl(a); }
 
 __device__ inline int init_flag_bit(int run) { return run == 0 ? NECI_FLAG_INITIATOR_1 : NECI_FLAG_INITIATOR_2; }
 __device__ inline bool test_bit(long long f, int b) { return ((unsigned long long)f >> b) & 1ull; }

@@ -48,6 +48,7 @@ struct Engine {
     // ensure_graph selected for the current parameters
     cudaGraphExec_t graphs[2] = {nullptr, nullptr};
     bool graph_core[2] = {false, false};
+    bool graph_fast[2] = {false, false};  // the sweep variant a graph was captured with
     cudaGraphExec_t graph = nullptr;
     // profiling
     bool profiling = false;

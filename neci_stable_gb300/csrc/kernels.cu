@@ -225,8 +225,68 @@ __global__ void k_compact_done(DevState st) {
 // ===========================================================================
 // k_sweep
 // ===========================================================================
-// LR: lenof_sign of the instance (1, or 2 for a replica pair).
-template <int LR>
+// a / b (IEEE round-to-nearest) as one inline PTX instruction, which the
+// compiler does not hoist out of its branch: a division written beside a
+// cheap alternative would otherwise be computed for every slot (it expands
+// to a long FP64 sequence).
+__device__ inline double div_dbl(double a, double b) {
+    double r;
+    asm("div.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+
+// The rare end of walker_death for one run, idie > |C| (more died than
+// there were): fmax(idie - |C|, 0) to the born count and, for an initiator
+// run whose determinant survives, the abort of the sign change
+// (fcimc_helper.F90:2352-2363).  Out of line (and so never executed
+// speculatively) with the accumulators passed through.
+struct DeathOver {
+    double born, ab, cp;
+};
+__device__ __noinline__ DeathOver death_over(double c, double idie, double cp, double born, double ab, bool abort_ok) {
+    const double aC = fabs(c);
+    if (!le_nonneg(idie, aC)) born += idie - aC;
+    if (abort_ok && is_positive(cp) != is_positive(c)) {
+        ab += fabs(cp);
+        cp = 0.0;
+    }
+    return {born, ab, cp};
+}
+
+// decide_num_to_spawn (fcimc_helper.F90:2160-2174) in FP64, for AvMCExcits
+// != 1 or |C| >= 2^31: the run's spawn-stream draw decides the extra attempt.
+// Out of line, so that the fast sweep does not carry its FP64 instructions.
+__device__ __noinline__ unsigned int spawn_count_fp64(double c, double av, unsigned long long dkey, long long iter,
+                                                      int run) {
+    Stream rs(dkey, iter, P_NSPAWN, run, 0);
+    const double pa = c * av;
+    unsigned int ns = abs((int)pa);
+    if (fabs(fabs(pa) - (double)ns) > kEps12) {
+        const double pe = fabs(pa) - (double)ns;
+        if (bern(rs, pe)) ++ns;
+    }
+    return ns;
+}
+
+// attempt_die_normal with integer walkers (fcimc_pointed_fns.F90:573-705):
+// fac |C| rounded stochastically with the determinant's death stream, whose
+// draws are taken one per run in run order.  Out of line as above.
+__device__ __noinline__ double death_integer(double fac, double c, unsigned long long dkey, long long iter, int run) {
+    Stream rd(dkey, iter, P_DEATH, 0, 0);
+    for (int k = 0; k < run; ++k) (void)rd.next64();
+    double rat = fac * fabs(c);
+    double idie = trunc(rat);
+    rat -= idie;
+    if (bern(rd, fabs(rat))) idie += nearbyint(fsign(1.0, rat));
+    return idie;
+}
+
+// LR: lenof_sign of the instance (1, or 2 for a replica pair).  FAST: the
+// instance for real coefficients with AvMCExcits = 1 (sweep_fast).  GB300
+// issues FP64 instructions at 1/64 of the FP32 rate and a predicated one
+// holds the pipe like an executed one, so the FP64 instructions of paths a
+// warp rarely takes sit behind branches (warp votes) or out of line.
+template <int LR, bool FAST>
 __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const IterParams p = *pp;
@@ -327,73 +387,72 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
             }
             // offdiagH is zero beyond the double excitations of the
             // reference; adding that +-0 product changes no sum, so it is
-            // skipped (GB300 runs FP64 at 1/64 of the FP32 rate)
+            // skipped
             const double odh = soffd[threadIdx.x];
             const bool has_odh = abs_bits(odh) != 0;
-            NECI_FOR_RUNS(k, L) {
-                if (is_ref) acc_hf[k] += C[k];
-                if (has_odh) acc_en[k] += odh * C[k];
-            }
+            NECI_FOR_RUNS(k, L) if (has_odh) acc_en[k] += odh * C[k];
+            if (__any_sync(__activemask(), is_ref))
+                if (is_ref) NECI_FOR_RUNS(k, L) acc_hf[k] += C[k];
             const unsigned long long dkey = det_key(d, W, p.seed);
             NECI_FOR_RUNS(k, L) {
                 // decide_num_to_spawn (fcimc_helper.F90:2160-2174)
-                Stream rs(dkey, p.iter, P_NSPAWN, k, 0);
                 uint32_t whole;
                 bool extra;
                 uint64_t thr;
                 unsigned int ns;
-                if (p.av_unit && split_count(C[k], whole, extra, thr)) {
+                if ((FAST || p.av_unit) && split_count(C[k], whole, extra, thr)) {
+                    Stream rs(dkey, p.iter, P_NSPAWN, k, 0);
                     ns = whole + (extra && rs.next64() < thr);
                 } else {
-                    const double pa = C[k] * p.av_mc_excits;
-                    ns = abs((int)pa);
-                    if (fabs(fabs(pa) - (double)ns) > kEps12) {
-                        const double pe = fabs(pa) - (double)ns;
-                        if (bern(rs, pe)) ++ns;
-                    }
+                    ns = spawn_count_fp64(C[k], p.av_mc_excits, dkey, p.iter, k);
                 }
                 nsp[k] = ns;
-                neg[k] = C[k] < 0.0;
+                neg[k] = is_negative(C[k]);
                 acc_att += ns;
             }
             // walker_death + attempt_die_normal (fcimc_helper.F90:2279-2407,
             // fcimc_pointed_fns.F90:573-705)
-            Stream rd(dkey, p.iter, P_DEATH, 0, 0);
             const double Kii = sdiag[threadIdx.x];
-            double cp[2] = {0.0, 0.0};
-            bool any = false;
+            double cp[2] = {0.0, 0.0}, id[2] = {0.0, 0.0};
+            bool any = false, over = false;
             NECI_FOR_RUNS(k, L) {
-                const double fac = p.tau * (Kii - p.diag_sft[k]);
-                if (s.tau_search) death_max = fmax(death_max, Kii - p.diag_sft[k]);  // log_death_magnitude
+                const double kd = Kii - p.diag_sft[k];
+                const double fac = p.tau * kd;
+                // log_death_magnitude: the largest K_ii - S >= 0 (non-negative
+                // doubles order like their bit patterns)
+                if (s.tau_search && !(dbl_bits(kd) >> 63) && dbl_bits(kd) > dbl_bits(death_max)) death_max = kd;
                 if (gt_pos(fac, 2.0)) set_err(c, NECI_GPU_ERR_UNSTABLE);
                 double idie;
-                if (p.t_all_real_coeff) {
-                    idie = fac * fabs(C[k]);
-                } else {
-                    double rat = fac * fabs(C[k]);
-                    idie = trunc(rat);
-                    rat -= idie;
-                    if (bern(rd, fabs(rat))) idie += nearbyint(fsign(1.0, rat));
-                }
-                // fmin(idie, |C|) to the died and fmax(idie - |C|, 0) to the
-                // born, with the compare in integers (a zero added to the
-                // born changes nothing)
-                if (le_nonneg(idie, fabs(C[k]))) {
-                    acc_died[k] += idie;
-                } else {
-                    acc_died[k] += fabs(C[k]);
-                    acc_born[k] += idie - fabs(C[k]);
-                }
+                if (FAST || p.t_all_real_coeff) idie = fac * fabs(C[k]);
+                else idie = death_integer(fac, C[k], dkey, p.iter, k);
+                id[k] = idie;
+                // fmin(idie, |C|) to the died; idie > |C| (more died than
+                // there were) is handled below
+                const double aC = abs_dbl(C[k]);
+                const bool le = le_nonneg(idie, aC);
+                acc_died[k] += le ? idie : aC;
+                if (!le) over = true;
                 // C - idie * sign(1, C) with Fortran's sign (+1 for C = -0.0); both products are exact
                 const bool nonneg = !(dbl_bits(C[k]) >> 63) || abs_bits(C[k]) == 0;
-                cp[k] = C[k] - (nonneg ? idie : -idie);
+                cp[k] = C[k] + (nonneg ? neg_dbl(idie) : idie);  // a - b is a + (-b), exactly
                 if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
             }
-            if (p.t_trunc_initiator && any) {
-                NECI_FOR_RUNS(k, L)
-                    if (is_positive(cp[k]) != is_positive(C[k])) { acc_ab[k] += fabs(cp[k]); cp[k] = 0.0; }
-                any = false;
-                NECI_FOR_RUNS(k, L) if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
+            // idie > |C| in a run: fmax(idie - |C|, 0) to the born, and the
+            // sign change it makes is aborted for initiator runs; the sign
+            // changes only then (at idie = |C| the new sign is +0 and the
+            // abort changes nothing)
+            if (over) {
+                const bool abort_ok = p.t_trunc_initiator && any;
+                NECI_FOR_RUNS(k, L) {
+                    const DeathOver o = death_over(C[k], id[k], cp[k], acc_born[k], acc_ab[k], abort_ok);
+                    acc_born[k] = o.born;
+                    acc_ab[k] = o.ab;
+                    cp[k] = o.cp;
+                }
+                if (abort_ok) {
+                    any = false;
+                    NECI_FOR_RUNS(k, L) if (abs_bits(cp[k]) > dbl_bits(kEps12)) any = true;
+                }
             }
             if (any || core) {
                 NECI_FOR_RUNS(k, L) {
@@ -714,7 +773,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                         if (a > kEps12 && a < p.occupied_thresh) {
                             Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
                             const double pRemove =
-                                1.0 - (dbl_bits(p.occupied_thresh) == dbl_bits(1.0) ? a : a / p.occupied_thresh);
+                                1.0 - (dbl_bits(p.occupied_thresh) == dbl_bits(1.0) ? a : div_dbl(a, p.occupied_thresh));
                             if (bern(rng, pRemove)) { a_rm[k] += a; ss[k] = 0.0; }
                             else { a_born[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
                         }
@@ -897,9 +956,9 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
                     NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)sr[w];
                     Stream rng(det_key(d, W, p.seed), p.iter, P_STATS_ROUND, k, 0);
                     // (T - a) / T; a division by T = 1 (the default) is exact and skipped
-                    const double pRemove = dbl_bits(p.occupied_thresh) == dbl_bits(1.0)
-                                               ? 1.0 - a
-                                               : (p.occupied_thresh - a) / p.occupied_thresh;
+                    const double tma = p.occupied_thresh - a;
+                    const double pRemove =
+                        dbl_bits(p.occupied_thresh) == dbl_bits(1.0) ? tma : div_dbl(tma, p.occupied_thresh);
                     if (bern(rng, pRemove)) {
                         a_rm[k] += a;
                         C[k] = 0.0;
@@ -911,7 +970,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
                             r[W + L] = flags | 1ll;
                         }
                     } else {
-                        a_born[k] += p.occupied_thresh - a;
+                        a_born[k] += tma;
                         C[k] = fsign(p.occupied_thresh, C[k]);
                     }
                     changed = true;
@@ -1178,8 +1237,11 @@ int configure_kernels(Engine &e) {
     const int rmax = kMaxWords + 2 + 1;
     const int sweep_max = 2 * kStageTile * (rmax + 2) * 8;
     const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 4);
-    if (cudaFuncSetAttribute(k_sweep<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess) return 1;
-    if (cudaFuncSetAttribute(k_sweep<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess) return 1;
+    if (cudaFuncSetAttribute(k_sweep<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
+        cudaFuncSetAttribute(k_sweep<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
+        cudaFuncSetAttribute(k_sweep<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
+        cudaFuncSetAttribute(k_sweep<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess)
+        return 1;
     if (cudaFuncSetAttribute(k_merge_stats<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
         return 1;
     if (cudaFuncSetAttribute(k_merge_stats<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
@@ -1188,8 +1250,16 @@ int configure_kernels(Engine &e) {
 }
 
 void launch_sweep(Engine &e, cudaStream_t s) {
-    if (e.sys.L == 2) k_sweep<2><<<grid_for(e, 256), kStageTile, sweep_smem_bytes(e), s>>>(e.sys, e.st, e.d_params);
-    else k_sweep<1><<<grid_for(e, 256), kStageTile, sweep_smem_bytes(e), s>>>(e.sys, e.st, e.d_params);
+    const int grid = grid_for(e, 256);
+    const size_t shm = sweep_smem_bytes(e);
+    const bool fast = sweep_fast(*e.h_params);
+    if (e.sys.L == 2) {
+        if (fast) k_sweep<2, true><<<grid, kStageTile, shm, s>>>(e.sys, e.st, e.d_params);
+        else k_sweep<2, false><<<grid, kStageTile, shm, s>>>(e.sys, e.st, e.d_params);
+    } else {
+        if (fast) k_sweep<1, true><<<grid, kStageTile, shm, s>>>(e.sys, e.st, e.d_params);
+        else k_sweep<1, false><<<grid, kStageTile, shm, s>>>(e.sys, e.st, e.d_params);
+    }
 }
 void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256), 256, 0, s>>>(e.st); }
 void launch_core(Engine &e, cudaStream_t s) {

@@ -175,105 +175,254 @@ __device__ inline void create_particle(const DevSys &s, const DevState &st, cons
     }
 }
 
-// A single excitation parked in the block's queue: the attempt's stream is
-// rebuilt and its first draw (the singles/doubles choice) skipped, so the
-// draws are those of an inline single.
-template <typename Real, int NW, int RW>
-__device__ inline void spawn_queued_single(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
-                                           unsigned long long w0, const int32_t *sh_rh2, int &ovf, TauAcc *tacc) {
-    Parent P;
+// One attempt of class CLS (0: double, 1: single) whose parent and stream
+// are loaded: the stream stands after its first draw (the singles/doubles
+// choice), so the draws are those of the attempt processed inline.
+template <typename Real, int GEN, int CLS, int NW, int RW>
+__device__ inline void spawn_class(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
+                                   const Parent &P, Stream &rng, const int32_t *sh_rh2, int &ovf, TauAcc *tacc) {
     Excit<Real> e;
     e.ok = false;
     long long qv = 0;
-    P.run = 0;
-    P.pinit = false;
     if (valid) {
-        load_parent<NW, RW>(s, st, p, w0, P);
-        Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
-        (void)rng.next64();
-        gen_uniform_single<Real, NW>(s, P.d, rng, e);
+        if (CLS == 1) gen_uniform_single<Real, NW>(s, P.d, rng, e);
+        else if (GEN == NECI_EXGEN_UNIFORM) gen_uniform_double<Real, NW>(s, P.d, rng, e);
+        else gen_pchb_double<Real, NW>(s, P.d, rng, e);
         qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, tacc);
     }
     create_particle<Real, NW, RW>(s, st, p, qv, P, e);
 }
 
-// The spawn attempts (FciMCPar.F90:1600-1745, loop_over_walkers): one
-// attempt per thread per round; every lane runs the same number of rounds so
-// that the record append is warp-wide.  For molecular systems an attempt
-// that draws a single excitation is parked in a block-local queue; once the
-// queue holds a block's worth, every thread takes one (singles are rare and
-// long: run inline they would stall the doubles of their warp).
+// The parent and stream of a queued attempt: the stream resumes after its
+// first draw from the saved second draw.
+template <int NW, int RW>
+__device__ inline Stream load_queued(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
+                                     unsigned long long w0, unsigned long long r1, Parent &P) {
+    P.run = 0;
+    P.pinit = false;
+    P.key = 0;
+    P.k = 0;
+    if (valid) load_parent<NW, RW>(s, st, p, w0, P);
+    Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
+    rng.resume_second(r1);
+    return rng;
+}
+
+// The spawn attempts (FciMCPar.F90:1600-1745, loop_over_walkers), one
+// attempt entry per thread per round; every lane runs the same number of
+// rounds, so the record append is warp-wide.  Molecular systems queue their
+// attempts by class (single or double) in shared memory and process full
+// batches with all lanes: with QD (both classes common, chosen by the host
+// from pSingles) both classes are queued; without it the doubles are
+// generated at once and only the singles are queued.  Lattice systems
+// (singles only) generate every attempt at once.
 //
 // NW is the number of words that can hold orbitals, ceil(nBasis/64), and RW
 // the row's W = nBasis/64 + 1 words (NIfD + 1): one more, always zero, when
 // nBasis is a multiple of 64.  Excitations are generated on NW words; the
 // determinant key, the records and the row offsets use all RW.  NW = RW = 0
 // is the instance for any size, with the counts read from the system.
-template <typename Real, int GEN, int NW, int RW>
+template <typename Real, int GEN, int NW, int RW, bool QD>
 __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     extern __shared__ int32_t sh[];
-    __shared__ unsigned long long sq[256];
-    __shared__ int sq_n;
+    // per class: attempt entries and their second draws (at most two
+    // rounds' worth are held), and each warp's appends of the round (by
+    // round parity)
+    __shared__ unsigned long long sq[2][256], sr1[2][256];
+    __shared__ int wcnt[2][2][4];
+    __shared__ unsigned int ring_tail;
     __shared__ TauAcc tacc;
     int32_t *sh_rh2 = sh;
     int32_t *sh_neigh = sh + (s.nbasis + 1);
     for (int i = threadIdx.x; i <= s.nbasis; i += blockDim.x) sh_rh2[i] = s.random_hash2[i];
     if (GEN == NECI_EXGEN_RS_HUBBARD)
         for (int i = threadIdx.x; i < s.nsites * s.max_neigh; i += blockDim.x) sh_neigh[i] = s.neighbours[i];
-    if (threadIdx.x == 0) sq_n = 0;
     if (threadIdx.x < 4) {
         tacc.g[threadIdx.x] = 0ull;
         tacc.c[threadIdx.x] = 0u;
     }
+    if (threadIdx.x == 0) ring_tail = 0u;
     __syncthreads();
     const IterParams p = *pp;
     const long long nat = (long long)min(st.ctl->n_att, (unsigned long long)st.max_att);
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((nat + stride - 1) / stride) * stride;
-    const int nb = blockDim.x;  // 128: the queue holds at most two rounds
+    const int nb = blockDim.x;  // 128: four warps
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int qn[2] = {0, 0};  // queue lengths, the same in every thread
     int ovf = 0;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
-        long long qv = 0;
-        Parent P;
-        P.run = 0;
-        P.pinit = false;
-        Excit<Real> e;
-        e.ok = false;
-        if (q < nat) {
-            const unsigned long long w0 = st.att[q];
-            load_parent<NW, RW>(s, st, p, w0, P);
-            Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
-            if (GEN == NECI_EXGEN_RS_HUBBARD) {
+    if (GEN == NECI_EXGEN_RS_HUBBARD) {
+        // lattice systems (singles only): one attempt per thread per round
+        for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
+            long long qv = 0;
+            Parent P;
+            P.run = 0;
+            P.pinit = false;
+            Excit<Real> e;
+            e.ok = false;
+            if (q < nat) {
+                load_parent<NW, RW>(s, st, p, st.att[q], P);
+                Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
                 gen_rs_hubbard<Real, NW>(s, P.d, sh_neigh, rng, e);
-            } else {
-                // gen_exc_sd: r < pSingles is a single; gen_rand_excit: r < pDoubles is a double
-                const unsigned long long r0 = rng.next64();
-                const bool single = GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles;
-                if (single) sq[atomicAdd(&sq_n, 1)] = w0;
-                else if (GEN == NECI_EXGEN_UNIFORM) gen_uniform_double<Real, NW>(s, P.d, rng, e);
-                else gen_pchb_double<Real, NW>(s, P.d, rng, e);
+                qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
             }
-            qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
+            create_particle<Real, NW, RW>(s, st, p, qv, P, e);
         }
-        create_particle<Real, NW, RW>(s, st, p, qv, P, e);
-        if (GEN != NECI_EXGEN_RS_HUBBARD) {
-            __syncthreads();
-            const int n = sq_n;
-            if (n >= nb) {
-                spawn_queued_single<Real, NW, RW>(s, st, p, true, sq[n - nb + threadIdx.x], sh_rh2, ovf, &tacc);
-                __syncthreads();
-                if (threadIdx.x == 0) sq_n = n - nb;
-                __syncthreads();
+    }
+    // Molecular systems without QD (singles rare or dominant): a round
+    // classifies one attempt per thread (gen_exc_sd: r < pSingles is a
+    // single; gen_rand_excit: r < pDoubles is a double), generates a double
+    // at once, inline, and appends a single to a ring of 512 entries.  The
+    // ring's tail only grows (shared atomics); the round's barrier is a
+    // __syncthreads_count, which gives every thread the round's appends, so
+    // the queue length and head are kept in registers, the same in every
+    // thread.  A full batch (or after the last attempt what is left) is read
+    // at once and processed: the next round's appends land at least 128 and
+    // less than 512 entries past the head, never on an entry being read.
+    if (GEN != NECI_EXGEN_RS_HUBBARD && !QD) {
+        unsigned long long *ring = &sq[0][0], *ring_r1 = &sr1[0][0];  // 512 entries each
+        unsigned int head = 0;
+        int cnt = 0;
+        long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        for (;; q += stride) {
+            const bool more = q - threadIdx.x < nround;  // the same in the whole block
+            if (!more && cnt == 0) break;
+            bool single = false;
+            unsigned long long w0 = 0, r1 = 0;
+            if (more) {
+                Parent P;
+                P.run = 0;
+                P.pinit = false;
+                Excit<Real> e;
+                e.ok = false;
+                long long qv = 0;
+                if (q < nat) {
+                    w0 = st.att[q];
+                    load_parent<NW, RW>(s, st, p, w0, P);
+                    Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
+                    const unsigned long long r0 = rng.next64();
+                    single = GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles;
+                    if (single) {
+                        r1 = rng.next64();
+                    } else {
+                        if (GEN == NECI_EXGEN_UNIFORM) gen_uniform_double<Real, NW>(s, P.d, rng, e);
+                        else gen_pchb_double<Real, NW>(s, P.d, rng, e);
+                        qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
+                    }
+                }
+                create_particle<Real, NW, RW>(s, st, p, qv, P, e);
+            }
+            if (single) {
+                const unsigned int t = atomicAdd(&ring_tail, 1u) & 511u;
+                ring[t] = w0;
+                ring_r1[t] = r1;
+            }
+            cnt += __syncthreads_count(single);
+            const int take = cnt >= nb ? nb : (more ? 0 : cnt);
+            if (take) {
+                const bool v = (int)threadIdx.x < take;
+                const unsigned int i = (head + threadIdx.x) & 511u;
+                const unsigned long long a = v ? ring[i] : 0ull, b = v ? ring_r1[i] : 0ull;
+                head += (unsigned int)take;
+                cnt -= take;
+                Parent P;
+                Stream rng = load_queued<NW, RW>(s, st, p, v, a, b, P);
+                spawn_class<Real, GEN, 1, NW, RW>(s, st, p, v, P, rng, sh_rh2, ovf, &tacc);
             }
         }
     }
-    if (GEN != NECI_EXGEN_RS_HUBBARD) {
-        __syncthreads();
-        const int n = sq_n;
-        for (int b = 0; b < n; b += nb)
-            spawn_queued_single<Real, NW, RW>(s, st, p, b + (int)threadIdx.x < n, b + threadIdx.x < n ? sq[b + threadIdx.x] : 0ull,
-                                      sh_rh2, ovf, &tacc);
+    // Molecular systems with QD (both classes common): a round classifies
+    // one attempt per thread and queues it by class; full batches of a queue
+    // are processed with all lanes, so neither class idles the lanes of the
+    // other (half of them after the tau search raises pSingles near 1/2).
+    // In the rounds after the last attempt the queues are emptied.  Each
+    // class is processed by one call site, so its generator is compiled once.
+    //
+    // Queue appends: each warp posts its counts per class; after one barrier
+    // every thread derives the same queue lengths and its own slot, so no
+    // shared counter is read and written in the same round.  A round that
+    // drains takes a second barrier (its entries visible) and reads its
+    // entries at once; the next round writes only after its own first
+    // barrier, by which time every thread has read them.
+    if (GEN != NECI_EXGEN_RS_HUBBARD && QD) {
+        long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        for (int round = 0;; ++round, q += stride) {
+            const bool more = q - threadIdx.x < nround;  // the same in the whole block
+            if (!more && qn[0] == 0 && qn[1] == 0) break;
+            const bool valid = more && q < nat;
+            int cls = 0;
+            unsigned long long w0 = 0, r1 = 0;
+            {
+                Parent P;
+                if (valid) {
+                    w0 = st.att[q];
+                    load_parent<NW, RW>(s, st, p, w0, P);
+                    Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
+                    const unsigned long long r0 = rng.next64();
+                    r1 = rng.next64();
+                    cls = (GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles) ? 1 : 0;
+                }
+            }
+            const bool queued = valid;
+            unsigned int m[2];
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                m[c] = __ballot_sync(0xffffffffu, queued && cls == c);
+                if (lane == 0) wcnt[round & 1][c][wid] = __popc(m[c]);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                int before = 0, total = 0;
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    const int x = wcnt[round & 1][c][w];
+                    before += w < wid ? x : 0;
+                    total += x;
+                }
+                if (queued && cls == c) {
+                    const int pos = qn[c] + before + __popc(m[c] & ((1u << lane) - 1u));
+                    sq[c][pos] = w0;
+                    sr1[c][pos] = r1;
+                }
+                qn[c] += total;
+            }
+            // a full batch, or after the last attempt what is left
+            const int t0 = qn[0] >= nb ? nb : (more ? 0 : qn[0]);
+            const int t1 = qn[1] >= nb ? nb : (more ? 0 : qn[1]);
+            if (t0 || t1) {
+                __syncthreads();
+                bool v0 = false, v1 = false;
+                unsigned long long a0 = 0, b0 = 0, a1 = 0, b1 = 0;
+                if (t0) {
+                    qn[0] -= t0;
+                    v0 = (int)threadIdx.x < t0;
+                    if (v0) {
+                        a0 = sq[0][qn[0] + threadIdx.x];
+                        b0 = sr1[0][qn[0] + threadIdx.x];
+                    }
+                }
+                if (t1) {
+                    qn[1] -= t1;
+                    v1 = (int)threadIdx.x < t1;
+                    if (v1) {
+                        a1 = sq[1][qn[1] + threadIdx.x];
+                        b1 = sr1[1][qn[1] + threadIdx.x];
+                    }
+                }
+                if (t0) {
+                    Parent P;
+                    Stream rng = load_queued<NW, RW>(s, st, p, v0, a0, b0, P);
+                    spawn_class<Real, GEN, 0, NW, RW>(s, st, p, v0, P, rng, sh_rh2, ovf, &tacc);
+                }
+                if (t1) {
+                    Parent P;
+                    Stream rng = load_queued<NW, RW>(s, st, p, v1, a1, b1, P);
+                    spawn_class<Real, GEN, 1, NW, RW>(s, st, p, v1, P, rng, sh_rh2, ovf, &tacc);
+                }
+            }
+        }
     }
     if (ovf) set_err(st.ctl, NECI_GPU_ERR_OVERFLOW);
     if (s.tau_search) {
@@ -291,15 +440,29 @@ inline int spawn_grid(const Engine &e, int threads) {
     return (int)(want < 8 ? 8 : (want > hi ? hi : want));
 }
 
+// Doubles are queued like singles when both classes are common: the
+// fraction of singles between 0.15 and 0.85 (on GB300, at 0.53 queueing
+// both made the spawn kernel 17% faster; with rare singles it is slower).
+inline int spawn_queue_doubles(const DevSys &s) {
+    const double ps = s.excitgen == NECI_EXGEN_UNIFORM ? 1.0 - s.p_doubles : s.p_singles;
+    return ps >= 0.15 && ps <= 0.85 ? 1 : 0;
+}
+
+template <typename Real, int GEN, bool QD>
+void launch_spawn_words(Engine &e, cudaStream_t s, int grid, size_t shm) {
+    const int rw = e.sys.W, nw = (e.sys.nbasis + 63) / 64;
+    if (rw == 1) k_spawn<Real, GEN, 1, 1, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 2) k_spawn<Real, GEN, 2, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else if (rw == 3) k_spawn<Real, GEN, 3, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    else k_spawn<Real, GEN, 0, 0, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+}
+
 template <typename Real, int GEN>
 void launch_spawn_gen(Engine &e, cudaStream_t s, int grid, size_t shm) {
-    const int rw = e.sys.W, nw = (e.sys.nbasis + 63) / 64;
-    if (rw == 1) k_spawn<Real, GEN, 1, 1><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 2) k_spawn<Real, GEN, 2, 2><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 3) k_spawn<Real, GEN, 3, 3><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else k_spawn<Real, GEN, 0, 0><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    if (GEN != NECI_EXGEN_RS_HUBBARD && spawn_queue_doubles(e.sys)) launch_spawn_words<Real, GEN, true>(e, s, grid, shm);
+    else launch_spawn_words<Real, GEN, false>(e, s, grid, shm);
 }
 
 // The spawn kernel for amplitudes in precision Real.
