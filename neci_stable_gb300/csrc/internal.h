@@ -34,6 +34,9 @@ struct Engine {
     DevState st{};
     int device = 0;
     int num_sms = 152;
+    // resident blocks per SM of the grid-stride spawn-list kernels (their
+    // grids fill the GPU once; the latency-bound hash passes want every warp)
+    int occ_probe = 4, occ_compress = 4, occ_insert = 8, occ_expand = 4;
     cudaStream_t stream = nullptr;
     IterParams *d_params = nullptr;
     IterParams *h_params = nullptr;          // pinned

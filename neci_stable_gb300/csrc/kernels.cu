@@ -660,7 +660,13 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
     const long long n = (long long)c->n_cand;
     const int W = s.W, R = s.R;
     constexpr int L = LR;
-    const unsigned long long mask = st.spawn_hash_n - 1;
+    // The table in use is sized to this step's candidates (a power of two at
+    // least twice their number), not to the allocation: at tens of millions
+    // of spawns it stays in L2 instead of scattering the probes over
+    // gigabytes of DRAM.  Its buckets are cleared through rep_bucket.
+    unsigned long long hn = 1024;
+    while (hn < 2ull * (unsigned long long)n && hn < st.spawn_hash_n) hn <<= 1;
+    const unsigned long long mask = (hn < st.spawn_hash_n ? hn : st.spawn_hash_n) - 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
     for (long long ci = blockIdx.x * (long long)blockDim.x + threadIdx.x; ci < nround; ci += stride) {
@@ -719,8 +725,14 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
     long long a_tomb = 0;  // tombstones taken over by the insertions (a negative count)
+    // the round's new determinants (blockDim.x = 128: four warps)
+    __shared__ int nq_w[2][4];
+    __shared__ long long q_slot[128];
+    __shared__ unsigned long long q_det[kMaxWords][128];
+    int round = 0;
     for (long long ri = blockIdx.x * (long long)blockDim.x + threadIdx.x; ri < nround; ri += stride) {
         bool inserted = false, want = false;
+        long long new_slot = -1;
         unsigned long long wd[kMaxWords];
         double ws[2] = {0.0, 0.0};
         long long wflags = 0, wci = 0;
@@ -823,17 +835,50 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                     NECI_FOR_WORDS(w, W) o[w] = (long long)wd[w];
                     NECI_FOR_RUNS(k, L) o[W + k] = double_to_word(ws[k]);
                     o[W + L] = wflags & ~1ll;
-                    st.diagH[slot] = diag_helement(s, wd) - s.hii;
-                    const int ic = excit_level(s.ilut_ref, wd, W);
-                    st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, wd, ic) : 0.0;
                     if (st.n_core > 0) st.core_of_slot[slot] = -1;
                     a_tomb -= hash_insert(st, slot, st.cand_h[wci], c);
                     inserted = true;
+                    new_slot = slot;
                 }
             }
         }
         const unsigned long long unused = warp_append(&c->n_new, inserted ? 1u : 0u);
         (void)unused;
+        // H_jj - Hii and <D0|H|D_j> of the round's new determinants, computed
+        // over a compacted list by consecutive threads: in place, the lanes
+        // without a new determinant would hold GB300's 1/64-rate FP64 pipe
+        // through the O(nel^2) diagonal sum as well.  List positions come
+        // from per-warp counts (by round parity), so no shared counter is
+        // read and written in the same round; the next round writes the list
+        // only after its first barrier, when this round's reads are done.
+        {
+            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            const unsigned int mb = __ballot_sync(0xffffffffu, inserted);
+            if (lane == 0) nq_w[round & 1][wid] = __popc(mb);
+            __syncthreads();
+            int before = 0, total = 0;
+#pragma unroll
+            for (int w2 = 0; w2 < 4; ++w2) {
+                const int x = nq_w[round & 1][w2];
+                before += w2 < wid ? x : 0;
+                total += x;
+            }
+            if (inserted) {
+                const int i = before + __popc(mb & ((1u << lane) - 1u));
+                q_slot[i] = new_slot;
+                NECI_FOR_WORDS(w, W) q_det[w][i] = wd[w];
+            }
+            __syncthreads();
+            if ((int)threadIdx.x < total) {
+                unsigned long long d[kMaxWords];
+                NECI_FOR_WORDS(w, W) d[w] = q_det[w][threadIdx.x];
+                const long long sl = q_slot[threadIdx.x];
+                st.diagH[sl] = diag_helement(s, d) - s.hii;
+                const int ic = excit_level(s.ilut_ref, d, W);
+                st.offdiagH[sl] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
+            }
+        }
+        ++round;
     }
     double v[6] = {a_ab[0], a_ab[1], a_rm[0], a_rm[1], a_born[0], a_born[1]};
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
@@ -1200,8 +1245,8 @@ __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, i
 // side by side (neci_gpu_iterate_batch) instead of each filling the GPU.
 static int clamp_grid(long long want, int hi) { return (int)(want < 8 ? 8 : (want > hi ? hi : want)); }
 static int grid_slots(const Engine &e) { return clamp_grid(e.st.max_walkers / 2048 + 1, e.num_sms * 4); }
-static int grid_spawns(const Engine &e, int threads) {
-    return clamp_grid(e.st.max_spawned / (threads * 4) + 1, e.num_sms * (threads == 128 ? 8 : 4));
+static int grid_spawns(const Engine &e, int threads, int occ = 0) {
+    return clamp_grid(e.st.max_spawned / (threads * 4) + 1, e.num_sms * (occ > 0 ? occ : (threads == 128 ? 8 : 4)));
 }
 static int grid_for(const Engine &e, int threads) {
     (void)threads;
@@ -1233,7 +1278,6 @@ int configure_kernels(Engine &e) {
     // 48 KB per block.  The limit is an attribute of the kernel for the whole
     // process, so it is raised to the largest row any context can have
     // (kMaxWords det words, two signs, a flag word), never lowered.
-    (void)e;
     const int rmax = kMaxWords + 2 + 1;
     const int sweep_max = 2 * kStageTile * (rmax + 2) * 8;
     const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 4);
@@ -1246,6 +1290,20 @@ int configure_kernels(Engine &e) {
         return 1;
     if (cudaFuncSetAttribute(k_merge_stats<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
         return 1;
+    // resident blocks per SM of each instance (the smaller of the two run counts)
+    auto occ = [](const void *f1, const void *f2, int threads, size_t smem) {
+        int a = 0, b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, f1, threads, smem) != cudaSuccess) a = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, f2, threads, smem) != cudaSuccess) b = 1;
+        const int m = a < b ? a : b;
+        return m < 1 ? 1 : m;
+    };
+    const size_t rh2 = (size_t)(kMaxWords * 64 + 1) * sizeof(int32_t);
+    e.occ_probe = occ((const void *)k_ann_probe<1>, (const void *)k_ann_probe<2>, 256, rh2);
+    e.occ_compress = occ((const void *)k_ann_compress<1>, (const void *)k_ann_compress<2>, 256, 0);
+    e.occ_insert = occ((const void *)k_ann_insert<1>, (const void *)k_ann_insert<2>, 128, 0);
+    e.occ_expand = occ((const void *)k_expand, (const void *)k_expand, 256, 0);
+    (void)cudaGetLastError();
     return 0;
 }
 
@@ -1261,22 +1319,22 @@ void launch_sweep(Engine &e, cudaStream_t s) {
         else k_sweep<1, false><<<grid, kStageTile, shm, s>>>(e.sys, e.st, e.d_params);
     }
 }
-void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256), 256, 0, s>>>(e.st); }
+void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256, e.occ_expand), 256, 0, s>>>(e.st); }
 void launch_core(Engine &e, cudaStream_t s) {
     if (e.st.n_core > 0) k_core<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_ann_probe(Engine &e, cudaStream_t s) {
     const size_t shm = (e.sys.nbasis + 1) * sizeof(int32_t);
-    if (e.sys.L == 2) k_ann_probe<2><<<grid_spawns(e, 256), 256, shm, s>>>(e.sys, e.st);
-    else k_ann_probe<1><<<grid_spawns(e, 256), 256, shm, s>>>(e.sys, e.st);
+    if (e.sys.L == 2) k_ann_probe<2><<<grid_spawns(e, 256, e.occ_probe), 256, shm, s>>>(e.sys, e.st);
+    else k_ann_probe<1><<<grid_spawns(e, 256, e.occ_probe), 256, shm, s>>>(e.sys, e.st);
 }
 void launch_ann_compress(Engine &e, cudaStream_t s) {
-    if (e.sys.L == 2) k_ann_compress<2><<<grid_spawns(e, 256), 256, 0, s>>>(e.sys, e.st);
-    else k_ann_compress<1><<<grid_spawns(e, 256), 256, 0, s>>>(e.sys, e.st);
+    if (e.sys.L == 2) k_ann_compress<2><<<grid_spawns(e, 256, e.occ_compress), 256, 0, s>>>(e.sys, e.st);
+    else k_ann_compress<1><<<grid_spawns(e, 256, e.occ_compress), 256, 0, s>>>(e.sys, e.st);
 }
 void launch_ann_insert(Engine &e, cudaStream_t s) {
-    if (e.sys.L == 2) k_ann_insert<2><<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
-    else k_ann_insert<1><<<grid_spawns(e, 128), 128, 0, s>>>(e.sys, e.st, e.d_params);
+    if (e.sys.L == 2) k_ann_insert<2><<<grid_spawns(e, 128, e.occ_insert), 128, 0, s>>>(e.sys, e.st, e.d_params);
+    else k_ann_insert<1><<<grid_spawns(e, 128, e.occ_insert), 128, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
     if (e.sys.L == 2)
