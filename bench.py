@@ -46,10 +46,10 @@ BLOOM = 3.0
 # this workload at 1e7 walkers) per unit of work, for roofline.traffic:
 # kernel -> (bytes per unit, step count that is the unit).
 NCU_DRAM_BYTES_PER_UNIT = {
-    "spawn": (16.4, "n_attempts"),
-    "sweep": (67.0, "tot_walkers"),
-    "merge_stats": (53.8, "tot_walkers"),
-    "ann_probe": (108.7, "n_spawned"),
+    "spawn": (14.5, "n_attempts"),
+    "sweep": (47.3, "tot_walkers"),
+    "merge_stats": (37.7, "tot_walkers"),
+    "ann_probe": (99.9, "n_spawned"),
 }
 
 
