@@ -127,27 +127,37 @@ def test_annihilate_injected(name, trunc):
     assert sg.n_new == sc.n_new and sg.n_occupied == sc.n_occupied
 
 
-def run_pair(name, iters, start_pop, tau, shift=0.0, seed=31, precision=capi.PREC_FP64, real=1):
+def run_pair(name, iters, start_pop, tau, shift=0.0, seed=31, precision=capi.PREC_FP64, real=1, p_singles=None,
+             av=1.0):
     spec, eng, orc = pair(name, 400_000, 800_000)
-    eng.start_from_reference(initial_part=start_pop)
-    rows, _, _ = eng.download()
-    orc.upload(rows)
-    W, L = spec.W, spec.lenof_sign
-    for it in range(1, iters + 1):
-        p = capi.default_params(tau=tau, diag_sft=[shift, shift], seed=seed, iter=it, precision=precision,
-                                t_all_real_coeff=real)
-        sg = eng.perform_fcimc_cyc_par(p)
-        sc, rc = orc.iterate(p)
-        assert rc == 0 and sg.err == 0, (it, rc, sg.err)
-        rg = canonical(eng.download()[0], W)
-        rcpu = canonical(orc.download()[0], W)
-        assert rg.shape == rcpu.shape, (it, rg.shape, rcpu.shape)
-        assert np.array_equal(rg[:, : W + L], rcpu[:, : W + L]), it
-        assert np.array_equal(rg[:, -1] & ~1, rcpu[:, -1] & ~1), it
-        for f in ("nborn", "ndied", "nannihil", "naborted", "nremoved", "tot_parts", "hf_cyc", "enum_cyc",
-                  "tot_parts_old"):
-            np.testing.assert_allclose(getattr(sg, f)[:], getattr(sc, f)[:], rtol=1e-9, atol=1e-7, err_msg=f"{f} it {it}")
-        assert sg.n_attempts == sc.n_attempts and sg.n_spawned == sc.n_spawned and sg.n_new == sc.n_new
+    if p_singles is not None:
+        eng.set_excit_biases(p_singles, spec.p_parallel)
+        orc.set_excit_biases(p_singles, spec.p_parallel)
+    try:
+        eng.start_from_reference(initial_part=start_pop)
+        rows, _, _ = eng.download()
+        orc.upload(rows)
+        W, L = spec.W, spec.lenof_sign
+        for it in range(1, iters + 1):
+            p = capi.default_params(tau=tau, diag_sft=[shift, shift], seed=seed, iter=it, precision=precision,
+                                    t_all_real_coeff=real, av_mc_excits=av)
+            sg = eng.perform_fcimc_cyc_par(p)
+            sc, rc = orc.iterate(p)
+            assert rc == 0 and sg.err == 0, (it, rc, sg.err)
+            rg = canonical(eng.download()[0], W)
+            rcpu = canonical(orc.download()[0], W)
+            assert rg.shape == rcpu.shape, (it, rg.shape, rcpu.shape)
+            assert np.array_equal(rg[:, : W + L], rcpu[:, : W + L]), it
+            assert np.array_equal(rg[:, -1] & ~1, rcpu[:, -1] & ~1), it
+            for f in ("nborn", "ndied", "nannihil", "naborted", "nremoved", "tot_parts", "hf_cyc", "enum_cyc",
+                      "tot_parts_old"):
+                np.testing.assert_allclose(getattr(sg, f)[:], getattr(sc, f)[:], rtol=1e-9, atol=1e-7,
+                                           err_msg=f"{f} it {it}")
+            assert sg.n_attempts == sc.n_attempts and sg.n_spawned == sc.n_spawned and sg.n_new == sc.n_new
+    finally:
+        if p_singles is not None:
+            eng.set_excit_biases(spec.p_singles, spec.p_parallel)
+            orc.set_excit_biases(spec.p_singles, spec.p_parallel)
     return sg
 
 
@@ -162,7 +172,27 @@ def test_iterations_bit_exact(name, iters, pop, tau):
 
 def test_iterations_integer_walkers_and_mixed():
     run_pair("hub10", 20, 30.0, 0.02, real=0)
+    run_pair("mol24", 12, 60.0, 0.01, real=0)
     run_pair("mol12", 15, 40.0, 0.02, precision=capi.PREC_MIXED)
+
+
+# pSingles 0.5 takes the spawn kernel's instance that queues both classes
+# (0.15 <= pSingles <= 0.85), the defaults (0.003-0.05) the one that runs
+# doubles inline; the systems cover the word-count instances: one word
+# (mol24), two (mol40, mol40u), three row words of which two hold orbitals
+# (mol64, 128 spin orbitals)
+@pytest.mark.parametrize("name,ps", [("mol24", 0.5), ("mol40", 0.5), ("mol64", 0.5), ("mol12u", 0.5),
+                                     ("mol40u", 0.5), ("mol64", None), ("mol40", None)])
+def test_spawn_instances_bit_exact(name, ps):
+    st = run_pair(name, 12, 100.0, 0.01, p_singles=ps)
+    assert st.n_spawned > 0
+
+
+# AvMCExcits != 1: decide_num_to_spawn in FP64 (the sweep's general instance)
+# and 1/AvMCExcits in the spawn amplitude
+@pytest.mark.parametrize("name,av", [("mol24", 2.0), ("hub10", 0.5)])
+def test_iterations_av_mc_excits(name, av):
+    run_pair(name, 12, 40.0, 0.01, av=av)
 
 
 def test_iterate_n_matches_single_steps():
