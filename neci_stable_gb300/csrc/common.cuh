@@ -108,7 +108,7 @@ __device__ inline void hash_remove(const DevState &st, long long j) {
 __device__ inline long long hash_find(const DevState &st, const unsigned long long *d, int W, int R,
                                       unsigned long long h, Control *ctl) {
     const unsigned long long mask = st.hash_n - 1;
-    unsigned long long b = hash_mod(h, st.hash_n);
+    unsigned long long b = hash_bucket(h, st.hash_n);
     for (int p = 0; p < kProbeLimit; ++p) {
         const uint32_t e = st.hash[b];
         if (e == kEmpty) return -1;
@@ -126,7 +126,7 @@ __device__ inline long long hash_find(const DevState &st, const unsigned long lo
 // tombstone's bucket (the caller takes one off its tombstone count).
 __device__ inline int hash_insert(const DevState &st, long long slot, unsigned long long h, Control *ctl) {
     const unsigned long long mask = st.hash_n - 1;
-    unsigned long long b = hash_mod(h, st.hash_n);
+    unsigned long long b = hash_bucket(h, st.hash_n);
     for (int p = 0; p < kProbeLimit; ++p) {
         const uint32_t e = st.hash[b];
         if (e == kEmpty || e == kTomb) {

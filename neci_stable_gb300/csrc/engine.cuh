@@ -463,6 +463,13 @@ __device__ inline unsigned long long hash_mod(unsigned long long hash, unsigned 
     const unsigned long long mag = h < 0 ? (0ull - (unsigned long long)h) : (unsigned long long)h;
     return mag % n;
 }
+// hash_mod for a table length n that is a power of two (the walker hash):
+// abs(mod(h, n)) is the magnitude's low bits, with no 64-bit division.
+__device__ inline unsigned long long hash_bucket(unsigned long long hash, unsigned long long n) {
+    const long long h = (long long)hash;
+    const unsigned long long mag = h < 0 ? (0ull - (unsigned long long)h) : (unsigned long long)h;
+    return mag & (n - 1);
+}
 
 // ---------------------------------------------------------------------------
 // Integrals.

@@ -64,7 +64,7 @@ __global__ void k_upload_fix(DevSys s, DevState st, long long nrows, int compute
         for (int k = 0; k < s.L; ++k) occ = occ || fabs(word_to_double(r[s.W + k])) >= kEps12;
         if (!occ) continue;
         const unsigned long long mask = st.hash_n - 1;
-        unsigned long long b = hash_mod(neci_hash(d, s.W, s.random_hash2), st.hash_n);
+        unsigned long long b = hash_bucket(neci_hash(d, s.W, s.random_hash2), st.hash_n);
         for (int p = 0; p < kProbeLimit; ++p) {
             if (atomicCAS(&st.hash[b], kEmpty, (uint32_t)(j + 1)) == kEmpty) {
                 st.slot_bucket[j] = (uint32_t)b;
@@ -178,7 +178,7 @@ __global__ void k_core_mark(DevSys s, DevState st, const long long *core_dets, l
         unsigned long long d[kMaxWords];
         for (int w = 0; w < s.W; ++w) d[w] = (unsigned long long)core_dets[c * s.W + w];
         const unsigned long long mask = st.hash_n - 1;
-        unsigned long long b = hash_mod(neci_hash(d, s.W, s.random_hash2), st.hash_n);
+        unsigned long long b = hash_bucket(neci_hash(d, s.W, s.random_hash2), st.hash_n);
         long long slot = -1;
         for (int p = 0; p < kProbeLimit; ++p) {
             const uint32_t e = st.hash[b];
