@@ -166,8 +166,10 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def algorithmic_bytes(kernel, st, W, L, nnz=0):
-    """Bytes a kernel must move per launch (per unit counts of the step)."""
+def algorithmic_bytes(kernel, st, W, L, nnz=0, fused=True):
+    """Bytes a kernel must move per launch (per unit counts of the step).
+    fused: pass 1 of the annihilation (the hash lookup of every spawn) ran
+    inside the spawn kernel, which is the case unless the 2-RDM is sampled."""
     R = 8 * (W + L + 1)
     G = 16
     D = st["n_occupied"]
@@ -178,9 +180,14 @@ def algorithmic_bytes(kernel, st, W, L, nnz=0):
     if kernel == "sweep":
         return slots * (R + G) + D * 8 * L + D * 16
     if kernel == "spawn":
-        # the 8 B attempt entries read and the spawn records written (parent
-        # rows and tables are gathered from L2)
-        return st["n_attempts"] * 8 + S * R
+        # the 8 B attempt entries read (parent rows and tables are gathered
+        # from L2); fused: per spawn a hash bucket and the row's det words
+        # read and a 12 B spawn sum updated, a record written per candidate
+        # (the estimate of the compression pass); else every record written
+        if not fused:
+            return st["n_attempts"] * 8 + S * R
+        cand = max(S - (U - N), 0)
+        return st["n_attempts"] * 8 + S * (4 + 8 * W + 12) + cand * (R + 12)
     if kernel == "core":
         # CSR column index and FP64 value per element, x gathered and y written
         return nnz * (4 + 8) + st["n_core"] * 16 * L
@@ -610,7 +617,8 @@ def main():
     top = max(kt, key=lambda k: kt[k][0])
     top_ms = kt[top][0] / kt[top][1]
     nnz = (r["core_info"] or {}).get("nnz", 0)
-    ab = algorithmic_bytes(top, r["last"], W, L, nnz)
+    fused = "ann_probe" not in kt  # pass 1 ran inside the spawn kernel
+    ab = algorithmic_bytes(top, r["last"], W, L, nnz, fused)
     hbm, peak_kind = peaks()
     achieved = ab / (top_ms / 1e3) / 1e9
     traffic = None
@@ -620,13 +628,13 @@ def main():
     # achieved GB/s of every kernel (algorithmic bytes of the last profiled step)
     kernel_gbs = {}
     for k, (ms, cnt) in kt.items():
-        b = algorithmic_bytes(k, r["last"], W, L, nnz)
+        b = algorithmic_bytes(k, r["last"], W, L, nnz, fused)
         if b > 0:
             kernel_gbs[k] = b / (ms / cnt / 1e3) / 1e9
-    ann = ("ann_probe", "ann_compress", "ann_insert")
-    ann_ms = sum(kt[k][0] / kt[k][1] for k in ann if k in kt)
+    ann = tuple(k for k in ("ann_probe", "ann_compress", "ann_insert") if k in kt)
+    ann_ms = sum(kt[k][0] / kt[k][1] for k in ann)
     ann_bytes = sum(algorithmic_bytes(k, r["last"], W, L) for k in ann)
-    launches_per_step = 16 + (1 if r["last"]["n_core"] > 0 else 0)
+    launches_per_step = 15 + (1 if r["last"]["n_core"] > 0 else 0) + (0 if fused else 1)
     line = {
         "metric": METRIC, "value": updates / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,

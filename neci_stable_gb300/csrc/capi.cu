@@ -107,7 +107,9 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_EXPAND, [&] { launch_expand(e, e.stream); });
     stage(e, K_SPAWN, [&] { launch_spawn(e, e.stream); });
     if (e.st.n_core > 0) stage(e, K_CORE, [&] { launch_core(e, e.stream); });
-    stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
+    // pass 1 (the hash lookup of every spawn) runs as its own kernel unless
+    // the spawn kernel does it (fuse_probe)
+    if (!e.fuse_probe || e.sys.rdm) stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
     stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
     stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream); });
     stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, e.st.n_core > 0 ? 1 : 0); });
@@ -706,6 +708,24 @@ static const char *not_ready(const Engine &e) {
     return nullptr;
 }
 
+// Pass 1 of the annihilation (the hash lookup of every spawn) moves into the
+// spawn kernel where spawns are frequent enough for its lookups to fill a
+// warp's lanes; where they are rare a separate kernel packs them 32 to a warp.
+// On GB300 a spawn rate of 0.41 (the 6x6 Hubbard lattice) made the fused step
+// 10% faster, rates of 0.16 and 0.024 (molecules) 3% and 9% slower, so only
+// the lattice instances of the spawn kernel carry the fused path.  Decided
+// from the last step, with a margin against flipping; a change drops the
+// captured step graphs.
+static void update_fuse_probe(Engine &e, const neci_gpu_iter_stats &last) {
+    if (e.sys.rdm || e.sys.excitgen != NECI_EXGEN_RS_HUBBARD || last.n_attempts <= 0) return;
+    const double rate = (double)last.n_spawned / (double)last.n_attempts;
+    const bool want = e.fuse_probe ? rate >= 0.25 : rate >= 0.3;
+    if (want != e.fuse_probe) {
+        e.fuse_probe = want;
+        drop_graphs(e);
+    }
+}
+
 static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_gpu_iter_stats *stats,
                      double *device_ms = nullptr) {
     if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
@@ -714,9 +734,9 @@ static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_
     CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
     int done = 0;
     if (device_ms) *device_ms = 0.0;
-    if (!e.profiling)
-        if (int r = ensure_graph(e)) return r;
     while (done < n_iter) {
+        if (!e.profiling)
+            if (int r = ensure_graph(e)) return r;
         const int batch = std::min(n_iter - done, e.max_stats);
         if (device_ms) CK(cudaEventRecord(e.ev[0], e.stream));
         if (e.profiling) {
@@ -744,6 +764,7 @@ static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_
                 return fail(stats[done - 1].err, "device reported an error in the step");
             }
         done += batch;
+        update_fuse_probe(e, stats[done - 1]);
     }
     return NECI_GPU_OK;
 }
@@ -822,6 +843,7 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         Engine &e = ctxs[c]->e;
         std::memcpy(stats + (size_t)c * n_iter, e.h_stats, sizeof(neci_gpu_iter_stats) * n_iter);
         for (int i = 0; i < n_iter && !first_err; ++i) first_err = e.h_stats[i].err;
+        if (!first_err) update_fuse_probe(e, e.h_stats[n_iter - 1]);
     }
     if (first_err) return fail(first_err, "device reported an error in a batched step");
     return NECI_GPU_OK;

@@ -37,6 +37,9 @@ struct Engine {
     // resident blocks per SM of the grid-stride spawn-list kernels (their
     // grids fill the GPU once; the latency-bound hash passes want every warp)
     int occ_probe = 4, occ_compress = 4, occ_insert = 8, occ_expand = 4;
+    // pass 1 of the annihilation runs inside the spawn kernel (chosen from the
+    // last step's spawn rate; see update_fuse_probe)
+    bool fuse_probe = false;
     cudaStream_t stream = nullptr;
     IterParams *d_params = nullptr;
     IterParams *h_params = nullptr;          // pinned

@@ -657,7 +657,9 @@ template <int LR>
 __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
     if (halted(st)) return;
     Control *c = st.ctl;
-    const long long n = (long long)c->n_cand;
+    // the appends count past the allocation when it overflows (SPAWN_FULL is
+    // reported at the end of the step): only the entries written are read
+    const long long n = (long long)min(c->n_cand, (unsigned long long)st.max_spawned);
     const int W = s.W, R = s.R;
     constexpr int L = LR;
     // The table in use is sized to this step's candidates (a power of two at

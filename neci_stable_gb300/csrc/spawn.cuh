@@ -151,12 +151,45 @@ __device__ inline double rdm_parent_weight(const IterParams &p, double invp, uns
     return neg ? -w : w;
 }
 
-// create_particle (fcimc_helper.F90:152-308): append the record; warp-wide.
+// The block's sums of the spawns it created, in shared memory: their number
+// and sum of |amplitude| per run (n_spawned and abs_q of the step).  Kept out
+// of registers, which the spawn loop is short of.
+struct SpawnSums {
+    unsigned long long *sh;  // [3]: number, |amplitude| of run 0, of run 1
+};
+
+// create_particle (fcimc_helper.F90:152-308) with pass 1 of the
+// annihilation done at once: the child is looked up in the walker hash
+// (hash_table_lookup); one that is occupied takes the found branch of
+// AnnihilateSpawnedParts (Annihilation.F90:1000-1140), its fixed-point
+// amplitude, record count and initiator bit added to the slot's spawn sums
+// (acc, meta), while an absent child becomes a candidate record of the
+// compression pass.  The sums are integer atomics, so the order of the spawns
+// does not matter.  Done when `fused` (chosen by the host where spawns are
+// frequent enough to fill the lookup's lanes, and never with 2-RDM sampling,
+// which needs every record and its parent); otherwise every spawn is written
+// and pass 1 runs as its own kernel.  Warp-wide (the appends).
 template <typename Real, int NW, int RW>
 __device__ inline void create_particle(const DevSys &s, const DevState &st, const IterParams &p, long long qv,
-                                       const Parent &P, const Excit<Real> &e) {
-    const unsigned long long pos = warp_append(&st.ctl->n_spawned, qv != 0 ? 1u : 0u);
-    if (qv == 0) return;
+                                       const Parent &P, const Excit<Real> &e, const int32_t *sh_rh2, const SpawnSums &ss,
+                                       bool fused) {
+    long long slot = -1;
+    unsigned long long h = 0;
+    if (qv != 0 && fused) {
+        h = neci_hash(e.child, nwords<NW>(s), sh_rh2);
+        slot = hash_find(st, e.child, nwords<NW>(s), s.R, h, st.ctl);
+        atomicAdd(&ss.sh[0], 1ull);
+        atomicAdd(&ss.sh[1 + P.run], (unsigned long long)(qv < 0 ? -qv : qv));
+    }
+    if (fused && qv != 0 && slot >= 0) {
+        const long long j = slot * s.L + P.run;
+        atomicAdd((unsigned long long *)&st.acc[j], (unsigned long long)qv);
+        atomicAdd(&st.meta[j], 1u);
+        if (P.pinit) atomicOr(&st.meta[j], 0x80000000u);
+    }
+    const bool rec = qv != 0 && (!fused || slot < 0);
+    const unsigned long long pos = warp_append(fused ? &st.ctl->n_cand : &st.ctl->n_spawned, rec ? 1u : 0u);
+    if (!rec) return;
     if (pos >= (unsigned long long)st.max_spawned) {
         set_err(st.ctl, NECI_GPU_ERR_SPAWN_FULL);
         return;
@@ -165,14 +198,18 @@ __device__ inline void create_particle(const DevSys &s, const DevState &st, cons
     NECI_FOR_WORDS(w, rwords<RW>(s)) o[w] = w < nwords<NW>(s) ? (long long)e.child[w] : 0ll;
     for (int k2 = 0; k2 < s.L; ++k2) o[rwords<RW>(s) + k2] = (k2 == P.run) ? qv : 0ll;
     o[rwords<RW>(s) + s.L] = P.pinit ? (1ll << init_flag_bit(P.run)) : 0ll;
-    if (s.rdm) {
-        // the parent and its unbiased sign for the 2-RDM: sign(C_i) divided
-        // by the expected number of non-zero spawns onto this child per unit
-        // of |C_i|, AvMCExcits p_gen P(spawn != 0)
-        long long *par = st.spawn_par + pos * (rwords<RW>(s) + 1);
-        NECI_FOR_WORDS(w, rwords<RW>(s)) par[w] = w < nwords<NW>(s) ? (long long)P.d[w] : 0ll;
-        par[rwords<RW>(s)] = double_to_word(rdm_parent_weight(p, (double)e.invp, e.aq, P.neg));
+    if (fused) {
+        st.cand[pos] = (uint32_t)pos;
+        st.cand_h[pos] = h;
+        return;
     }
+    if (!s.rdm) return;
+    // the parent and its unbiased sign for the 2-RDM: sign(C_i) divided
+    // by the expected number of non-zero spawns onto this child per unit
+    // of |C_i|, AvMCExcits p_gen P(spawn != 0)
+    long long *par = st.spawn_par + pos * (rwords<RW>(s) + 1);
+    NECI_FOR_WORDS(w, rwords<RW>(s)) par[w] = w < nwords<NW>(s) ? (long long)P.d[w] : 0ll;
+    par[rwords<RW>(s)] = double_to_word(rdm_parent_weight(p, (double)e.invp, e.aq, P.neg));
 }
 
 // One attempt of class CLS (0: double, 1: single) whose parent and stream
@@ -180,7 +217,8 @@ __device__ inline void create_particle(const DevSys &s, const DevState &st, cons
 // choice), so the draws are those of the attempt processed inline.
 template <typename Real, int GEN, int CLS, int NW, int RW>
 __device__ inline void spawn_class(const DevSys &s, const DevState &st, const IterParams &p, bool valid,
-                                   const Parent &P, Stream &rng, const int32_t *sh_rh2, int &ovf, TauAcc *tacc) {
+                                   const Parent &P, Stream &rng, const int32_t *sh_rh2, int &ovf, TauAcc *tacc,
+                                   const SpawnSums &ss, bool fused) {
     Excit<Real> e;
     e.ok = false;
     long long qv = 0;
@@ -190,7 +228,7 @@ __device__ inline void spawn_class(const DevSys &s, const DevState &st, const It
         else gen_pchb_double<Real, NW>(s, P.d, rng, e);
         qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, tacc);
     }
-    create_particle<Real, NW, RW>(s, st, p, qv, P, e);
+    create_particle<Real, NW, RW>(s, st, p, qv, P, e, sh_rh2, ss, fused);
 }
 
 // The parent and stream of a queued attempt: the stream resumes after its
@@ -223,8 +261,11 @@ __device__ inline Stream load_queued(const DevSys &s, const DevState &st, const 
 // determinant key, the records and the row offsets use all RW.  NW = RW = 0
 // is the instance for any size, with the counts read from the system.
 template <typename Real, int GEN, int NW, int RW, bool QD>
-__global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp) {
+__global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp, int fuse_probe) {
     if (halted(st)) return;
+    // lattice systems only: their singles spawn often enough to fill the
+    // lookup's lanes; the molecular instances carry no fused code
+    const bool fused = GEN == NECI_EXGEN_RS_HUBBARD && fuse_probe != 0 && !s.rdm;
     extern __shared__ int32_t sh[];
     // per class: attempt entries and their second draws (at most two
     // rounds' worth are held), and each warp's appends of the round (by
@@ -232,6 +273,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
     __shared__ unsigned long long sq[2][256], sr1[2][256];
     __shared__ int wcnt[2][2][4];
     __shared__ unsigned int ring_tail;
+    __shared__ unsigned long long sh_sums[3];
     __shared__ TauAcc tacc;
     int32_t *sh_rh2 = sh;
     int32_t *sh_neigh = sh + (s.nbasis + 1);
@@ -243,6 +285,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
         tacc.c[threadIdx.x] = 0u;
     }
     if (threadIdx.x == 0) ring_tail = 0u;
+    if (threadIdx.x < 3) sh_sums[threadIdx.x] = 0ull;
     __syncthreads();
     const IterParams p = *pp;
     const long long nat = (long long)min(st.ctl->n_att, (unsigned long long)st.max_att);
@@ -252,6 +295,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     int qn[2] = {0, 0};  // queue lengths, the same in every thread
     int ovf = 0;
+    const SpawnSums ss = {sh_sums};
     if (GEN == NECI_EXGEN_RS_HUBBARD) {
         // lattice systems (singles only): one attempt per thread per round
         for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nround; q += stride) {
@@ -267,7 +311,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
                 gen_rs_hubbard<Real, NW>(s, P.d, sh_neigh, rng, e);
                 qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
             }
-            create_particle<Real, NW, RW>(s, st, p, qv, P, e);
+            create_particle<Real, NW, RW>(s, st, p, qv, P, e, sh_rh2, ss, fused);
         }
     }
     // Molecular systems without QD (singles rare or dominant): a round
@@ -311,7 +355,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
                         qv = attempt_create<Real, NW, RW>(s, st, p, P, e, rng, sh_rh2, ovf, &tacc);
                     }
                 }
-                create_particle<Real, NW, RW>(s, st, p, qv, P, e);
+                create_particle<Real, NW, RW>(s, st, p, qv, P, e, sh_rh2, ss, fused);
             }
             if (single) {
                 const unsigned int t = atomicAdd(&ring_tail, 1u) & 511u;
@@ -328,7 +372,7 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
                 cnt -= take;
                 Parent P;
                 Stream rng = load_queued<NW, RW>(s, st, p, v, a, b, P);
-                spawn_class<Real, GEN, 1, NW, RW>(s, st, p, v, P, rng, sh_rh2, ovf, &tacc);
+                spawn_class<Real, GEN, 1, NW, RW>(s, st, p, v, P, rng, sh_rh2, ovf, &tacc, ss, fused);
             }
         }
     }
@@ -414,17 +458,25 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
                 if (t0) {
                     Parent P;
                     Stream rng = load_queued<NW, RW>(s, st, p, v0, a0, b0, P);
-                    spawn_class<Real, GEN, 0, NW, RW>(s, st, p, v0, P, rng, sh_rh2, ovf, &tacc);
+                    spawn_class<Real, GEN, 0, NW, RW>(s, st, p, v0, P, rng, sh_rh2, ovf, &tacc, ss, fused);
                 }
                 if (t1) {
                     Parent P;
                     Stream rng = load_queued<NW, RW>(s, st, p, v1, a1, b1, P);
-                    spawn_class<Real, GEN, 1, NW, RW>(s, st, p, v1, P, rng, sh_rh2, ovf, &tacc);
+                    spawn_class<Real, GEN, 1, NW, RW>(s, st, p, v1, P, rng, sh_rh2, ovf, &tacc, ss, fused);
                 }
             }
         }
     }
     if (ovf) set_err(st.ctl, NECI_GPU_ERR_OVERFLOW);
+    // n_spawned and abs_q of the spawns created here (with 2-RDM sampling
+    // pass 1 counts them)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (sh_sums[0]) atomicAdd(&st.ctl->n_spawned, sh_sums[0]);
+        if (sh_sums[1]) atomicAdd(&st.ctl->abs_q[0], sh_sums[1]);
+        if (sh_sums[2]) atomicAdd(&st.ctl->abs_q[1], sh_sums[2]);
+    }
     if (s.tau_search) {
         __syncthreads();
         if (threadIdx.x < 4) {
@@ -451,12 +503,12 @@ inline int spawn_queue_doubles(const DevSys &s) {
 template <typename Real, int GEN, bool QD>
 void launch_spawn_words(Engine &e, cudaStream_t s, int grid, size_t shm) {
     const int rw = e.sys.W, nw = (e.sys.nbasis + 63) / 64;
-    if (rw == 1) k_spawn<Real, GEN, 1, 1, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 2) k_spawn<Real, GEN, 2, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else if (rw == 3) k_spawn<Real, GEN, 3, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
-    else k_spawn<Real, GEN, 0, 0, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params);
+    if (rw == 1) k_spawn<Real, GEN, 1, 1, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
+    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
+    else if (rw == 2) k_spawn<Real, GEN, 2, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
+    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
+    else if (rw == 3) k_spawn<Real, GEN, 3, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
+    else k_spawn<Real, GEN, 0, 0, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
 }
 
 template <typename Real, int GEN>
