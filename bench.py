@@ -45,6 +45,12 @@ BLOOM = 3.0
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of
 # this workload at 1e7 walkers) per unit of work, for roofline.traffic:
 # kernel -> (bytes per unit, step count that is the unit).
+# The spawn kernel is bound by instruction issue, not by HBM: one ncu capture
+# of it on this workload (profiles/spawn_n24_pchb_2e6.md), reported beside its
+# HBM roofline.
+NCU_SPAWN_ISSUE = {"issue_active": 0.571, "alu_pipe": 0.563, "fp64_pipe": 0.398, "warps_active": 0.431,
+                   "lanes_per_instruction": 18.1, "dram_bytes_per_attempt": 14.5}
+
 NCU_DRAM_BYTES_PER_UNIT = {
     "spawn": (14.5, "n_attempts"),
     "sweep": (47.3, "tot_walkers"),
@@ -659,6 +665,8 @@ def main():
                      "frac": achieved / hbm, "peak_kind": peak_kind, "traffic": traffic,
                      "algorithmic_bytes": ab, "ms_per_launch": top_ms,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per unit of this workload"},
+        "spawn_issue": dict(NCU_SPAWN_ISSUE, source="ncu --set full of k_spawn on this workload at 2e6 walkers; "
+                                                   "fractions of the sustained peak, per SM"),
         "annihilation_roofline": {"kernels": list(ann), "achieved": ann_bytes / (ann_ms / 1e3) / 1e9, "peak": hbm,
                                   "unit": "GB/s", "frac": ann_bytes / (ann_ms / 1e3) / 1e9 / hbm,
                                   "ms_per_step": ann_ms, "algorithmic_bytes": ann_bytes},
