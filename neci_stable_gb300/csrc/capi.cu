@@ -616,6 +616,9 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
     s.alias_prob = prob;
     s.alias_alias = alias;
     s.alias_present = present;
+    AliasRec *arec;
+    if (int r = dalloc(e, &arec, ntab * s.abMax)) return r;
+    s.alias_rec = arec;
     s.pexch = pexch;
     s.tgt_pair = tgt;
     launch_pchb_build(e);

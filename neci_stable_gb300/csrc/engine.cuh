@@ -77,6 +77,28 @@ enum TauClass : int { TC_SING = 0, TC_DOUB = 1, TC_PAR = 2, TC_OPP = 3 };
 constexpr unsigned int kTauCntThreshold = 50;  // cnt_threshold
 
 // System description as seen by the kernels (passed by value).
+// One slot of a PCHB alias table (per (ij, type) and slot), the fields a
+// draw reads in one 32-byte sector: the slot's threshold and alias, and the
+// probability, 1/probability and target pair of the slot itself.  A draw that
+// keeps its slot reads one record, one that takes the alias a second.
+struct __align__(32) AliasRec {
+    unsigned long long thr;  // prob_thresh(bias)
+    double prob, inv;        // p(ab | ij, type) and its reciprocal
+    int32_t alias;           // 1-based alias slot
+    int32_t tgt;             // tgt_pair of this slot: (small << 16) | large
+};
+__device__ inline AliasRec load_alias(const AliasRec *p) {
+    const ulonglong2 *q = reinterpret_cast<const ulonglong2 *>(p);
+    const ulonglong2 x = __ldg(q), y = __ldg(q + 1);
+    AliasRec r;
+    r.thr = x.x;
+    r.prob = __longlong_as_double((long long)x.y);
+    r.inv = __longlong_as_double((long long)y.x);
+    r.alias = (int32_t)(uint32_t)(y.y & 0xFFFFFFFFull);
+    r.tgt = (int32_t)(uint32_t)(y.y >> 32);
+    return r;
+}
+
 struct DevSys {
     int nel, nbasis, W, L, R, system, excitgen, max_neigh, nsites, nOccAlpha, nOccBeta, nBI;
     double uhub, bhub, ecore, p_singles, p_parallel, hii;
@@ -91,6 +113,7 @@ struct DevSys {
     const int32_t *alias_alias;
     const double *alias_prob;
     const uint8_t *alias_present;  // [(ij-1)*3 + type-1]
+    const struct AliasRec *alias_rec;  // [(ij-1)*3 + type-1][abMax]: one 32 B record per slot
     const int32_t *tgt_pair;       // [abMax+1]: (small << 16) | large
     // hoisted constants of the generators
     double pgen_par, pgen_opp, p_doubles, p_elec;        // pBias/par, (1-pBias)/AB, 1-pSingles, 1/nel

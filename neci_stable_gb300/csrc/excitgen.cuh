@@ -276,10 +276,30 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     const unsigned long long pos0 = __umul64hi(r, n);
     const unsigned long long frac = r * n;
     const size_t base = t * (size_t)s.abMax;
-    const unsigned long long thr = __ldg(&s.alias_thr[base + pos0]);
-    const int ab = (frac < thr || thr == ~0ull) ? (int)pos0 + 1 : __ldg(&s.alias_alias[base + pos0]);
-    const Real pholes = dbl ? (Real)__ldg(&s.alias_prob[base + ab - 1]) : (Real)__ldg(&s.alias_prob32[base + ab - 1]);
-    const int tp = __ldg(&s.tgt_pair[ab]);
+    int ab, tp;
+    Real pholes, ainv;
+    if (dbl) {
+        // the slot's 32-byte record; a taken alias reads the alias's record
+        const AliasRec a = load_alias(&s.alias_rec[base + pos0]);
+        if (frac < a.thr || a.thr == ~0ull) {
+            ab = (int)pos0 + 1;
+            pholes = (Real)a.prob;
+            ainv = (Real)a.inv;
+            tp = a.tgt;
+        } else {
+            ab = a.alias;
+            const AliasRec b = load_alias(&s.alias_rec[base + ab - 1]);
+            pholes = (Real)b.prob;
+            ainv = (Real)b.inv;
+            tp = b.tgt;
+        }
+    } else {
+        const unsigned long long thr = __ldg(&s.alias_thr[base + pos0]);
+        ab = (frac < thr || thr == ~0ull) ? (int)pos0 + 1 : __ldg(&s.alias_alias[base + pos0]);
+        pholes = (Real)__ldg(&s.alias_prob32[base + ab - 1]);
+        ainv = (Real)__ldg(&s.alias_inv32[base + ab - 1]);
+        tp = __ldg(&s.tgt_pair[ab]);
+    }
     const int o0 = 2 * (tp >> 16) - spin0, o1 = 2 * (tp & 0xFFFF) - spin1;
     // pholes > 1e-10 (pholes >= 0: compared on the bits in FP64)
     const bool small = dbl ? !(dbl_bits((double)pholes) > dbl_bits(1e-10)) : !(pholes > (Real)1e-10);
@@ -287,7 +307,7 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     finish_double<Real, NW>(s, d, src0, src1, o0, o1, e);
     pgen *= pholes;
     e.pgen = pgen * (dbl ? (Real)s.p_doubles : (Real)s.f_p_doubles);
-    invp *= dbl ? (Real)__ldg(&s.alias_inv[base + ab - 1]) : (Real)__ldg(&s.alias_inv32[base + ab - 1]);
+    invp *= ainv;
     e.invp = invp * (dbl ? (Real)s.inv_pdoub : (Real)s.f_inv_pdoub);
     e.ok = true;
 }

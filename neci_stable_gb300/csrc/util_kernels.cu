@@ -346,6 +346,21 @@ __global__ void k_pchb_derived(long long n, const double *bias, const double *pr
     }
 }
 
+// The interleaved records of the alias tables (AliasRec), from the arrays
+// above; slot i's target pair is tgt_pair[i + 1].
+__global__ void k_alias_rec(long long n, long long ab_max, const unsigned long long *thr, const double *prob,
+                            const double *inv, const int32_t *alias, const int32_t *tgt, AliasRec *out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        AliasRec r;
+        r.thr = thr[i];
+        r.prob = prob[i];
+        r.inv = inv[i];
+        r.alias = alias[i];
+        r.tgt = tgt[i % ab_max + 1];
+        out[i] = r;
+    }
+}
+
 // ---------------------------------------------------------------- launchers
 static int gsz(const Engine &e) { return e.num_sms * 4; }
 
@@ -411,6 +426,9 @@ void launch_pchb_build(Engine &e) {
     k_pchb_derived<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, e.sys.alias_bias, e.sys.alias_prob,
                                                  (unsigned long long *)e.sys.alias_thr, (float *)e.sys.alias_prob32,
                                                  (double *)e.sys.alias_inv, (float *)e.sys.alias_inv32);
+    k_alias_rec<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, n, e.sys.alias_thr, e.sys.alias_prob,
+                                              e.sys.alias_inv, e.sys.alias_alias, e.sys.tgt_pair,
+                                              (AliasRec *)e.sys.alias_rec);
     cudaStreamSynchronize(e.stream);
     cudaFree(wsum);
     cudaFree(scratch);
