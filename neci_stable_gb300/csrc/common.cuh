@@ -88,6 +88,17 @@ __device__ inline unsigned long long warp_append(unsigned long long *counter, un
     return base + incl - want;
 }
 
+// warp_append of at most one item per lane: the positions follow from a
+// ballot (the same as warp_append's for want in {0, 1}).
+__device__ inline unsigned long long warp_append1(unsigned long long *counter, bool want) {
+    const unsigned int lane = threadIdx.x & 31;
+    const unsigned int m = __ballot_sync(0xffffffffu, want);
+    unsigned long long base = 0;
+    if (lane == 31 && m) base = atomicAdd(counter, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
 __device__ inline void set_err(Control *c, int code) { atomicCAS(&c->err, 0, code); }
 
 __device__ inline void load_rh2(const DevSys &s, int32_t *sh) {

@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
         // append free slots
         {
             const unsigned int want = (hole || freed) ? 1u : 0u;
-            const unsigned long long pos = warp_append(&c->n_free, want);
+            const unsigned long long pos = warp_append1(&c->n_free, want != 0);
             if (want) st.free_list[pos] = (int32_t)j;
         }
         // one spawn-attempt entry per attempt; a parent with more than
@@ -639,7 +639,7 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
                 cand = true;
             }
         }
-        const unsigned long long pos = warp_append(&c->n_cand, cand ? 1u : 0u);
+        const unsigned long long pos = warp_append1(&c->n_cand, cand);
         if (cand) {
             st.cand[pos] = (uint32_t)i;
             st.cand_h[pos] = h;
@@ -702,7 +702,7 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
                 }
             }
         }
-        const unsigned long long pos = warp_append(&c->n_reps, won ? 1u : 0u);
+        const unsigned long long pos = warp_append1(&c->n_reps, won);
         if (won) {
             st.reps[pos] = (uint32_t)ci;
             st.rep_bucket[pos] = won_bucket;
@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                 }
             }
         }
-        const unsigned long long unused = warp_append(&c->n_new, inserted ? 1u : 0u);
+        const unsigned long long unused = warp_append1(&c->n_new, inserted);
         (void)unused;
         // H_jj - Hii and <D0|H|D_j> of the round's new determinants, computed
         // over a compacted list by consecutive threads: in place, the lanes

@@ -188,7 +188,7 @@ __device__ inline void create_particle(const DevSys &s, const DevState &st, cons
         if (P.pinit) atomicOr(&st.meta[j], 0x80000000u);
     }
     const bool rec = qv != 0 && (!fused || slot < 0);
-    const unsigned long long pos = warp_append(fused ? &st.ctl->n_cand : &st.ctl->n_spawned, rec ? 1u : 0u);
+    const unsigned long long pos = warp_append1(fused ? &st.ctl->n_cand : &st.ctl->n_spawned, rec);
     if (!rec) return;
     if (pos >= (unsigned long long)st.max_spawned) {
         set_err(st.ctl, NECI_GPU_ERR_SPAWN_FULL);
