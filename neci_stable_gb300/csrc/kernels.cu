@@ -604,14 +604,35 @@ template <int LR>
 __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
     if (halted(st)) return;
     extern __shared__ int32_t sh_rh2[];
+    // each warp gathers its candidates in shared memory and appends them to
+    // the global list when more than kWarpFlush are held (and at the end): an
+    // append per iteration would make every iteration wait for an atomic's
+    // round trip
+    constexpr int kWarpBuf = 256, kWarpFlush = kWarpBuf - 32;
+    __shared__ uint32_t sc_i[8][kWarpBuf];
+    __shared__ unsigned long long sc_h[8][kWarpBuf];
     load_rh2(s, sh_rh2);
     Control *c = st.ctl;
     const long long n = (long long)min(c->n_spawned, (unsigned long long)st.max_spawned);
     const int W = s.W, R = s.R;
     constexpr int L = LR;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;  // blockDim.x = 256
     unsigned long long aq[2] = {0, 0};
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
+    int wn = 0;  // the warp's buffered candidates, the same in every lane
+    auto flush = [&]() {
+        __syncwarp();
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&c->n_cand, (unsigned long long)wn);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (int k = lane; k < wn; k += 32) {
+            st.cand[base + k] = sc_i[wid][k];
+            st.cand_h[base + k] = sc_h[wid][k];
+        }
+        __syncwarp();
+        wn = 0;
+    };
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nround; i += stride) {
         bool cand = false;
         unsigned long long h = 0;
@@ -620,11 +641,9 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
             unsigned long long d[kMaxWords];
             NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
             long long q[2] = {0, 0};
-            NECI_FOR_RUNS(k, L) {
-                q[k] = rec[W + k];
-                aq[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
-            }
+            NECI_FOR_RUNS(k, L) q[k] = rec[W + k];
             const long long fl = rec[W + L];
+            NECI_FOR_RUNS(k, L) aq[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
             h = neci_hash(d, W, sh_rh2);
             const long long slot = hash_find(st, d, W, R, h, c);
             if (slot >= 0) {
@@ -639,12 +658,16 @@ __global__ void __launch_bounds__(256) k_ann_probe(DevSys s, DevState st) {
                 cand = true;
             }
         }
-        const unsigned long long pos = warp_append1(&c->n_cand, cand);
+        const unsigned int m = __ballot_sync(0xffffffffu, cand);
         if (cand) {
-            st.cand[pos] = (uint32_t)i;
-            st.cand_h[pos] = h;
+            const int k = wn + __popc(m & ((1u << lane) - 1u));
+            sc_i[wid][k] = (uint32_t)i;
+            sc_h[wid][k] = h;
         }
+        wn += __popc(m);
+        if (wn > kWarpFlush) flush();
     }
+    if (wn > 0) flush();
     unsigned long long *const dst[2] = {&c->abs_q[0], &c->abs_q[1]};
     block_add_u<2>(aq, dst);
 }
@@ -671,6 +694,25 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
     const unsigned long long mask = (hn < st.spawn_hash_n ? hn : st.spawn_hash_n) - 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
+    // each warp gathers the representatives it elects in shared memory and
+    // appends them when more than kWarpFlush are held (and at the end), so
+    // that an iteration does not wait for an atomic's round trip
+    constexpr int kWarpBuf = 256, kWarpFlush = kWarpBuf - 32;
+    __shared__ uint32_t sr_i[8][kWarpBuf], sr_b[8][kWarpBuf];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;  // blockDim.x = 256
+    int wn = 0;  // the warp's buffered representatives, the same in every lane
+    auto flush = [&]() {
+        __syncwarp();
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(&c->n_reps, (unsigned long long)wn);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        for (int k = lane; k < wn; k += 32) {
+            st.reps[base + k] = sr_i[wid][k];
+            st.rep_bucket[base + k] = sr_b[wid][k];
+        }
+        __syncwarp();
+        wn = 0;
+    };
     for (long long ci = blockIdx.x * (long long)blockDim.x + threadIdx.x; ci < nround; ci += stride) {
         bool won = false;
         uint32_t won_bucket = 0;
@@ -702,12 +744,16 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
                 }
             }
         }
-        const unsigned long long pos = warp_append1(&c->n_reps, won);
+        const unsigned int m = __ballot_sync(0xffffffffu, won);
         if (won) {
-            st.reps[pos] = (uint32_t)ci;
-            st.rep_bucket[pos] = won_bucket;
+            const int k = wn + __popc(m & ((1u << lane) - 1u));
+            sr_i[wid][k] = (uint32_t)ci;
+            sr_b[wid][k] = won_bucket;
         }
+        wn += __popc(m);
+        if (wn > kWarpFlush) flush();
     }
+    if (wn > 0) flush();
 }
 
 // ===========================================================================
@@ -727,6 +773,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
     long long a_tomb = 0;  // tombstones taken over by the insertions (a negative count)
+    unsigned long long a_new = 0;
     // the round's new determinants (blockDim.x = 128: four warps)
     __shared__ int nq_w[2][4];
     __shared__ long long q_slot[128];
@@ -844,8 +891,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                 }
             }
         }
-        const unsigned long long unused = warp_append1(&c->n_new, inserted);
-        (void)unused;
+        a_new += inserted ? 1ull : 0ull;
         // H_jj - Hii and <D0|H|D_j> of the round's new determinants, computed
         // over a compacted list by consecutive threads: in place, the lanes
         // without a new determinant would hold GB300's 1/64-rate FP64 pipe
@@ -886,9 +932,9 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                             &c->nborn[0], &c->nborn[1]};
     block_add<6>(v, dst, L);
-    unsigned long long u[3] = {a_s[0], a_s[1], (unsigned long long)a_tomb};  // two's complement for -count
-    unsigned long long *const du[3] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb};
-    block_add_u<3>(u, du);
+    unsigned long long u[4] = {a_s[0], a_s[1], (unsigned long long)a_tomb, a_new};  // two's complement for -count
+    unsigned long long *const du[4] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb, &c->n_new};
+    block_add_u<4>(u, du);
 }
 
 // ===========================================================================
