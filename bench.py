@@ -49,13 +49,13 @@ BLOOM = 3.0
 # of it on this workload (profiles/spawn_n24_pchb_2e6.md), reported beside its
 # HBM roofline.
 NCU_SPAWN_ISSUE = {"issue_active": 0.571, "alu_pipe": 0.563, "fp64_pipe": 0.398, "warps_active": 0.431,
-                   "lanes_per_instruction": 18.1, "dram_bytes_per_attempt": 14.5}
+                   "lanes_per_instruction": 18.1, "dram_bytes_per_attempt": 14.6}
 
 NCU_DRAM_BYTES_PER_UNIT = {
-    "spawn": (14.5, "n_attempts"),
-    "sweep": (47.3, "tot_walkers"),
-    "merge_stats": (37.7, "tot_walkers"),
-    "ann_probe": (99.9, "n_spawned"),
+    "spawn": (14.6, "n_attempts"),
+    "sweep": (47.2, "tot_walkers"),
+    "merge_stats": (38.3, "tot_walkers"),
+    "ann_probe": (102.3, "n_spawned"),
 }
 
 
