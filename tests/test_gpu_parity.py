@@ -30,6 +30,12 @@ SYSTEMS = {
     "mol64": lambda: molecule(64, 20),      # 128 spin orbitals: three det words
     "mol12u": lambda: molecule_uniform(12, 6),   # the uniform generator (gen_rand_excit)
     "mol40u": lambda: molecule_uniform(40, 12),
+    "mol32": lambda: molecule(32, 8),           # 64 spin orbitals: one orbital word in two row words
+    "mol32u": lambda: molecule_uniform(32, 8),
+    "mol80u": lambda: molecule_uniform(80, 10),  # 160 spin orbitals: three words
+    "hub4x8": lambda: hubbard_square(4, 8, 16),
+    "hub8x10": lambda: hubbard_square(8, 10, 20),
+    "hub10x10": lambda: hubbard_square(10, 10, 20),  # 200 spin orbitals: four words (the any-size instance)
 }
 
 _cache = {}
@@ -186,6 +192,45 @@ def test_iterations_integer_walkers_and_mixed():
 def test_spawn_instances_bit_exact(name, ps):
     st = run_pair(name, 12, 100.0, 0.01, p_singles=ps)
     assert st.n_spawned > 0
+
+
+# The remaining word-count instances of the spawn kernel, for the molecular
+# generators and the lattice one: one orbital word in two row words (64 spin
+# orbitals), three words (160), and the instance for any size (200, four words)
+@pytest.mark.parametrize("name,pop,tau", [("mol32", 500.0, 0.05), ("mol32u", 500.0, 0.05), ("mol80u", 500.0, 0.05),
+                                          ("hub4x8", 40.0, 0.01), ("hub8x10", 40.0, 0.01), ("hub10x10", 40.0, 0.01)])
+def test_word_count_instances_bit_exact(name, pop, tau):
+    st = run_pair(name, 10, pop, tau)
+    assert st.n_occupied > 1
+
+
+def test_empty_list_and_steps_without_spawns():
+    """A step on an empty walker list: no error, zero counts, an empty list.
+    Steps in which nothing spawns (tau so small that every amplitude rounds
+    to zero): the list still dies by the oracle's rules."""
+    spec, eng, orc = pair("mol12", 400_000, 800_000)
+    W, L = spec.W, spec.lenof_sign
+    empty = np.zeros((0, W + L + 1), dtype=np.int64)
+    eng.upload(empty)
+    orc.upload(empty)
+    p = capi.default_params(tau=0.01, seed=3, iter=1)
+    sg = eng.perform_fcimc_cyc_par(p)
+    sc, rc = orc.iterate(p)
+    assert rc == 0 and sg.err == 0
+    assert sg.n_attempts == 0 == sc.n_attempts and sg.n_spawned == 0 and sg.n_occupied == 0
+    assert sg.tot_parts[0] == 0.0 == sc.tot_parts[0]
+    assert eng.download()[0].shape[0] == 0
+    eng.start_from_reference(initial_part=50.0)
+    orc.upload(eng.download()[0])
+    for it in range(1, 4):
+        p = capi.default_params(tau=1e-12, seed=3, iter=it)
+        sg = eng.perform_fcimc_cyc_par(p)
+        sc, rc = orc.iterate(p)
+        assert rc == 0 and sg.err == 0
+        assert sg.n_attempts > 0 and sg.n_spawned == 0 == sc.n_spawned
+        rg = canonical(eng.download()[0], W)
+        rcpu = canonical(orc.download()[0], W)
+        assert np.array_equal(rg[:, : W + L], rcpu[:, : W + L]), it
 
 
 # AvMCExcits != 1: decide_num_to_spawn in FP64 (the sweep's general instance)
