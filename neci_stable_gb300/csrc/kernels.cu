@@ -468,19 +468,33 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
         }
         // the signs just written are all zero
         const bool freed = live && occ && !core && out_zero;
-        // append free slots
-        {
-            const unsigned int want = (hole || freed) ? 1u : 0u;
-            const unsigned long long pos = warp_append1(&c->n_free, want != 0);
-            if (want) st.free_list[pos] = (int32_t)j;
-        }
-        // one spawn-attempt entry per attempt; a parent with more than
+        // The round's two appends, free slots and spawn-attempt entries: both
+        // atomics are issued before either result is read, so that their
+        // round trips overlap.  One entry per attempt; a parent with more than
         // kBigAttempts attempts is handed to k_expand, which writes its
-        // entries with a whole block
+        // entries with a whole block.
         {
+            const int lane = threadIdx.x & 31;
+            const bool want = hole || freed;
+            const unsigned int mf = __ballot_sync(0xffffffffu, want);
             unsigned int nat = 0;
             NECI_FOR_RUNS(k, L) nat += nsp[k];
-            const unsigned long long base = warp_append(&c->n_att, nat);
+            unsigned int incl = nat;  // inclusive scan of the warp's attempts
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const unsigned int tot = __shfl_sync(0xffffffffu, incl, 31);
+            unsigned long long bf = 0, ba = 0;
+            if (lane == 31) {
+                if (mf) bf = atomicAdd(&c->n_free, (unsigned long long)__popc(mf));
+                if (tot) ba = atomicAdd(&c->n_att, (unsigned long long)tot);
+            }
+            bf = __shfl_sync(0xffffffffu, bf, 31);
+            ba = __shfl_sync(0xffffffffu, ba, 31);
+            if (want) st.free_list[bf + __popc(mf & ((1u << lane) - 1u))] = (int32_t)j;
+            const unsigned long long base = ba + incl - nat;
             if (nat) {
                 if (base + nat > (unsigned long long)st.max_att) {
                     set_err(c, NECI_GPU_ERR_SPAWN_FULL);
