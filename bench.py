@@ -208,6 +208,20 @@ def algorithmic_bytes(kernel, st, W, L, nnz=0, fused=True):
     return 0
 
 
+def combine_ranks(updates, dev_s, e2e_updates, e2e_s, device="cuda"):
+    """The whole job's figures from N replicas (one per GPU, no collective on
+    the data path): walker updates summed over the ranks, times the slowest
+    rank's.  Returns (updates, device seconds, e2e updates, e2e seconds)."""
+    import torch
+    import torch.distributed as dist
+    s = torch.tensor([updates, dev_s, e2e_updates, e2e_s], dtype=torch.float64, device=device)
+    dist.all_reduce(s[0:1], op=dist.ReduceOp.SUM)
+    dist.all_reduce(s[2:3], op=dist.ReduceOp.SUM)
+    dist.all_reduce(s[1:2], op=dist.ReduceOp.MAX)
+    dist.all_reduce(s[3:4], op=dist.ReduceOp.MAX)
+    return tuple(float(x) for x in s.tolist())
+
+
 def run_gpu(args, rank, world):
     import numpy as np
     from neci_stable_gb300 import capi
@@ -605,15 +619,7 @@ def main():
     updates = r["updates"]
     e2e_upd, e2e_s = r["e2e_updates"], r["e2e_s"]
     if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([updates, dev_s, e2e_upd, e2e_s], dtype=torch.float64, device="cuda")
-        s = t.clone()
-        dist.all_reduce(s[0:1], op=dist.ReduceOp.SUM)
-        dist.all_reduce(s[2:3], op=dist.ReduceOp.SUM)
-        dist.all_reduce(s[1:2], op=dist.ReduceOp.MAX)
-        dist.all_reduce(s[3:4], op=dist.ReduceOp.MAX)
-        updates, dev_s, e2e_upd, e2e_s = (float(x) for x in s.tolist())
+        updates, dev_s, e2e_upd, e2e_s = combine_ranks(updates, dev_s, e2e_upd, e2e_s)
     if rank != 0:
         dist.destroy_process_group()
         return
