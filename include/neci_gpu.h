@@ -170,9 +170,20 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx);
 /* ---- walker list transfer (POPSFILE read/write, host estimators) ------
  * Upload replaces CurrentDets: `ilut` holds nrows rows in CurrentDets layout;
  * diag_h (H_jj - Hii) and offdiag_h (<D0|H|D_j>) may be NULL, in which case
- * the device computes them (get_diagonal_matel / get_off_diagonal_matel). */
+ * the device computes them (get_diagonal_matel / get_off_diagonal_matel).
+ * Every row's determinant must hold nel electrons among the nBasis spin
+ * orbitals (NECI's EncodeBitDet of an nI array, BitReps.F90:75); a row that
+ * does not is refused with NECI_GPU_ERR_INVALID before anything is copied. */
 int32_t neci_gpu_upload_walkers(neci_gpu_ctx *ctx, const int64_t *ilut, int64_t nrows,
                                 const double *diag_h, const double *offdiag_h);
+/* The check the upload applies, on the host and without a context: the index
+ * of the first of nrows rows (nifd+1 determinant words, lenof_sign signs and
+ * a flag word each) whose determinant does not hold exactly nel set bits
+ * below bit nbasis, or -1 when every row does (or the arguments are out of
+ * range: nifd 0..3, lenof_sign 1..2, nrows >= 0, and ilut non-NULL for
+ * nrows > 0; those give -2). */
+int64_t neci_gpu_check_rows(const int64_t *ilut, int64_t nrows, int32_t nifd, int32_t lenof_sign,
+                            int32_t nel, int32_t nbasis);
 /* Downloads the occupied rows (holes skipped) into `ilut` (max_rows rows) and,
  * if non-NULL, their diag_h/offdiag_h.  *nrows receives the row count.    */
 int32_t neci_gpu_download_walkers(neci_gpu_ctx *ctx, int64_t *ilut, double *diag_h,

@@ -132,6 +132,7 @@ _SIGS = {
     "neci_gpu_get_rdm": (_i32, [_P, _P, _i64, _i32]),
     "neci_gpu_upload_walkers": (_i32, [_P, _P, _i64, _P, _P]),
     "neci_gpu_download_walkers": (_i32, [_P, _P, _P, _P, _i64, _P]),
+    "neci_gpu_check_rows": (_i64, [_P, _i64, _i32, _i32, _i32, _i32]),
     "neci_gpu_iterate": (_i32, [_P, C.POINTER(IterParams), C.POINTER(IterStats)]),
     "neci_gpu_iterate_n": (_i32, [_P, C.POINTER(IterParams), _i32, _P]),
     "neci_gpu_iterate_timed": (_i32, [_P, C.POINTER(IterParams), _i32, _P, _P]),

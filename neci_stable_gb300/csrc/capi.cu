@@ -629,6 +629,27 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
     return NECI_GPU_OK;
 }
 
+int64_t neci_gpu_check_rows(const int64_t *ilut, int64_t nrows, int32_t nifd, int32_t lenof_sign, int32_t nel,
+                            int32_t nbasis) {
+    if (nrows < 0 || (nrows > 0 && !ilut) || nifd < 0 || nifd + 1 > kMaxWords || lenof_sign < 1 || lenof_sign > 2)
+        return -2;
+    const int W = nifd + 1, R = W + lenof_sign + 1;
+    for (int64_t j = 0; j < nrows; ++j) {
+        const int64_t *r = ilut + (size_t)j * R;
+        int n = 0;
+        bool outside = false;
+        for (int w = 0; w < W; ++w) {
+            const unsigned long long x = (unsigned long long)r[w];
+            const int below = nbasis - 64 * w;  // orbitals this word may hold
+            if (below <= 0) outside |= x != 0;
+            else if (below < 64) outside |= (x >> below) != 0;
+            n += __builtin_popcountll(x);
+        }
+        if (outside || n != nel) return j;
+    }
+    return -1;
+}
+
 int32_t neci_gpu_upload_walkers(neci_gpu_ctx *ctx, const int64_t *ilut, int64_t nrows, const double *dh,
                                 const double *odh) {
     if (int r = check_ctx(ctx)) return r;
@@ -636,6 +657,11 @@ int32_t neci_gpu_upload_walkers(neci_gpu_ctx *ctx, const int64_t *ilut, int64_t 
     if (!ilut && nrows > 0) return fail(NECI_GPU_ERR_INVALID, "null rows");
     if (nrows < 0 || nrows >= e.st.max_walkers) return fail(NECI_GPU_ERR_LIST_FULL, "more rows than MaxWalkersPart - 1");
     if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
+    // a determinant with the wrong electron count, or an orbital past nBasis,
+    // would index the integral and lattice tables out of range on the device
+    if (const int64_t bad = neci_gpu_check_rows(ilut, nrows, e.sys.W - 1, e.sys.L, e.sys.nel, e.sys.nbasis); bad != -1)
+        return fail(NECI_GPU_ERR_INVALID, "upload: row " + std::to_string(bad) +
+                                              " does not hold nel electrons among the nBasis orbitals");
     const int R = e.sys.R;
     CK(cudaMemsetAsync(e.st.dets, 0, (size_t)e.st.max_walkers * R * 8, e.stream));
     CK(cudaMemsetAsync(e.st.hash, 0, (size_t)e.st.hash_n * 4, e.stream));

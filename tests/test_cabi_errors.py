@@ -10,10 +10,12 @@ from __future__ import annotations
 import ctypes as C
 import re
 from pathlib import Path
+from types import SimpleNamespace
 
+import numpy as np
 import pytest
 
-from neci_stable_gb300 import capi
+from neci_stable_gb300 import capi, systems
 
 ROOT = Path(__file__).resolve().parents[1]
 HEADER = ROOT / "include" / "neci_gpu.h"
@@ -161,3 +163,65 @@ def test_kernel_names(lib):
     assert all(names) and len(set(names)) == n
     assert {"spawn", "sweep", "ann_probe", "ann_insert", "merge_stats"} <= set(names)
     assert lib.neci_gpu_kernel_name(-1) == b"" and lib.neci_gpu_kernel_name(n) == b""
+
+
+def _check(lib, rows, nifd, lenof_sign, nel, nbasis):
+    rows = np.ascontiguousarray(rows, dtype=np.int64)
+    return lib.neci_gpu_check_rows(rows.ctypes.data_as(C.c_void_p), rows.shape[0], nifd, lenof_sign, nel, nbasis)
+
+
+@pytest.mark.parametrize("name", ["hub4x8", "mol24", "mol80u"])
+def test_upload_row_check_accepts_every_valid_determinant(lib, name):
+    from helpers import make_rows, random_dets
+    spec = {"hub4x8": lambda: systems.hubbard_system("square", (4, 8), 32, u=4.0),
+            "mol24": lambda: _fake_molecule(48, 10, 0),
+            "mol80u": lambda: _fake_molecule(160, 20, 2)}[name]()
+    rng = np.random.default_rng(1)
+    dets = random_dets(spec, 500, rng)
+    signs = np.zeros((dets.shape[0], spec.lenof_sign))
+    signs[::2, 0] = 3.0                      # zero-sign rows (holes) are uploaded too
+    rows = make_rows(dets, signs, np.zeros(dets.shape[0], dtype=np.int64))
+    assert _check(lib, rows, spec.nifd, spec.lenof_sign, spec.nel, spec.nbasis) == -1
+    assert _check(lib, rows[:0], spec.nifd, spec.lenof_sign, spec.nel, spec.nbasis) == -1
+
+
+def _fake_molecule(nbasis, nel, nifd):
+    # the check needs only the layout: nel electrons, nBasis, NIfD, a reference
+    ref = list(range(1, nel + 1))
+    return SimpleNamespace(nbasis=nbasis, nel=nel, nifd=nifd, W=nifd + 1, lenof_sign=1, reference=ref)
+
+
+def test_upload_row_check_finds_the_first_bad_row(lib):
+    from helpers import make_rows
+    nifd, nel, nbasis = 2, 20, 160
+    good = systems.encode_det(list(range(1, nel + 1)), nifd)
+    rows = make_rows(np.repeat(good[None], 6, axis=0), np.ones((6, 1)), np.zeros(6, dtype=np.int64))
+    assert _check(lib, rows, nifd, 1, nel, nbasis) == -1
+    few = rows.copy()
+    few[3, 0] &= ~1                          # one electron short
+    assert _check(lib, few, nifd, 1, nel, nbasis) == 3
+    many = rows.copy()
+    many[4, 1] |= 1 << 5                     # one electron too many
+    assert _check(lib, many, nifd, 1, nel, nbasis) == 4
+    past = rows.copy()
+    past[2, 0] &= ~1
+    past[2, 2] = 1 << 40                     # orbital 169 > nBasis, count still nel
+    assert _check(lib, past, nifd, 1, nel, nbasis) == 2
+    edge = rows.copy()
+    edge[1, 0] &= ~1
+    edge[1, 2] = 1 << 31                     # orbital 160 = nBasis: allowed
+    assert _check(lib, edge, nifd, 1, nel, nbasis) == -1
+    # flags and signs do not count
+    rows[:, -1] = -1
+    rows[:, nifd + 1] = -1
+    assert _check(lib, rows, nifd, 1, nel, nbasis) == -1
+
+
+def test_upload_row_check_arguments(lib):
+    rows = np.zeros((2, 3), dtype=np.int64)
+    assert _check(lib, rows, -1, 1, 2, 64) == -2
+    assert _check(lib, rows, 4, 1, 2, 64) == -2
+    assert _check(lib, rows, 0, 3, 2, 64) == -2
+    assert lib.neci_gpu_check_rows(None, 1, 0, 1, 2, 64) == -2
+    assert lib.neci_gpu_check_rows(None, -1, 0, 1, 2, 64) == -2
+    assert lib.neci_gpu_check_rows(None, 0, 0, 1, 2, 64) == -1
