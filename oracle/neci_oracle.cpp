@@ -1774,6 +1774,21 @@ int32_t orc_get_tau_stats(void *h, neci_gpu_tau_stats *out, int32_t reset) {
 int32_t orc_upload_walkers(void *h, const int64_t *ilut, int64_t nrows, const double *dh, const double *odh) {
     Oracle *o = (Oracle *)h;
     if (nrows >= o->sys.max_walkers) return NECI_GPU_ERR_LIST_FULL;
+    // the engine's upload refuses the same rows: nel electrons below nBasis
+    for (int64_t j = 0; j < nrows; ++j) {
+        const int64_t *r = ilut + (size_t)j * o->R;
+        int n = 0;
+        for (int w = 0; w < o->W; ++w) {
+            const u64 x = (u64)r[w];
+            const int below = o->sys.nbasis - 64 * w;
+            if ((below <= 0 && x) || (below > 0 && below < 64 && (x >> below))) n = -1;
+            if (n >= 0) n += Oracle::popc(x);
+        }
+        if (n != o->sys.nel) {
+            g_err = "upload: row " + std::to_string(j) + " does not hold nel electrons among the nBasis orbitals";
+            return NECI_GPU_ERR_INVALID;
+        }
+    }
     for (auto &b : o->HashIndex) b.clear();
     std::fill(o->CurrentDets.begin(), o->CurrentDets.end(), 0);
     std::memcpy(o->CurrentDets.data(), ilut, (size_t)nrows * o->R * 8);

@@ -72,3 +72,17 @@ def test_full_core_step_is_the_dense_projection(make):
     assert st.enum_cyc[0] == pytest.approx(enum, rel=1e-12, abs=1e-12)
     assert st.tot_parts_old[0] == pytest.approx(np.abs(c).sum(), rel=1e-14)
     assert st.tot_parts[0] == pytest.approx(np.abs(expect).sum(), rel=1e-12)
+
+
+def test_upload_refuses_a_determinant_without_nel_electrons():
+    # a 4-site chain cannot hold a Neel reference of 8 electrons: the row has 4
+    spec = systems.hubbard_system("chain", (4,), 8, u=4.0)
+    W = spec.W
+    orc = Oracle(spec, 64, 64)
+    rows = np.zeros((1, W + 2), dtype=np.int64)
+    rows[0, :W] = systems.encode_det(list(range(1, 5)), spec.nifd)
+    rows[0, W] = np.array([10.0]).view(np.int64)[0]
+    with pytest.raises(RuntimeError, match="does not hold nel electrons"):
+        orc.upload(rows)
+    rows[0, :W] = systems.encode_det(list(range(1, 9)), spec.nifd)
+    orc.upload(rows)
