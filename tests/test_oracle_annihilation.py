@@ -136,3 +136,19 @@ def test_compression_alone_matches_the_rules():
     # sorted by ilut_lt (DetBitOps.F90:431): signed 64-bit words, first word first
     keys = [tuple(int(x) for x in r[:W]) for r in out]
     assert keys == sorted(keys)
+
+
+def test_compressed_list_sorts_by_signed_words():
+    # 32 sites: spin orbital 64 is bit 63 of the first word, so half the
+    # determinants have a negative first word; ilut_lt compares signed int64
+    from helpers import random_dets
+    spec = systems.hubbard_system("square", (4, 8), 32, u=4.0)
+    W = spec.W
+    orc = Oracle(spec, 8192, 65536)
+    rng = np.random.default_rng(9)
+    dets = random_dets(spec, 400, rng)
+    assert (dets[:, 0] < 0).any() and (dets[:, 0] > 0).any()
+    spawned = _rows(dets, np.ones(dets.shape[0]), 0, W)
+    out, _ = orc.compress_spawns(capi.default_params(), spawned)
+    keys = [tuple(int(x) for x in r[:W]) for r in out]
+    assert keys == sorted(set(tuple(int(x) for x in d) for d in dets))
