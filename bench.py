@@ -205,6 +205,21 @@ def algorithmic_bytes(kernel, st, W, L, nnz=0, fused=True):
         return N * (R + G + 4)
     if kernel == "merge_stats":
         return slots * (R + 12 * L)
+    # the sort form of the annihilation (NECI_ANN_SORT)
+    if kernel == "sort_keys":
+        # per record: its determinant words and amplitudes read, key, index
+        # and 64-bit hash written
+        return S * (8 * (W + L) + 16)
+    if kernel == "sort_radix":
+        # 4 passes of 8 bits over (32-bit key, 32-bit index): the count pass
+        # reads the key, the scatter reads and writes key and index
+        return S * 4 * (4 + 16)
+    if kernel == "sort_group":
+        # per record: key, its neighbour's key and the index read, the record
+        # gathered; per unique determinant: the hash probe (bucket and row
+        # words) and its sums written (acc/meta, or a new determinant's
+        # candidate entry)
+        return S * (12 + R) + U * (4 + 8 * W + 12 * L) + N * (24 + 12 * L)
     return 0
 
 
@@ -283,13 +298,10 @@ def run_gpu(args, rank, world):
         t0 = time.perf_counter()
         st0 = eng.iterate_n(drv.params(), 1)[0]
         drv.iter += 1
-        rows = eng.download(max_rows=int(st0.tot_walkers) + 1)[0]
-        W, L = spec.W, spec.lenof_sign
-        pop = np.abs(rows[:, W:W + L].view(np.float64)).sum(axis=1)
-        n_core = min(wl["core"], rows.shape[0])
-        core = rows[np.argsort(-pop, kind="stable")[:n_core], :W]
-        eng.set_core_space(core, capi.PREC_FP64)
-        core_info = {"n_core": n_core, "nnz": eng.core_nnz(), "set_up_s": time.perf_counter() - t0}
+        # selected on the device (neci_gpu_select_core): no download of the list
+        core = eng.select_core(wl["core"], capi.PREC_FP64)
+        core_info = {"n_core": int(core.shape[0]), "nnz": eng.core_nnz(), "set_up_s": time.perf_counter() - t0,
+                     "selection": "device (neci_gpu_select_core)"}
         drv.run(20)
     p = drv.params()
     # warm-up steps (untimed)
@@ -353,13 +365,42 @@ def run_gpu(args, rank, world):
         den = np.array([sum(x.hf_cyc[0] for x in sts[k:k + 10]) for k in range(0, len(sts), 10)])
         e, err = analysis.projected_energy(num, den, eng.hii) if len(num) >= 2 else (float(num.sum() / den.sum()) + eng.hii, None)
         proje[name] = {"e_proj": e, "err": err}
-    # ---- per-kernel timing pass (events around each kernel; not the timed number)
-    eng.set_profiling(True)
-    prof_stats = eng.iterate_n(p, 3)
+    # ---- per-kernel timing passes (events around each kernel; not the timed
+    # number): FP64, then the mixed-precision step
+    def profile(prec, n=3):
+        pp = drv_params_like(p, prec)
+        eng.set_profiling(True)
+        st = eng.iterate_n(pp, n)
+        p.iter += n
+        kt = eng.kernel_times()
+        eng.set_profiling(False)
+        return kt, st[-1].as_dict()
+
+    def drv_params_like(base, prec):
+        q = capi.default_params()
+        for name, _ in capi.IterParams._fields_:
+            setattr(q, name, getattr(base, name))
+        q.precision = prec
+        return q
+
+    ktimes, last = profile(capi.PREC_FP64)
+    ktimes_mixed, last_mixed = profile(capi.PREC_MIXED)
+    # ---- the sort form of the annihilation (NECI_ANN_SORT) on the same
+    # population: K steps timed alone as above, then a profiling pass
+    eng.set_option(capi.OPT_ANNIHILATION, capi.ANN_SORT)
+    eng.iterate_n(p, 3)
     p.iter += 3
-    ktimes = eng.kernel_times()
-    eng.set_profiling(False)
-    last = prof_stats[-1].as_dict()
+    sort_upd, sort_ms = 0.0, 0.0
+    for _ in range(args.steps):
+        flush.fill_(float(k))
+        k += 1
+        torch.cuda.synchronize()
+        st1, ms = eng.iterate_timed(p, 1)
+        p.iter += 1
+        sort_upd += st1[0].tot_parts_old[0]
+        sort_ms += ms
+    ktimes_sort, last_sort = profile(capi.PREC_FP64)
+    eng.set_option(capi.OPT_ANNIHILATION, capi.ANN_HASH)
     return {
         "eng": eng, "spec": spec, "tau": tau, "tau_info": tau_info, "core_info": core_info, "proje": proje,
         "scale_info": scale_info,
@@ -367,7 +408,8 @@ def run_gpu(args, rank, world):
         "e2e_updates": e2e_updates, "e2e_s": e2e_s, "ktimes": ktimes, "last": last, "stats": stats,
         "first": stats[0].as_dict(),
         "equil": equil, "mixed_updates": mixed_updates, "mixed_ms": mixed_ms, "bb_updates": bb_updates,
-        "bb_ms": bb_ms,
+        "bb_ms": bb_ms, "ktimes_mixed": ktimes_mixed, "last_mixed": last_mixed, "ktimes_sort": ktimes_sort,
+        "last_sort": last_sort, "sort_updates": sort_upd, "sort_ms": sort_ms,
     }
 
 
@@ -401,6 +443,8 @@ def run_batched(args):
     for i, (spec, walkers) in enumerate(specs):
         eng = Engine(spec, max_walkers=int(max(6 * walkers, 1e5)), max_spawned=int(max(6 * walkers, 2e5)))
         eng.start_from_reference(initial_part=walkers)
+        # each instance is a replica pair sampling the 2-RDM in every step
+        eng.set_rdm_sampling(True)
         tau = min(0.02, estimate_tau(eng, 20_000))
         p = capi.default_params(tau=tau, seed=SEED + i, iter=1)
         engines.append(eng)
@@ -444,12 +488,14 @@ def run_batched(args):
         e.close()
     v_single = fp64_upd / (fp64_ms / 1e3)
     v_mixed = mixed_upd / (mixed_ms / 1e3)
-    return {"instances": len(specs), "steps": K, "unit": UNIT,
-            "fp64_single_instance": v_single, "fp64_batched": fb_upd / (fb_ms / 1e3), "mixed_batched": v_mixed,
+    v_fb = fb_upd / (fb_ms / 1e3)
+    return {"instances": len(specs), "steps": K, "unit": UNIT, "rdm": True,
+            "fp64_single_instance": v_single, "fp64_batched": v_fb, "mixed_batched": v_mixed,
             "speedup_mixed_batched_vs_fp64_single": v_mixed / v_single,
+            "speedup_mixed_batched_vs_fp64_batched": v_mixed / v_fb,
             "walkers_total": sum(w for _, w in specs),
             "workload": "64 synthetic FCIDUMP instances (instance-indexed seeds), n 12..40, nel 6..20, "
-                        "walkers 1e4..1e6 log-uniform, replica pairs, PCHB"}
+                        "walkers 1e4..1e6 log-uniform, replica pairs sampling the 2-RDM every step, PCHB"}
 
 
 class OracleSample:
@@ -646,6 +692,20 @@ def main():
     ann = tuple(k for k in ("ann_probe", "ann_compress", "ann_insert") if k in kt)
     ann_ms = sum(kt[k][0] / kt[k][1] for k in ann)
     ann_bytes = sum(algorithmic_bytes(k, r["last"], W, L) for k in ann)
+    # the sort form of the annihilation: per stage (keys, the 4 radix passes,
+    # grouping + walker-hash lookup) and the insertion of new determinants
+    kts = {k: v for k, v in r["ktimes_sort"].items() if v[1] > 0}
+    sort_stages = {}
+    for k in ("sort_keys", "sort_radix", "sort_group", "ann_insert"):
+        if k not in kts:
+            continue
+        ms = kts[k][0] / kts[k][1]
+        b = algorithmic_bytes(k, r["last_sort"], W, L)
+        sort_stages[k] = {"ms": ms, "algorithmic_bytes": b, "gbs": b / (ms / 1e3) / 1e9,
+                          "frac": b / (ms / 1e3) / 1e9 / hbm}
+    sort_ms = sum(v["ms"] for v in sort_stages.values())
+    sort_bytes = sum(v["algorithmic_bytes"] for v in sort_stages.values())
+    ktm = {k: v for k, v in r["ktimes_mixed"].items() if v[1] > 0}
     launches_per_step = 15 + (1 if r["last"]["n_core"] > 0 else 0) + (0 if fused else 1)
     line = {
         "metric": METRIC, "value": updates / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -677,7 +737,15 @@ def main():
                                   "unit": "GB/s", "frac": ann_bytes / (ann_ms / 1e3) / 1e9 / hbm,
                                   "ms_per_step": ann_ms, "algorithmic_bytes": ann_bytes},
         "kernel_ms_per_step": {k: v[0] / v[1] for k, v in kt.items()},
+        "kernel_ms_per_step_mixed": {k: v[0] / v[1] for k, v in ktm.items()},
         "kernel_gbs": kernel_gbs,
+        "sort_annihilation": {
+            "value": r["sort_updates"] / (r["sort_ms"] / 1000.0), "unit": UNIT,
+            "ms_per_step": r["sort_ms"] / args.steps,
+            "stages": sort_stages, "ms_per_step_annihilation": sort_ms,
+            "annihilation_frac": sort_bytes / (sort_ms / 1e3) / 1e9 / hbm if sort_ms > 0 else None,
+            "note": "NECI_ANN_SORT on the same population: spawns radix-sorted by a 32-bit key of their "
+                    "determinant's hash and reduced as runs; the hash form is the default"},
         "proje": r["proje"],
         "mixed_precision": {"value": r["mixed_updates"] / (r["mixed_ms"] / 1000.0), "unit": UNIT,
                             "ms_per_step": r["mixed_ms"] / args.steps,
@@ -687,6 +755,8 @@ def main():
     }
     if not args.no_batched and world == 1 and args.workload == "n24":
         line["batched"] = run_batched(args)
+        # against the headline: the FP64 single instance of the 1e7-walker molecule
+        line["batched"]["speedup_mixed_batched_vs_n24_fp64"] = line["batched"]["mixed_batched"] / line["value"]
     if not args.no_cpu_baseline and world == 1 and args.workload == "n24":
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))

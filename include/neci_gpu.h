@@ -272,7 +272,9 @@ int32_t neci_gpu_annihilate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *param
 /* CompressSpawnedList alone: the compressed list (one row per surviving
  * determinant, sorted by ilut_lt, DetBitOps.F90:431) is written to `out`
  * (n_spawned rows at most); *n_out gets its length, nannihil (lenof_sign
- * doubles) the annihilation count of the compression.                    */
+ * doubles) the annihilation count of the compression.  The flag rules use
+ * tTruncInitiator and tInitCoherentRule of the parameters the context was
+ * last given (by a step or neci_gpu_annihilate; both on before the first). */
 int32_t neci_gpu_compress_spawns(neci_gpu_ctx *ctx, const int64_t *spawned, int64_t n_spawned,
                                  int64_t *out, int64_t *n_out, double *nannihil);
 
@@ -298,7 +300,9 @@ int32_t neci_gpu_compress_spawns(neci_gpu_ctx *ctx, const int64_t *spawned, int6
  * device addresses of the scratch arrays (cudaGetSymbolAddress) and should
  * come before any stream capture.  Every call on a device shares the same
  * scratch: it is cleared at the start of each call, and calls that overlap on
- * the GPU race. */
+ * the GPU race, so a caller with several streams or threads serialises them.
+ * The looked-up addresses are kept for the life of the process: after a
+ * cudaDeviceReset the entry point must not be called again. */
 int32_t neci_gpu_compress_spawns_noalloc(const int64_t *d_spawned, int64_t n, int32_t nifd,
                                          int32_t lenof_sign, int32_t t_trunc_initiator,
                                          int32_t t_init_coherent_rule, int64_t *d_out, int64_t *n_out,
@@ -334,8 +338,67 @@ int32_t neci_gpu_gen_excit(neci_gpu_ctx *ctx, const int64_t *det, int64_t n_samp
  * with compensated accumulation when precision == NECI_PREC_MIXED.       */
 int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core_dets, int64_t n_core,
                                 int32_t precision);
+/* Selects the core space on the device and sets it as neci_gpu_set_core_space
+ * does: the min(n_core, occupied) determinants of CurrentDets with the largest
+ * weight sum over runs of |C| (core_space_weight, semi_stoch_procs.F90:1623-1642,
+ * in proc_most_populated_states, :1310-1421), in order of decreasing weight.
+ * Among equal weights the lower slot wins, as NECI's strict ">" keeps the
+ * first determinant it meets.  core_dets (may be NULL) receives the selected
+ * determinants (nifd+1 words each, room for n_core rows) and *n_selected
+ * (may be NULL) their number.                                              */
+int32_t neci_gpu_select_core(neci_gpu_ctx *ctx, int64_t n_core, int32_t precision, int64_t *core_dets,
+                             int64_t *n_selected);
 /* Number of stored off-diagonal core Hamiltonian elements. */
 int32_t neci_gpu_core_nnz(neci_gpu_ctx *ctx, int64_t *nnz);
+
+/* ---- engine variants ------------------------------------------------------
+ * Options that choose how a step is computed, never what it computes: the
+ * walker lists and estimators are the same bit for bit under every setting.
+ * They have no counterpart in the reference, whose one CPU path has no such
+ * choice; the reference routine each variant restates is named below.  A
+ * change takes effect from the next step.                                 */
+#define NECI_OPT_FUSE_PROBE   0  /* lattice systems: look every child up in the walker
+                                    hash inside the spawn kernel (hash_table_lookup,
+                                    hash.F90:294).  -1 (default): chosen from the last
+                                    step's spawn rate; 0: never; 1: always.  Only with
+                                    the hash annihilation and without 2-RDM sampling */
+#define NECI_OPT_ANNIHILATION 1  /* NECI_ANN_HASH (default) or NECI_ANN_SORT           */
+#define NECI_ANN_HASH 0  /* spawns looked up in the walker hash, the others merged in an
+                            open-addressing table                                    */
+#define NECI_ANN_SORT 1  /* spawns radix-sorted by a key of their determinant and
+                            equal determinants reduced as runs: CompressSpawnedList's
+                            sort and FindResidualParticle (Annihilation.F90:273,
+                            551-634)                                                  */
+int32_t neci_gpu_set_option(neci_gpu_ctx *ctx, int32_t option, int32_t value);
+
+/* ---- autotuning -----------------------------------------------------------
+ * The launch shapes and the annihilation form of a context, which change the
+ * speed of a step and never its results.  No counterpart in the reference,
+ * whose CPU loop has no such settings.                                    */
+typedef struct {
+    int32_t annihilation;         /* NECI_ANN_HASH or NECI_ANN_SORT                            */
+    int32_t spawn_blocks_per_sm;  /* blocks of 128 threads per SM in the spawn kernel's grid,
+                                     1..8 (8: every block the registers allow)                 */
+    int32_t table_shift;          /* hash form: the compression table of a step holds at least
+                                     2^table_shift buckets per spawn onto an absent
+                                     determinant (load factor 2^-table_shift), 1..4            */
+    int32_t sort_blocks_per_sm;   /* sort form: blocks per SM of a radix pass, 1..4 (each
+                                     block sorts a chunk of the spawn list)                    */
+    double  ns_per_update;        /* autotuning: device ns per walker update it measured       */
+    int32_t reserved[2];
+} neci_gpu_tuning;
+int32_t neci_gpu_set_tuning(neci_gpu_ctx *ctx, const neci_gpu_tuning *tuning);
+int32_t neci_gpu_get_tuning(neci_gpu_ctx *ctx, neci_gpu_tuning *tuning);
+/* Times a fixed list of settings on live steps and keeps the fastest: for
+ * each setting one step (which captures its step graph) and then
+ * steps_per_setting steps timed by CUDA events, whose cost is device time per
+ * walker update (TotParts entering the steps).  The steps are ordinary steps
+ * of the run, the same under every setting, from params->iter on: stats
+ * (max_stats records) receives them and *n_steps their number, by which the
+ * caller advances its iteration count.  *chosen (may be NULL) gets the
+ * setting kept.  Settings that do not fit in max_stats are not tried.     */
+int32_t neci_gpu_autotune(neci_gpu_ctx *ctx, const neci_gpu_iter_params *params, int32_t steps_per_setting,
+                          neci_gpu_iter_stats *stats, int32_t max_stats, int32_t *n_steps, neci_gpu_tuning *chosen);
 
 /* ---- timing --------------------------------------------------------------
  * When enabled, every kernel launch of the iteration is bracketed by CUDA

@@ -31,6 +31,10 @@ EXGEN_UNIFORM = 1
 EXGEN_PCHB = 2
 PREC_FP64 = 0
 PREC_MIXED = 1
+OPT_FUSE_PROBE = 0
+OPT_ANNIHILATION = 1
+ANN_HASH = 0
+ANN_SORT = 1
 FLAG_INITIATOR = (13, 14)
 FLAG_DETERMINISTIC = (19, 20)
 SPAWN_FIXED_BITS = 32
@@ -85,6 +89,17 @@ class TauStats(C.Structure):
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    """neci_gpu_tuning: launch shapes and the annihilation form of a context."""
+    _fields_ = [
+        ("annihilation", C.c_int32), ("spawn_blocks_per_sm", C.c_int32), ("table_shift", C.c_int32),
+        ("sort_blocks_per_sm", C.c_int32), ("ns_per_update", C.c_double), ("reserved", C.c_int32 * 2),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_ if name != "reserved"}
 
 
 def default_params(**kw) -> IterParams:
@@ -145,7 +160,12 @@ _SIGS = {
     "neci_gpu_helement": (_i32, [_P, _P, _P, _i64, _P]),
     "neci_gpu_gen_excit": (_i32, [_P, _P, _i64, _u64, _i64, _P, _P, _P]),
     "neci_gpu_set_core_space": (_i32, [_P, _P, _i64, _i32]),
+    "neci_gpu_select_core": (_i32, [_P, _i64, _i32, _P, _P]),
     "neci_gpu_core_nnz": (_i32, [_P, _P]),
+    "neci_gpu_set_option": (_i32, [_P, _i32, _i32]),
+    "neci_gpu_set_tuning": (_i32, [_P, C.POINTER(Tuning)]),
+    "neci_gpu_get_tuning": (_i32, [_P, C.POINTER(Tuning)]),
+    "neci_gpu_autotune": (_i32, [_P, C.POINTER(IterParams), _i32, _P, _i32, _P, C.POINTER(Tuning)]),
     "neci_gpu_set_profiling": (_i32, [_P, _i32]),
     "neci_gpu_kernel_times": (_i32, [_P, _P, _P, _i32]),
     "neci_gpu_kernel_name": (C.c_char_p, [_i32]),

@@ -44,6 +44,16 @@ int dalloc(Engine &e, T **p, size_t count) {
     return NECI_GPU_OK;
 }
 
+// Frees a dalloc'ed array (the context's list forgets it) and clears the pointer.
+template <typename T>
+void dfree(Engine &e, T *&p) {
+    if (!p) return;
+    auto it = std::find(e.allocs.begin(), e.allocs.end(), (void *)p);
+    if (it != e.allocs.end()) e.allocs.erase(it);
+    cudaFree((void *)p);
+    p = nullptr;
+}
+
 unsigned long long next_pow2(unsigned long long x) {
     unsigned long long p = 1;
     while (p < x) p <<= 1;
@@ -76,9 +86,9 @@ void copy_params(IterParams &d, const neci_gpu_iter_params &p) {
     d.av_unit = p.av_mc_excits == 1.0;
 }
 
-const char *kKernelNames[K_NUM] = {"compact",   "rehash",       "begin",        "sweep",      "expand", "spawn",
-                                   "core",      "ann_probe",    "ann_compress", "ann_insert", "merge_stats",
-                                   "rdm",       "final"};
+const char *kKernelNames[K_NUM] = {"compact",     "rehash",       "begin",        "sweep",      "expand", "spawn",
+                                   "core",        "ann_probe",    "ann_compress", "ann_insert", "merge_stats",
+                                   "rdm",         "final",        "sort_keys",    "sort_radix", "sort_group"};
 
 // Launch one kernel stage, bracketed by events when profiling.
 template <typename F>
@@ -98,6 +108,28 @@ int stage(Engine &e, int id, F &&f) {
     return NECI_GPU_OK;
 }
 
+// The annihilation passes before the insertion of new determinants.  Hash
+// form: pass 1 (the walker-hash lookup of every spawn) as its own kernel
+// unless the spawn kernel does it, then the compression of the spawns onto
+// absent determinants.  Sort form: keys, radix passes, and the grouping of
+// runs of equal keys (looked up in the walker hash when `lookup`; without it
+// every group is a new determinant, as the compression alone needs).
+void annihilation_passes(Engine &e, int lookup) {
+    if (e.ann_mode == NECI_ANN_SORT) {
+        int cur = 0;
+        stage(e, K_SORT_KEYS, [&] { launch_sort_keys(e, e.stream); });
+        stage(e, K_SORT_RADIX, [&] { cur = launch_sort_radix(e, e.stream); });
+        stage(e, K_SORT_GROUP, [&] { launch_sort_group(e, e.stream, lookup, cur); });
+        return;
+    }
+    if (!lookup) {
+        launch_all_cand(e);
+    } else if (!fused_lookup(e)) {
+        stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
+    }
+    stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
+}
+
 // The launch sequence of one PerformFCIMCycPar step.
 void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_COMPACT, [&] { launch_compact(e, e.stream); });
@@ -107,10 +139,7 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_EXPAND, [&] { launch_expand(e, e.stream); });
     stage(e, K_SPAWN, [&] { launch_spawn(e, e.stream); });
     if (e.st.n_core > 0) stage(e, K_CORE, [&] { launch_core(e, e.stream); });
-    // pass 1 (the hash lookup of every spawn) runs as its own kernel unless
-    // the spawn kernel does it (fuse_probe)
-    if (!e.fuse_probe || e.sys.rdm) stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
-    stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
+    annihilation_passes(e, 1);
     stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream); });
     stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, e.st.n_core > 0 ? 1 : 0); });
     if (e.sys.rdm) stage(e, K_RDM, [&] { launch_rdm(e, e.stream); });
@@ -226,6 +255,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     st.hash_n = next_pow2(std::max<unsigned long long>((unsigned long long)sys->n_walker_hashes,
                                                        2ull * (unsigned long long)sys->max_walkers));
     st.spawn_hash_n = next_pow2(2ull * (unsigned long long)sys->max_spawned);
+    st.comp_shift = 1;
     int rc = NECI_GPU_OK;
 #define A(p, n) if (rc == NECI_GPU_OK) rc = dalloc(e, &(p), (n))
     int32_t *rh2 = nullptr;
@@ -621,9 +651,9 @@ int32_t neci_gpu_init_pchb(neci_gpu_ctx *ctx) {
     s.alias_rec = arec;
     s.pexch = pexch;
     s.tgt_pair = tgt;
-    launch_pchb_build(e);
+    if (const int err = launch_pchb_build(e))
+        return fail(NECI_GPU_ERR_CUDA, std::string("PCHB table build: ") + cudaGetErrorString((cudaError_t)err));
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(e.stream));
     e.have_pchb = true;
     drop_graphs(e);
     return NECI_GPU_OK;
@@ -746,6 +776,7 @@ static const char *not_ready(const Engine &e) {
 // from the last step, with a margin against flipping; a change drops the
 // captured step graphs.
 static void update_fuse_probe(Engine &e, const neci_gpu_iter_stats &last) {
+    if (e.fuse_mode >= 0 || e.ann_mode != NECI_ANN_HASH) return;  // fixed by NECI_OPT_FUSE_PROBE, or no hash passes
     if (e.sys.rdm || e.sys.excitgen != NECI_EXGEN_RS_HUBBARD || last.n_attempts <= 0) return;
     const double rate = (double)last.n_spawned / (double)last.n_attempts;
     const bool want = e.fuse_probe ? rate >= 0.25 : rate >= 0.3;
@@ -896,8 +927,13 @@ int32_t neci_gpu_annihilate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, co
     launch_begin(e, e.stream);
     launch_collect_holes(e);
     if (int r = upload_spawns(e, spawned, n)) return r;
-    launch_ann_probe(e, e.stream);
-    launch_ann_compress(e, e.stream);
+    // every record is written: the spawn kernel's fused lookup plays no part
+    const bool fused = e.fuse_probe;
+    const int mode = e.fuse_mode;
+    e.fuse_mode = 0;
+    annihilation_passes(e, 1);
+    e.fuse_probe = fused;
+    e.fuse_mode = mode;
     launch_ann_insert(e, e.stream);
     launch_merge_stats(e, e.stream, 0);
     launch_final(e, e.stream, e.d_stats, 0);
@@ -918,12 +954,22 @@ int32_t neci_gpu_compress_spawns(neci_gpu_ctx *ctx, const int64_t *spawned, int6
     const int R = e.sys.R, W = e.sys.W, L = e.sys.L;
     launch_begin(e, e.stream);
     if (int r = upload_spawns(e, spawned, n)) return r;
-    launch_all_cand(e);
-    launch_ann_compress(e, e.stream);
-    long long *d_out = nullptr;
-    unsigned long long *d_n = nullptr;
-    CK(cudaMallocAsync(&d_out, (size_t)std::max<int64_t>(n, 1) * R * 8, e.stream));
-    CK(cudaMallocAsync(&d_n, sizeof(unsigned long long), e.stream));
+    annihilation_passes(e, 0);
+    // the output buffers come from the stream's pool and go back to it on
+    // every exit, the early returns of a failed call included
+    struct StreamBuffers {
+        cudaStream_t s;
+        long long *out = nullptr;
+        unsigned long long *n = nullptr;
+        ~StreamBuffers() {
+            if (out) cudaFreeAsync(out, s);
+            if (n) cudaFreeAsync(n, s);
+        }
+    } buf{e.stream};
+    CK(cudaMallocAsync(&buf.out, (size_t)std::max<int64_t>(n, 1) * R * 8, e.stream));
+    CK(cudaMallocAsync(&buf.n, sizeof(unsigned long long), e.stream));
+    long long *const d_out = buf.out;
+    unsigned long long *const d_n = buf.n;
     CK(cudaMemsetAsync(d_n, 0, sizeof(unsigned long long), e.stream));
     launch_compress_out(e, d_out, d_n);
     CK(cudaGetLastError());
@@ -934,8 +980,6 @@ int32_t neci_gpu_compress_spawns(neci_gpu_ctx *ctx, const int64_t *spawned, int6
     CK(cudaStreamSynchronize(e.stream));
     std::vector<long long> rows((size_t)hn * R);
     if (hn) CK(cudaMemcpyAsync(rows.data(), d_out, (size_t)hn * R * 8, cudaMemcpyDeviceToHost, e.stream));
-    CK(cudaFreeAsync(d_out, e.stream));
-    CK(cudaFreeAsync(d_n, e.stream));
     CK(cudaStreamSynchronize(e.stream));
     if (c.err) return fail(c.err, "device reported an error in the compression");
     // order of CompressSpawnedList's output: sorted by ilut_lt
@@ -1041,25 +1085,49 @@ int32_t neci_gpu_gen_excit(neci_gpu_ctx *ctx, const int64_t *det, int64_t n, uin
     return NECI_GPU_OK;
 }
 
-int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core, int64_t n_core, int32_t precision) {
-    if (int r = check_ctx(ctx)) return r;
-    Engine &e = ctx->e;
-    (void)precision;  // both value arrays are kept; the step's precision picks one
-    if (n_core < 1 || !core || n_core >= (1ll << 31)) return fail(NECI_GPU_ERR_INVALID, "bad core space");
+}  // extern "C"
+
+namespace {
+
+// The core space from n_core determinants (W words each) in device memory:
+// the previous core space's arrays are freed and its flags cleared, the new
+// determinants are flagged deterministic and the core Hamiltonian is built
+// as CSR (calc_determ_hamil_sparse, sparse_arrays.F90:426).
+int core_build(Engine &e, const long long *dcore, long long n_core) {
     DevState &st = e.st;
-    const int W = e.sys.W, L = e.sys.L;
+    const int L = e.sys.L;
+    // a new core space replaces the old one: its arrays are freed (the step
+    // graphs that read them are dropped first) and its flags cleared below
+    CK(cudaStreamSynchronize(e.stream));
+    drop_graphs(e);
+    st.n_core = 0;
+    dfree(e, st.core_slot);
+    dfree(e, st.core_x);
+    dfree(e, st.core_y);
+    dfree(e, st.core_rowptr);
+    dfree(e, st.core_col);
+    dfree(e, st.core_val);
+    dfree(e, st.core_val32);
     if (!st.core_of_slot) {
         if (int r = dalloc(e, &st.core_of_slot, (size_t)st.max_walkers)) return r;
     }
     CK(cudaMemsetAsync(st.core_of_slot, 0xFF, (size_t)st.max_walkers * 4, e.stream));
-    long long *dcore = nullptr, *counts = nullptr;
-    if (int r = dalloc(e, &dcore, (size_t)n_core * W)) return r;
-    CK(cudaMemcpyAsync(dcore, core, (size_t)n_core * W * 8, cudaMemcpyHostToDevice, e.stream));
+    launch_core_unmark(e);
+    // the row counts, a set-up temporary freed on every exit
+    struct Temp {
+        Engine &e;
+        long long *counts = nullptr;
+        ~Temp() {
+            cudaStreamSynchronize(e.stream);
+            dfree(e, counts);
+        }
+    } tmp{e};
     if (int r = dalloc(e, &st.core_slot, (size_t)n_core)) return r;
     if (int r = dalloc(e, &st.core_x, (size_t)n_core * L)) return r;
     if (int r = dalloc(e, &st.core_y, (size_t)n_core * L)) return r;
     if (int r = dalloc(e, &st.core_rowptr, (size_t)n_core + 1)) return r;
-    if (int r = dalloc(e, &counts, (size_t)n_core)) return r;
+    if (int r = dalloc(e, &tmp.counts, (size_t)n_core)) return r;
+    long long *const counts = tmp.counts;
     CK(cudaMemsetAsync(&st.ctl->err, 0, sizeof(int), e.stream));
     launch_core_mark(e, dcore, n_core);
     launch_core_count(e, dcore, n_core, counts);
@@ -1069,7 +1137,11 @@ int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core, int64_t 
     int err = 0;
     CK(cudaMemcpyAsync(&err, &st.ctl->err, sizeof(int), cudaMemcpyDeviceToHost, e.stream));
     CK(cudaStreamSynchronize(e.stream));
-    if (err) return fail(NECI_GPU_ERR_INVALID, "core determinant not in CurrentDets");
+    if (err) {
+        launch_core_unmark(e);
+        CK(cudaMemsetAsync(&st.ctl->err, 0, sizeof(int), e.stream));
+        return fail(NECI_GPU_ERR_INVALID, "core determinant not in CurrentDets");
+    }
     for (long long i = 0; i < n_core; ++i) rp[i + 1] = rp[i] + hc[i];
     const long long nnz = rp[n_core];
     CK(cudaMemcpyAsync(st.core_rowptr, rp.data(), (size_t)(n_core + 1) * 8, cudaMemcpyHostToDevice, e.stream));
@@ -1077,11 +1149,223 @@ int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core, int64_t 
     if (int r = dalloc(e, &st.core_val, (size_t)nnz)) return r;
     if (int r = dalloc(e, &st.core_val32, (size_t)nnz)) return r;
     st.n_core = n_core;
+    st.core_group = core_group_size(nnz, n_core);
     launch_core_fill(e, dcore, n_core);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e.stream));
+    return NECI_GPU_OK;
+}
+
+// Allocates the arrays of the sort form of the annihilation (once).
+int alloc_sort_buffers(Engine &e) {
+    DevState &st = e.st;
+    if (st.sk_key[0]) return NECI_GPU_OK;
+    const size_t n = (size_t)st.max_spawned;
+    st.sk_blocks = sort_ann_blocks(e);
+    int hb = 0;
+    while ((1ull << hb) < st.hash_n) ++hb;
+    st.sk_hb = hb;
+    int rc = NECI_GPU_OK;
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_key[0], n);
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_key[1], n);
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_val[0], n);
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_val[1], n);
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_h, n);
+    // counts for the most blocks a tuning may give a radix pass (4 per SM)
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_counts, (size_t)kSortBins * (4 * e.num_sms + 1));
+    if (rc == NECI_GPU_OK) rc = dalloc(e, &st.sk_long, n / 32 + 2);
+    if (rc == NECI_GPU_OK && cudaStreamSynchronize(e.stream) != cudaSuccess) rc = fail(NECI_GPU_ERR_CUDA, "sync");
+    if (rc != NECI_GPU_OK) {
+        dfree(e, st.sk_key[0]);
+        dfree(e, st.sk_key[1]);
+        dfree(e, st.sk_val[0]);
+        dfree(e, st.sk_val[1]);
+        dfree(e, st.sk_h);
+        dfree(e, st.sk_counts);
+        dfree(e, st.sk_long);
+    }
+    return rc;
+}
+
+// A tuning's settings checked and applied (the step graphs are captured
+// again with them).
+int apply_tuning(Engine &e, const neci_gpu_tuning &t) {
+    if ((t.annihilation != NECI_ANN_HASH && t.annihilation != NECI_ANN_SORT) || t.spawn_blocks_per_sm < 1 ||
+        t.spawn_blocks_per_sm > 8 || t.table_shift < 1 || t.table_shift > 4 || t.sort_blocks_per_sm < 1 ||
+        t.sort_blocks_per_sm > 4)
+        return fail(NECI_GPU_ERR_INVALID, "tuning out of range: annihilation NECI_ANN_*, spawn blocks per SM 1..8, "
+                                          "table shift 1..4, sort blocks per SM 1..4");
+    e.sort_bpsm = t.sort_blocks_per_sm;
+    if (t.annihilation == NECI_ANN_SORT)
+        if (int r = alloc_sort_buffers(e)) return r;
+    if (e.st.sk_key[0]) e.st.sk_blocks = sort_ann_blocks(e);
+    e.ann_mode = t.annihilation;
+    e.spawn_occ = t.spawn_blocks_per_sm;
+    e.st.comp_shift = t.table_shift;
     drop_graphs(e);
     return NECI_GPU_OK;
+}
+
+neci_gpu_tuning current_tuning(const Engine &e) {
+    neci_gpu_tuning t{};
+    t.annihilation = e.ann_mode;
+    t.spawn_blocks_per_sm = e.spawn_occ;
+    t.table_shift = e.st.comp_shift;
+    t.sort_blocks_per_sm = e.sort_bpsm;
+    t.ns_per_update = 0.0;
+    return t;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t neci_gpu_set_tuning(neci_gpu_ctx *ctx, const neci_gpu_tuning *t) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!t) return fail(NECI_GPU_ERR_INVALID, "null tuning");
+    return apply_tuning(ctx->e, *t);
+}
+
+int32_t neci_gpu_get_tuning(neci_gpu_ctx *ctx, neci_gpu_tuning *t) {
+    if (int r = check_ctx(ctx)) return r;
+    if (!t) return fail(NECI_GPU_ERR_INVALID, "null tuning");
+    *t = current_tuning(ctx->e);
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_autotune(neci_gpu_ctx *ctx, const neci_gpu_iter_params *params, int32_t steps_per_setting,
+                          neci_gpu_iter_stats *stats, int32_t max_stats, int32_t *n_steps, neci_gpu_tuning *chosen) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (!params || !stats || !n_steps || steps_per_setting < 1) return fail(NECI_GPU_ERR_INVALID, "bad argument");
+    if (e.profiling) return fail(NECI_GPU_ERR_INVALID, "autotuning needs profiling off");
+    // the candidate settings: the hash form with the spawn grid at 8, 6 or 4
+    // blocks per SM and the compression table at load 1/2 or 1/4, and the
+    // sort form with 1, 2 or 4 radix-pass blocks per SM
+    static const neci_gpu_tuning cands[] = {
+        {NECI_ANN_HASH, 8, 1, 2, 0.0, {0}}, {NECI_ANN_HASH, 6, 1, 2, 0.0, {0}}, {NECI_ANN_HASH, 4, 1, 2, 0.0, {0}},
+        {NECI_ANN_HASH, 8, 2, 2, 0.0, {0}}, {NECI_ANN_SORT, 8, 1, 1, 0.0, {0}}, {NECI_ANN_SORT, 8, 1, 2, 0.0, {0}},
+        {NECI_ANN_SORT, 8, 1, 4, 0.0, {0}}};
+    const int per = 1 + steps_per_setting;  // one untimed step captures the setting's graph
+    neci_gpu_iter_params p = *params;
+    const neci_gpu_tuning start = current_tuning(e);
+    neci_gpu_tuning best = start;
+    double best_cost = -1.0;
+    int done = 0;
+    for (const neci_gpu_tuning &c : cands) {
+        if (done + per > max_stats) break;
+        if (apply_tuning(e, c) != NECI_GPU_OK) continue;  // e.g. no memory for the sort form
+        if (int r = run_steps(e, &p, 1, stats + done)) { *n_steps = done + 1; return r; }
+        p.iter += 1;
+        double ms = 0.0;
+        if (int r = run_steps(e, &p, steps_per_setting, stats + done + 1, &ms)) { *n_steps = done + per; return r; }
+        p.iter += steps_per_setting;
+        double upd = 0.0;
+        for (int i = 1; i < per; ++i)
+            for (int k = 0; k < e.sys.L; ++k) upd += stats[done + i].tot_parts_old[k];
+        done += per;
+        const double cost = upd > 0.0 ? ms * 1e6 / upd : 0.0;  // ns per walker update
+        if (best_cost < 0.0 || cost < best_cost) {
+            best_cost = cost;
+            best = c;
+            best.ns_per_update = cost;
+        }
+    }
+    *n_steps = done;
+    if (int r = apply_tuning(e, best_cost < 0.0 ? start : best)) return r;
+    if (chosen) *chosen = best;
+    return NECI_GPU_OK;
+}
+
+int32_t neci_gpu_set_core_space(neci_gpu_ctx *ctx, const int64_t *core, int64_t n_core, int32_t precision) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    (void)precision;  // both value arrays are kept; the step's precision picks one
+    if (n_core < 1 || !core || n_core >= (1ll << 31)) return fail(NECI_GPU_ERR_INVALID, "bad core space");
+    struct Temp {
+        Engine &e;
+        long long *dcore = nullptr;
+        ~Temp() {
+            cudaStreamSynchronize(e.stream);
+            dfree(e, dcore);
+        }
+    } tmp{e};
+    if (int r = dalloc(e, &tmp.dcore, (size_t)n_core * e.sys.W)) return r;
+    CK(cudaMemcpyAsync(tmp.dcore, core, (size_t)n_core * e.sys.W * 8, cudaMemcpyHostToDevice, e.stream));
+    return core_build(e, tmp.dcore, n_core);
+}
+
+int32_t neci_gpu_select_core(neci_gpu_ctx *ctx, int64_t n_core, int32_t precision, int64_t *core_dets,
+                             int64_t *n_selected) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    (void)precision;
+    if (n_core < 1 || n_core >= (1ll << 31)) return fail(NECI_GPU_ERR_INVALID, "bad core size");
+    if (!e.have_ref) return fail(NECI_GPU_ERR_INVALID, "set the reference first");
+    DevState &st = e.st;
+    const size_t n = (size_t)st.max_walkers;
+    const int blocks = (int)std::min<long long>((long long)e.num_sms * 2, st.max_walkers / 4096 + 1);
+    // the sort's scratch: keys and slots, two buffers each, the digit counts
+    // and the occupied count, freed on every exit
+    struct Temp {
+        Engine &e;
+        unsigned long long *key[2] = {nullptr, nullptr}, *n_occ = nullptr;
+        uint32_t *val[2] = {nullptr, nullptr}, *counts = nullptr;
+        long long *dcore = nullptr;
+        ~Temp() {
+            cudaStreamSynchronize(e.stream);
+            dfree(e, key[0]);
+            dfree(e, key[1]);
+            dfree(e, val[0]);
+            dfree(e, val[1]);
+            dfree(e, counts);
+            dfree(e, n_occ);
+            dfree(e, dcore);
+        }
+    } t{e};
+    if (int r = dalloc(e, &t.key[0], n)) return r;
+    if (int r = dalloc(e, &t.key[1], n)) return r;
+    if (int r = dalloc(e, &t.val[0], n)) return r;
+    if (int r = dalloc(e, &t.val[1], n)) return r;
+    if (int r = dalloc(e, &t.counts, (size_t)kSortBins * (blocks + 1))) return r;
+    if (int r = dalloc(e, &t.n_occ, 1)) return r;
+    const int cur = launch_core_select_sort(e, t.key, t.val, t.counts, blocks, t.n_occ);
+    CK(cudaGetLastError());
+    unsigned long long occ = 0;
+    CK(cudaMemcpyAsync(&occ, t.n_occ, sizeof(occ), cudaMemcpyDeviceToHost, e.stream));
+    CK(cudaStreamSynchronize(e.stream));
+    const long long nsel = std::min<long long>(n_core, (long long)occ);
+    if (n_selected) *n_selected = nsel;
+    if (nsel < 1) return fail(NECI_GPU_ERR_INVALID, "no occupied determinant to select");
+    if (int r = dalloc(e, &t.dcore, (size_t)nsel * e.sys.W)) return r;
+    launch_core_select_gather(e, t.val[cur], nsel, t.dcore);
+    CK(cudaGetLastError());
+    if (core_dets)
+        CK(cudaMemcpyAsync(core_dets, t.dcore, (size_t)nsel * e.sys.W * 8, cudaMemcpyDeviceToHost, e.stream));
+    return core_build(e, t.dcore, nsel);
+}
+
+int32_t neci_gpu_set_option(neci_gpu_ctx *ctx, int32_t option, int32_t value) {
+    if (int r = check_ctx(ctx)) return r;
+    Engine &e = ctx->e;
+    if (option == NECI_OPT_FUSE_PROBE) {
+        if (value < -1 || value > 1) return fail(NECI_GPU_ERR_INVALID, "NECI_OPT_FUSE_PROBE takes -1, 0 or 1");
+        if (value == 1 && e.sys.excitgen != NECI_EXGEN_RS_HUBBARD)
+            return fail(NECI_GPU_ERR_UNSUPPORTED, "the fused lookup exists for lattice systems only");
+        e.fuse_mode = value;
+        drop_graphs(e);
+        return NECI_GPU_OK;
+    }
+    if (option == NECI_OPT_ANNIHILATION) {
+        if (value != NECI_ANN_HASH && value != NECI_ANN_SORT)
+            return fail(NECI_GPU_ERR_INVALID, "NECI_OPT_ANNIHILATION takes NECI_ANN_HASH or NECI_ANN_SORT");
+        if (value == NECI_ANN_SORT)
+            if (int r = alloc_sort_buffers(e)) return r;
+        e.ann_mode = value;
+        drop_graphs(e);
+        return NECI_GPU_OK;
+    }
+    return fail(NECI_GPU_ERR_INVALID, "unknown option");
 }
 
 int32_t neci_gpu_core_nnz(neci_gpu_ctx *ctx, int64_t *nnz) {

@@ -31,6 +31,9 @@ constexpr int kCompactTile = 1024;        // slots per block of the compaction s
 constexpr int kProbeLimit = 1 << 16;
 constexpr uint32_t kEmpty = 0u;
 constexpr uint32_t kTomb = 0xFFFFFFFFu;
+// rep_bucket of a unique new determinant that holds no compression-table
+// bucket (the sort form of the annihilation merges without the table)
+constexpr uint32_t kNoBucket = 0xFFFFFFFFu;
 constexpr double kEps12 = 1e-12;
 
 enum Purpose : uint32_t { P_NSPAWN = 1, P_ATTEMPT = 2, P_DEATH = 3, P_ANN_ROUND = 4, P_STATS_ROUND = 5 };
@@ -49,9 +52,12 @@ struct Control {
     unsigned long long n_occupied;
     unsigned long long n_holes;
     unsigned long long n_tomb;          // hash tombstones
-    unsigned long long n_found;         // unique spawned determinants already present
+    unsigned long long n_found;         // unique spawned determinants already present, with a
+                                        // non-zero summed amplitude
+    unsigned long long n_reps_nz;       // unique new determinants with a non-zero summed amplitude
     unsigned long long n_big;           // parents expanded by k_expand
     unsigned long long n_huge;          // parents expanded by the whole grid
+    unsigned long long n_long;          // sort annihilation: runs of equal keys left to k_sk_long
     unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
@@ -175,6 +181,7 @@ struct DevState {
     unsigned long long *cand_h;    // their 64-bit NECI hash
     uint32_t *spawn_hash;          // compression table: candidate position + 1
     unsigned long long spawn_hash_n;
+    int comp_shift;                // the table in use holds >= 2^comp_shift buckets per candidate
     uint32_t *reps;                // candidate position of each unique new determinant
     uint32_t *rep_bucket;
     long long *rep_q;              // per candidate*L fixed-point sums
@@ -194,11 +201,31 @@ struct DevState {
     double *rdm2;
     double *core_x, *core_y;
     long long *core_rowptr;
+    int core_group;                // lanes that sum one core row (core_group_size)
+    // sort form of the annihilation: 32-bit sort keys and record indices
+    // (two buffers each, ping-ponged by the radix passes), the 64-bit NECI
+    // hash of every record, per-block digit counts of a radix pass, and the
+    // starts of runs of equal keys longer than kShortRun
+    uint32_t *sk_key[2], *sk_val[2];
+    unsigned long long *sk_h;
+    uint32_t *sk_counts;
+    uint32_t *sk_long;
+    int sk_blocks;                 // blocks of a radix pass (the counts hold 256 per block)
+    int sk_hb;                     // log2 of the walker-hash length
     int32_t *core_col;
     double *core_val;
     float *core_val32;
     Control *ctl;
 };
+
+// Lanes that sum one row of the core Hamiltonian in k_core: the smallest
+// power of two G with 4 G at least the mean row length, at most 32 (so a
+// lane takes about four elements of a row); 1 sums a row in one thread.
+__host__ __device__ inline int core_group_size(long long nnz, long long n_core) {
+    int g = 1;
+    while (g < 32 && 4ll * g * n_core < nnz) g <<= 1;
+    return g;
+}
 
 // Slots in use, never above the allocation (a step that overflowed the list
 // leaves TotWalkers above it).

@@ -142,8 +142,25 @@ __device__ inline void gen_rs_hubbard(const DevSys &s, const unsigned long long 
     e.ok = true;
 }
 
+// The c-th (1-based) unoccupied spin orbital among those of `pattern`, 0 if none.
+template <int NW = 0>
+__device__ inline int nth_unoccupied(const DevSys &s, const unsigned long long *d, unsigned long long pattern, int c) {
+    unsigned long long u[kMaxWords];
+    NECI_FOR_WORDS(w, nwords<NW>(s)) {
+        const int lo = 64 * w;
+        const unsigned long long valid = s.nbasis >= lo + 64 ? ~0ull : (s.nbasis > lo ? (1ull << (s.nbasis - lo)) - 1 : 0ull);
+        u[w] = ~d[w] & valid;
+    }
+    return nth_orbital(u, nwords<NW>(s), pattern, c);
+}
+
 // CreateSingleExcit (GenRandSymExcitNUMod.F90:1118-1243), C1 symmetry,
-// tCycleOrbs = .false. (rejection for the electron and for the hole).
+// tCycleOrbs = .false.: the electron by rejection (repeated only while it
+// lands in a spin without holes).  The hole is uniform over the unoccupied
+// orbitals of the electron's spin, the distribution of the reference's
+// rejection loop, but drawn as an index into those orbitals: one draw and a
+// bit select where the loop takes a variable number of draws, which made
+// the lanes of a warp diverge and their later Philox blocks fall apart.
 // Returns the full single pgen, pSingles / (NExcit * (nel - ElecsWNoExcits)).
 template <typename Real, int NW = 0>
 __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long long *d, Stream &rng, Excit<Real> &e) {
@@ -168,14 +185,10 @@ __device__ inline void gen_uniform_single(const DevSys &s, const unsigned long l
         if (nexcit != 0) break;
     }
     if (nexcit == 0) { e.pgen = 0; return; }
-    int orb = 0;
-    bool found = false;
-    for (int attempts = 0; attempts <= 250; ++attempts) {
-        const int chosen = (int)uniform_index(rng, (unsigned)norbs);
-        orb = 2 * (chosen + 1) - (ispn - 1);
-        if (!orb_occ(d, orb)) { found = true; break; }
-    }
-    if (!found) { e.pgen = 0; return; }
+    // ispn 1: alpha (even orbitals), 2: beta (odd)
+    const int orb = nth_unoccupied<NW>(s, d, ispn == 1 ? kAlphaBits : kBetaBits,
+                                       (int)uniform_index(rng, (unsigned)nexcit) + 1);
+    if (orb == 0) { e.pgen = 0; return; }
     const int count = nexcit * (s.nel - elecs_wno);
     if (sizeof(Real) == 8) {
         e.pgen = (Real)(s.p_singles / (double)count);
@@ -312,17 +325,6 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     e.ok = true;
 }
 
-// The c-th (1-based) unoccupied spin orbital among those of `pattern`, 0 if none.
-template <int NW = 0>
-__device__ inline int nth_unoccupied(const DevSys &s, const unsigned long long *d, unsigned long long pattern, int c) {
-    unsigned long long u[kMaxWords];
-    NECI_FOR_WORDS(w, nwords<NW>(s)) {
-        const int lo = 64 * w;
-        const unsigned long long valid = s.nbasis >= lo + 64 ? ~0ull : (s.nbasis > lo ? (1ull << (s.nbasis - lo)) - 1 : 0ull);
-        u[w] = ~d[w] & valid;
-    }
-    return nth_orbital(u, nwords<NW>(s), pattern, c);
-}
 
 // CreateDoubExcit (GenRandSymExcitNUMod.F90:155-205) without spatial
 // symmetry (C1: tNoSymGenRandExcits), tCycleOrbs = .false.:

@@ -25,6 +25,9 @@ enum KernelId {
     K_MERGE_STATS,
     K_RDM,
     K_FINAL,
+    K_SORT_KEYS,   // sort form of the annihilation: keys, radix passes, grouping
+    K_SORT_RADIX,
+    K_SORT_GROUP,
     K_NUM
 };
 
@@ -40,6 +43,14 @@ struct Engine {
     // pass 1 of the annihilation runs inside the spawn kernel (chosen from the
     // last step's spawn rate; see update_fuse_probe)
     bool fuse_probe = false;
+    // NECI_OPT_FUSE_PROBE: -1 chosen from the spawn rate, 0 never, 1 always
+    int fuse_mode = -1;
+    // NECI_OPT_ANNIHILATION: NECI_ANN_HASH or NECI_ANN_SORT
+    int ann_mode = NECI_ANN_HASH;
+    // tuned launch shapes (neci_gpu_tuning): spawn blocks per SM, radix-pass
+    // blocks per SM (DevState::comp_shift holds the table load setting)
+    int spawn_occ = 8;
+    int sort_bpsm = 2;
     cudaStream_t stream = nullptr;
     IterParams *d_params = nullptr;
     IterParams *h_params = nullptr;          // pinned
@@ -63,6 +74,14 @@ struct Engine {
     long long kernel_launches[K_NUM] = {};
 };
 
+// Whether the spawn kernel does pass 1 of the annihilation (the walker-hash
+// lookup of every child): lattice systems with the hash annihilation and no
+// 2-RDM sampling, as NECI_OPT_FUSE_PROBE (or, by default, the spawn rate) says.
+inline bool fused_lookup(const Engine &e) {
+    if (e.sys.rdm || e.sys.excitgen != NECI_EXGEN_RS_HUBBARD || e.ann_mode != NECI_ANN_HASH) return false;
+    return e.fuse_mode < 0 ? e.fuse_probe : e.fuse_mode == 1;
+}
+
 // launchers (kernels.cu)
 void launch_begin(Engine &e, cudaStream_t s);
 void launch_rehash(Engine &e, cudaStream_t s);
@@ -80,6 +99,16 @@ void launch_merge_stats(Engine &e, cudaStream_t s, int with_core);
 void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter);
 void launch_rdm(Engine &e, cudaStream_t s);
 
+// sort form of the annihilation and core selection (sort_kernels.cu)
+constexpr int kSortBins = 256;  // digit values of a radix pass (radix.cuh kRadixBins)
+void launch_sort_keys(Engine &e, cudaStream_t s);
+int launch_sort_radix(Engine &e, cudaStream_t s);
+void launch_sort_group(Engine &e, cudaStream_t s, int lookup, int cur);
+int sort_ann_blocks(const Engine &e);
+int launch_core_select_sort(Engine &e, unsigned long long *key[2], uint32_t *val[2], uint32_t *counts, int blocks,
+                            unsigned long long *n_occ);
+void launch_core_select_gather(Engine &e, const uint32_t *slot, long long n, long long *core_dets);
+
 // utility launchers (util_kernels.cu)
 void launch_util_hash(Engine &e, const long long *dets, long long n, unsigned long long len, long long *out);
 void launch_util_excit_level(Engine &e, const long long *a, const long long *b, long long n, int *out);
@@ -91,10 +120,13 @@ void launch_collect_holes(Engine &e);
 void launch_convert_spawns(Engine &e, long long n);
 void launch_all_cand(Engine &e);
 void launch_compress_out(Engine &e, long long *out, unsigned long long *n_out);
+void launch_core_unmark(Engine &e);
 void launch_core_mark(Engine &e, const long long *core_dets, long long n_core);
 void launch_core_count(Engine &e, const long long *core_dets, long long n_core, long long *counts);
 void launch_core_fill(Engine &e, const long long *core_dets, long long n_core);
-void launch_pchb_build(Engine &e);
+// PCHB alias tables; returns a cudaError_t value (0: built), and launches
+// nothing when its scratch cannot be allocated
+int launch_pchb_build(Engine &e);
 void launch_build_jk(Engine &e, double *jrow, double *jkrow, float *jrow32, float *jkrow32);
 
 }  // namespace neci

@@ -47,8 +47,10 @@ __global__ void k_begin(DevState st) {
     if (blockIdx.x == 0 && threadIdx.x == 0 && !c->halted) {
         c->n_free = 0; c->free_taken = 0; c->n_att = 0; c->n_spawned = 0; c->n_cand = 0;
         c->n_reps = 0; c->n_new = 0; c->n_attempts = 0; c->n_occupied = 0; c->n_holes = 0; c->n_found = 0;
+        c->n_reps_nz = 0;
         c->n_big = 0;
         c->n_huge = 0;
+        c->n_long = 0;
         for (int k = 0; k < 2; ++k) {
             c->abs_q[k] = 0; c->abs_s[k] = 0;
             c->nborn[k] = c->ndied[k] = c->nannihil[k] = c->naborted[k] = c->nremoved[k] = 0.0;
@@ -304,6 +306,10 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
     extern __shared__ __align__(16) unsigned char sweep_smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int stage_ok;
+    // the round's appends: per-warp counts of free slots and attempts, and
+    // the block's first positions
+    __shared__ unsigned int s_wfree[kStageTile / 32], s_watt[kStageTile / 32];
+    __shared__ unsigned long long s_base_free, s_base_att;
     const size_t stage_bytes = (size_t)kStageTile * (R + 2) * 8;
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
@@ -468,13 +474,14 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
         }
         // the signs just written are all zero
         const bool freed = live && occ && !core && out_zero;
-        // The round's two appends, free slots and spawn-attempt entries: both
-        // atomics are issued before either result is read, so that their
-        // round trips overlap.  One entry per attempt; a parent with more than
-        // kBigAttempts attempts is handed to k_expand, which writes its
-        // entries with a whole block.
+        // The round's two appends, free slots and spawn-attempt entries, with
+        // one atomic per counter for the whole block (both issued before
+        // either result is read): per-warp atomics on these two addresses
+        // serialise in one L2 slice, tens of thousands to millions per step.
+        // One entry per attempt; a parent with more than kBigAttempts attempts
+        // is handed to k_expand, which writes its entries with a whole block.
         {
-            const int lane = threadIdx.x & 31;
+            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
             const bool want = hole || freed;
             const unsigned int mf = __ballot_sync(0xffffffffu, want);
             unsigned int nat = 0;
@@ -485,14 +492,26 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                 const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
                 if (lane >= o) incl += y;
             }
-            const unsigned int tot = __shfl_sync(0xffffffffu, incl, 31);
-            unsigned long long bf = 0, ba = 0;
             if (lane == 31) {
-                if (mf) bf = atomicAdd(&c->n_free, (unsigned long long)__popc(mf));
-                if (tot) ba = atomicAdd(&c->n_att, (unsigned long long)tot);
+                s_wfree[wid] = __popc(mf);
+                s_watt[wid] = incl;
             }
-            bf = __shfl_sync(0xffffffffu, bf, 31);
-            ba = __shfl_sync(0xffffffffu, ba, 31);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                unsigned int tf = 0, ta = 0;
+                for (int w = 0; w < kStageTile / 32; ++w) {
+                    tf += s_wfree[w];
+                    ta += s_watt[w];
+                }
+                s_base_free = tf ? atomicAdd(&c->n_free, (unsigned long long)tf) : 0ull;
+                s_base_att = ta ? atomicAdd(&c->n_att, (unsigned long long)ta) : 0ull;
+            }
+            __syncthreads();
+            unsigned long long bf = s_base_free, ba = s_base_att;
+            for (int w = 0; w < wid; ++w) {
+                bf += s_wfree[w];
+                ba += s_watt[w];
+            }
             if (want) st.free_list[bf + __popc(mf & ((1u << lane) - 1u))] = (int32_t)j;
             const unsigned long long base = ba + incl - nat;
             if (nat) {
@@ -576,36 +595,65 @@ __global__ void k_expand(DevState st) {
 }
 
 // ===========================================================================
-// k_core: y = -tau * H_offdiag x  (FP64, or FP32 values with compensated
-// FP32 hi/lo accumulation and an FP64 final sum)
+// k_core: y = -tau H_offdiag x over the core rows (determ_projection_no_death,
+// semi_stoch_procs.F90:290-365).  Each row is summed by a group of G lanes (a
+// power of two chosen at set-up from the mean row length, core_group_size):
+// lane l of the group accumulates the row's elements l, l+G, l+2G, ... in
+// order, and the group's G partial sums are added in a fixed tree (offsets
+// G/2, G/4, ..., 1).  FP64: fused multiply-adds acc = fma(-H_ij, x_j, acc),
+// which the oracle restates in the same order, so the projection is
+// bit-exact.  Mixed precision: FP32 values and products with compensated
+// (TwoSum) FP32 accumulation per lane, each lane's hi + lo then summed in
+// FP64 by the same tree.  Four elements of a lane are loaded before their
+// products are accumulated (in element order), so that a lane keeps four
+// independent gathers in flight.
 // ===========================================================================
-__global__ void k_core(DevSys s, DevState st, const IterParams *pp) {
+template <int G, bool MIXED>
+__global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const int L = s.L;
     const double tau = pp->tau;
-    const bool mixed = pp->precision == NECI_PREC_MIXED;
-    const int lane = threadIdx.x & 31;
-    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long i = warp; i < st.n_core; i += nwarps) {
-        const long long e0 = st.core_rowptr[i], e1 = st.core_rowptr[i + 1];
-        NECI_FOR_RUNS(k, L) {
-            double acc = 0.0;
-            if (!mixed) {
-                for (long long e = e0 + lane; e < e1; e += 32)
-                    acc -= st.core_val[e] * st.core_x[(long long)st.core_col[e] * L + k];
-                acc = warp_sum(acc);
-            } else {
-                float hi = 0.0f, lo = 0.0f;  // Kahan-Babuska (TwoSum) accumulation
-                for (long long e = e0 + lane; e < e1; e += 32) {
-                    const float term = -(st.core_val32[e] * (float)st.core_x[(long long)st.core_col[e] * L + k]);
-                    const float t = hi + term;
-                    if (fabsf(hi) >= fabsf(term)) lo += (hi - t) + term; else lo += (term - t) + hi;
-                    hi = t;
+    const int gl = threadIdx.x & (G - 1);
+    const long long grp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
+    const long long ngrp = ((long long)gridDim.x * blockDim.x) / G;
+    const long long nrows = st.n_core;
+    // every lane runs the same number of rounds (the tree's shuffles are warp-wide)
+    const long long nround = ((nrows + ngrp - 1) / ngrp) * ngrp;
+    const int32_t *col = st.core_col;
+    const double *xv = st.core_x;
+    for (long long i = grp; i < nround; i += ngrp) {
+        const bool valid = i < nrows;
+        const long long e0 = valid ? st.core_rowptr[i] : 0, e1 = valid ? st.core_rowptr[i + 1] : 0;
+        double acc[2] = {0.0, 0.0};
+        float hi[2] = {0.0f, 0.0f}, lo[2] = {0.0f, 0.0f};
+        auto add = [&](long long e, int c) {
+            NECI_FOR_RUNS(k, L) {
+                const double x = xv[(long long)c * L + k];
+                if (!MIXED) {
+                    acc[k] = fma(-st.core_val[e], x, acc[k]);
+                } else {
+                    const float term = -__fmul_rn(st.core_val32[e], (float)x);
+                    const float t = __fadd_rn(hi[k], term);
+                    lo[k] = fabsf(hi[k]) >= fabsf(term) ? __fadd_rn(lo[k], __fadd_rn(__fsub_rn(hi[k], t), term))
+                                                        : __fadd_rn(lo[k], __fadd_rn(__fsub_rn(term, t), hi[k]));
+                    hi[k] = t;
                 }
-                acc = warp_sum((double)hi + (double)lo);
             }
-            if (lane == 0) st.core_y[i * L + k] = acc * tau;
+        };
+        long long e = e0 + gl;
+        for (; e + 3 * G < e1; e += 4 * G) {
+            const int c0 = col[e], c1 = col[e + G], c2 = col[e + 2 * G], c3 = col[e + 3 * G];
+            add(e, c0);
+            add(e + G, c1);
+            add(e + 2 * G, c2);
+            add(e + 3 * G, c3);
+        }
+        for (; e < e1; e += G) add(e, col[e]);
+        NECI_FOR_RUNS(k, L) {
+            double t = MIXED ? (double)hi[k] + (double)lo[k] : acc[k];
+#pragma unroll
+            for (int o = G / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o, G);
+            if (gl == 0 && valid) st.core_y[i * L + k] = t * tau;
         }
     }
 }
@@ -700,11 +748,12 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
     const int W = s.W, R = s.R;
     constexpr int L = LR;
     // The table in use is sized to this step's candidates (a power of two at
-    // least twice their number), not to the allocation: at tens of millions
+    // least 2^comp_shift times their number, twice by default), not to the
+    // allocation: at tens of millions
     // of spawns it stays in L2 instead of scattering the probes over
     // gigabytes of DRAM.  Its buckets are cleared through rep_bucket.
     unsigned long long hn = 1024;
-    while (hn < 2ull * (unsigned long long)n && hn < st.spawn_hash_n) hn <<= 1;
+    while (hn < ((unsigned long long)n << st.comp_shift) && hn < st.spawn_hash_n) hn <<= 1;
     const unsigned long long mask = (hn < st.spawn_hash_n ? hn : st.spawn_hash_n) - 1;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
@@ -787,7 +836,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
     long long a_tomb = 0;  // tombstones taken over by the insertions (a negative count)
-    unsigned long long a_new = 0;
+    unsigned long long a_new = 0, a_nz = 0;
     // the round's new determinants (blockDim.x = 128: four warps)
     __shared__ int nq_w[2][4];
     __shared__ long long q_slot[128];
@@ -801,7 +850,8 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
         long long wflags = 0, wci = 0;
         if (ri < n) {
             const long long ci = st.reps[ri];
-            st.spawn_hash[st.rep_bucket[ri]] = kEmpty;  // leave the table clean
+            const uint32_t rb = st.rep_bucket[ri];
+            if (rb != kNoBucket) st.spawn_hash[rb] = kEmpty;  // leave the table clean
             const long long i = st.cand[ci];
             const long long *rec = st.spawn + i * R;
             unsigned long long d[kMaxWords];
@@ -833,6 +883,7 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                 if (q[k] != 0) zero = false;
                 a_s[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
             }
+            a_nz += zero ? 0ull : 1ull;
             if (!zero) {
                 double ss[2] = {from_fixed(q[0]), from_fixed(q[1])};
                 if (p.t_trunc_initiator)
@@ -946,9 +997,9 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                             &c->nborn[0], &c->nborn[1]};
     block_add<6>(v, dst, L);
-    unsigned long long u[4] = {a_s[0], a_s[1], (unsigned long long)a_tomb, a_new};  // two's complement for -count
-    unsigned long long *const du[4] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb, &c->n_new};
-    block_add_u<4>(u, du);
+    unsigned long long u[5] = {a_s[0], a_s[1], (unsigned long long)a_tomb, a_new, a_nz};  // two's complement for -count
+    unsigned long long *const du[5] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb, &c->n_new, &c->n_reps_nz};
+    block_add_u<5>(u, du);
 }
 
 // ===========================================================================
@@ -1018,15 +1069,17 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
             if (m[k]) has = true;
         }
         if (has) {
-            ++a_found;
             double S[2] = {0.0, 0.0};
+            bool nz = false;  // a block of the compressed list (CompressSpawnedList drops zero sums)
             NECI_FOR_RUNS(k, L) {
                 const long long q = st.acc[j * L + k];
                 st.acc[j * L + k] = 0;
                 st.meta[j * L + k] = 0;
                 a_s[k] += (unsigned long long)(q < 0 ? -q : q);
                 S[k] = from_fixed(q);
+                nz = nz || q != 0;
             }
+            a_found += nz ? 1ull : 0ull;
             NECI_FOR_RUNS(k, L) {
                 if (abs_bits(C[k]) < dbl_bits(kEps12) && p.t_trunc_initiator) {
                     const bool sp_init = (m[k] & 0x80000000u) ||
@@ -1284,7 +1337,9 @@ __global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, i
     r.holes_in_list = (long long)c->n_holes;
     r.n_attempts = (long long)c->n_attempts;
     r.n_spawned = (long long)c->n_spawned;
-    r.n_unique = (long long)(c->n_reps + c->n_found);
+    // the length of the compressed spawn list: unique determinants whose
+    // spawns do not sum to zero
+    r.n_unique = (long long)(c->n_reps_nz + c->n_found);
     r.n_new = (long long)c->n_new;
     r.n_core = n_core;
     r.err = c->err;
@@ -1382,8 +1437,22 @@ void launch_sweep(Engine &e, cudaStream_t s) {
     }
 }
 void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256, e.occ_expand), 256, 0, s>>>(e.st); }
+template <int G>
+static void launch_core_g(Engine &e, cudaStream_t s) {
+    const int grid = clamp_grid(e.st.n_core * G / 256 + 1, e.num_sms * 8);
+    if (e.h_params->precision == NECI_PREC_MIXED) k_core<G, true><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
+    else k_core<G, false><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
+}
 void launch_core(Engine &e, cudaStream_t s) {
-    if (e.st.n_core > 0) k_core<<<grid_for(e, 256), 256, 0, s>>>(e.sys, e.st, e.d_params);
+    if (e.st.n_core <= 0) return;
+    switch (e.st.core_group) {
+        case 1: launch_core_g<1>(e, s); break;
+        case 2: launch_core_g<2>(e, s); break;
+        case 4: launch_core_g<4>(e, s); break;
+        case 8: launch_core_g<8>(e, s); break;
+        case 16: launch_core_g<16>(e, s); break;
+        default: launch_core_g<32>(e, s); break;
+    }
 }
 void launch_ann_probe(Engine &e, cudaStream_t s) {
     const size_t shm = (e.sys.nbasis + 1) * sizeof(int32_t);

@@ -51,41 +51,76 @@ __device__ inline unsigned long long na_hash(const long long *rec, int W) {
     return h;
 }
 
+// Sum of |q| per run over a block's threads, added with one atomic per warp
+// (an atomic per record on these two addresses would serialise the pass).
+__device__ inline void na_add_abs(unsigned long long (&a)[2], unsigned long long *dst, int L) {
+    for (int k = 0; k < L; ++k) {
+        unsigned long long v = a[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(&dst[k], v);
+    }
+}
+
+// Position of this lane's item among the warp's items (want: this lane has
+// one), from one atomic per warp on `counter`.  Every lane of the warp calls it.
+__device__ inline unsigned long long na_append(unsigned long long *counter, bool want) {
+    const unsigned int lane = threadIdx.x & 31;
+    const unsigned int m = __ballot_sync(0xffffffffu, want);
+    unsigned long long base = 0;
+    if (lane == 0 && m) base = atomicAdd(counter, (unsigned long long)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    return base + __popc(m & ((1u << lane) - 1u));
+}
+
 // Pass 1: every record finds (or claims) the table bucket of its
-// determinant and adds its amplitude to the owner's accumulators.
+// determinant and adds its amplitude to the owner's accumulators.  The loop
+// runs the same number of rounds in every lane (the appends are warp-wide).
 __global__ void k_na_merge(const long long *spawned, long long n, int W, int L, NoAllocScratch sc) {
     const int R = W + L + 1;
     int ovf = 0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const long long *rec = spawned + i * R;
-        unsigned long long b = na_hash(rec, W) & (kNoAllocBuckets - 1);
-        long long owner = -1;
-        for (unsigned long long p = 0; p < kNoAllocBuckets; ++p) {
-            const uint32_t e = atomicCAS(&sc.table[b], 0u, (uint32_t)(i + 1));
-            if (e == 0u) {
-                owner = i;
-                const unsigned long long pos = atomicAdd(&sc.ctr->n_reps, 1ull);
-                sc.reps[pos] = (uint32_t)i;
-                break;
+    unsigned long long aq[2] = {0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nround; i += stride) {
+        bool claimed = false;
+        if (i < n) {
+            const long long *rec = spawned + i * R;
+            unsigned long long b = na_hash(rec, W) & (kNoAllocBuckets - 1);
+            long long owner = -1;
+            for (unsigned long long p = 0; p < kNoAllocBuckets; ++p) {
+                const uint32_t e = atomicCAS(&sc.table[b], 0u, (uint32_t)(i + 1));
+                if (e == 0u) {
+                    owner = i;
+                    claimed = true;
+                    break;
+                }
+                const long long o = (long long)e - 1;
+                bool same = true;
+                for (int w = 0; w < W; ++w) same = same && spawned[o * R + w] == rec[w];
+                if (same) { owner = o; break; }
+                b = (b + 1) & (kNoAllocBuckets - 1);
             }
-            const long long o = (long long)e - 1;
-            bool same = true;
-            for (int w = 0; w < W; ++w) same = same && spawned[o * R + w] == rec[w];
-            if (same) { owner = o; break; }
-            b = (b + 1) & (kNoAllocBuckets - 1);
+            if (owner < 0) {
+                atomicCAS(&sc.ctr->err, 0, NECI_GPU_ERR_HASH_FULL);
+            } else {
+                const long long fl = rec[W + L];
+                atomicAdd(&sc.cnt[owner * 3 + 2], 1u);
+                for (int k = 0; k < L; ++k) {
+                    const long long q = na_fixed(rec[W + k], &ovf);
+                    if (q == 0) continue;
+                    atomicAdd((unsigned long long *)&sc.q[owner * 2 + k], (unsigned long long)q);
+                    aq[k] += (unsigned long long)(q < 0 ? -q : q);
+                    atomicAdd(&sc.cnt[owner * 3 + k], 1u);
+                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&sc.cnt[owner * 3 + k], 0x80000000u);
+                }
+            }
         }
-        if (owner < 0) { atomicCAS(&sc.ctr->err, 0, NECI_GPU_ERR_HASH_FULL); continue; }
-        const long long fl = rec[W + L];
-        atomicAdd(&sc.cnt[owner * 3 + 2], 1u);
-        for (int k = 0; k < L; ++k) {
-            const long long q = na_fixed(rec[W + k], &ovf);
-            if (q == 0) continue;
-            atomicAdd((unsigned long long *)&sc.q[owner * 2 + k], (unsigned long long)q);
-            atomicAdd((unsigned long long *)&sc.ctr->abs_q[k], (unsigned long long)(q < 0 ? -q : q));
-            atomicAdd(&sc.cnt[owner * 3 + k], 1u);
-            if (test_bit(fl, init_flag_bit(k))) atomicOr(&sc.cnt[owner * 3 + k], 0x80000000u);
-        }
+        // the records that claimed a bucket are the determinants' owners
+        const unsigned long long pos = na_append(&sc.ctr->n_reps, claimed);
+        if (claimed) sc.reps[pos] = (uint32_t)i;
     }
+    na_add_abs(aq, sc.ctr->abs_q, L);
     if (ovf) atomicCAS(&sc.ctr->err, 0, NECI_GPU_ERR_OVERFLOW);
 }
 
@@ -95,33 +130,39 @@ __global__ void k_na_out(const long long *spawned, int W, int L, int trunc_init,
                          NoAllocScratch sc) {
     const int R = W + L + 1;
     const long long n = (long long)sc.ctr->n_reps;
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
-        const long long i = sc.reps[r];
-        const long long *rec = spawned + i * R;
-        long long q[2] = {sc.q[i * 2], sc.q[i * 2 + 1]};
-        bool zero = true;
-        for (int k = 0; k < L; ++k) {
-            if (q[k] != 0) zero = false;
-            atomicAdd((unsigned long long *)&sc.ctr->abs_s[k], (unsigned long long)(q[k] < 0 ? -q[k] : q[k]));
-        }
-        if (zero) continue;
-        long long flags;
-        if (sc.cnt[i * 3 + 2] == 1u) {
-            flags = rec[W + L];
-        } else {
-            flags = 0;
-            if (trunc_init)
+    unsigned long long as[2] = {0, 0};
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < nround; r += stride) {
+        bool emit = false;
+        long long i = 0, flags = 0;
+        long long q[2] = {0, 0};
+        if (r < n) {
+            i = sc.reps[r];
+            q[0] = sc.q[i * 2];
+            q[1] = sc.q[i * 2 + 1];
+            for (int k = 0; k < L; ++k) {
+                if (q[k] != 0) emit = true;
+                as[k] += (unsigned long long)(q[k] < 0 ? -q[k] : q[k]);
+            }
+            if (sc.cnt[i * 3 + 2] == 1u) {
+                flags = spawned[i * R + W + L];
+            } else if (trunc_init) {
                 for (int k = 0; k < L; ++k) {
                     const uint32_t c = sc.cnt[i * 3 + k];
                     if ((coherent && (c & 0x7FFFFFFFu) >= 2u) || (c & 0x80000000u)) flags |= 1ll << init_flag_bit(k);
                 }
+            }
         }
-        const unsigned long long pos = atomicAdd(&sc.ctr->n_out, 1ull);
+        const unsigned long long pos = na_append(&sc.ctr->n_out, emit);
+        if (!emit) continue;
+        const long long *rec = spawned + i * R;
         long long *o = out + pos * R;
         for (int w = 0; w < W; ++w) o[w] = rec[w];
         for (int k = 0; k < L; ++k) o[W + k] = double_to_word(from_fixed(q[k]));
         o[W + L] = flags;
     }
+    na_add_abs(as, sc.ctr->abs_s, L);
 }
 
 std::mutex g_na_mutex;

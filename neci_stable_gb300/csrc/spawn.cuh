@@ -487,8 +487,9 @@ __global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const I
 }
 
 // Grids are sized to the context's capacity (as in kernels.cu).
+// The grid fills spawn_occ blocks per SM (8, the launch bound, unless tuned).
 inline int spawn_grid(const Engine &e, int threads) {
-    const long long want = e.st.max_spawned / (threads * 4) + 1, hi = e.num_sms * (threads == 128 ? 8 : 4);
+    const long long want = e.st.max_spawned / (threads * 4) + 1, hi = (long long)e.num_sms * e.spawn_occ;
     return (int)(want < 8 ? 8 : (want > hi ? hi : want));
 }
 
@@ -503,12 +504,12 @@ inline int spawn_queue_doubles(const DevSys &s) {
 template <typename Real, int GEN, bool QD>
 void launch_spawn_words(Engine &e, cudaStream_t s, int grid, size_t shm) {
     const int rw = e.sys.W, nw = (e.sys.nbasis + 63) / 64;
-    if (rw == 1) k_spawn<Real, GEN, 1, 1, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
-    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
-    else if (rw == 2) k_spawn<Real, GEN, 2, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
-    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
-    else if (rw == 3) k_spawn<Real, GEN, 3, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
-    else k_spawn<Real, GEN, 0, 0, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, e.fuse_probe ? 1 : 0);
+    if (rw == 1) k_spawn<Real, GEN, 1, 1, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, fused_lookup(e) ? 1 : 0);
+    else if (rw == 2 && nw == 1) k_spawn<Real, GEN, 1, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, fused_lookup(e) ? 1 : 0);
+    else if (rw == 2) k_spawn<Real, GEN, 2, 2, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, fused_lookup(e) ? 1 : 0);
+    else if (rw == 3 && nw == 2) k_spawn<Real, GEN, 2, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, fused_lookup(e) ? 1 : 0);
+    else if (rw == 3) k_spawn<Real, GEN, 3, 3, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, fused_lookup(e) ? 1 : 0);
+    else k_spawn<Real, GEN, 0, 0, QD><<<grid, 128, shm, s>>>(e.sys, e.st, e.d_params, fused_lookup(e) ? 1 : 0);
 }
 
 template <typename Real, int GEN>

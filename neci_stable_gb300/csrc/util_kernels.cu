@@ -136,7 +136,8 @@ __global__ void k_compress_out(DevSys s, DevState st, long long *out, unsigned l
     unsigned long long as[2] = {0, 0};
     for (long long ri = blockIdx.x * (long long)blockDim.x + threadIdx.x; ri < n; ri += (long long)gridDim.x * blockDim.x) {
         const long long ci = st.reps[ri];
-        st.spawn_hash[st.rep_bucket[ri]] = kEmpty;
+        const uint32_t rb = st.rep_bucket[ri];
+        if (rb != kNoBucket) st.spawn_hash[rb] = kEmpty;
         const long long *rec = st.spawn + (long long)st.cand[ci] * s.R;
         long long q[2] = {0, 0};
         uint32_t cnt[2] = {0, 0};
@@ -195,6 +196,31 @@ __global__ void k_core_mark(DevSys s, DevState st, const long long *core_dets, l
         st.core_slot[c] = slot;
     }
 }
+// Clears the deterministic flags of the previous core space.  A former core
+// determinant whose signs are all zero was kept only because it was in the
+// core: it leaves the walker hash (RemoveHashDet) as the sweep would have
+// removed it, so that its slot can become a hole.
+__global__ void k_core_unmark(DevSys s, DevState st) {
+    const long long n = slots_in_use(st);
+    unsigned long long tomb = 0;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+        long long *r = st.dets + j * s.R;
+        long long f = r[s.W + s.L];
+        const long long det_bits = (1ll << NECI_FLAG_DETERMINISTIC_1) | (1ll << NECI_FLAG_DETERMINISTIC_2);
+        if (!(f & det_bits)) continue;
+        f &= ~det_bits;
+        bool occ = false;
+        for (int k = 0; k < s.L; ++k) occ = occ || fabs(word_to_double(r[s.W + k])) >= kEps12;
+        if (!occ) {
+            st.hash[st.slot_bucket[j]] = kTomb;
+            f |= 1ll;  // flag_removed
+            ++tomb;
+        }
+        r[s.W + s.L] = f;
+    }
+    if (tomb) atomicAdd(&st.ctl->n_tomb, tomb);
+}
+
 // One warp per core row: connected core determinants (excitation level 1-2).
 __global__ void k_core_count(DevSys s, const long long *core_dets, long long n_core, long long *counts) {
     const int lane = threadIdx.x & 31;
@@ -390,6 +416,7 @@ void launch_compress_out(Engine &e, long long *out, unsigned long long *n_out) {
     k_compress_out<<<gsz(e), 256, 0, e.stream>>>(e.sys, e.st, out, n_out, e.h_params->t_trunc_initiator,
                                                  e.h_params->t_init_coherent_rule);
 }
+void launch_core_unmark(Engine &e) { k_core_unmark<<<gsz(e), 256, 0, e.stream>>>(e.sys, e.st); }
 void launch_core_mark(Engine &e, const long long *core_dets, long long n_core) {
     k_core_mark<<<gsz(e), 128, 0, e.stream>>>(e.sys, e.st, core_dets, n_core);
 }
@@ -405,17 +432,25 @@ void launch_build_jk(Engine &e, double *jrow, double *jkrow, float *jrow32, floa
     k_build_jk<<<grid, 256, 0, e.stream>>>(e.sys, jrow, jkrow, jrow32, jkrow32);
 }
 
-void launch_pchb_build(Engine &e) {
+int launch_pchb_build(Engine &e) {
     const long long ntab = e.sys.ijMax * 3;
     const long long n = e.sys.abMax;
     const int threads = 128;
     const long long max_threads = (long long)gsz(e) * threads;
     const long long nthreads = ntab < max_threads ? ntab : max_threads;
     const int blocks = (int)((nthreads + threads - 1) / threads);
+    // the weight sums and the per-thread stacks of the alias construction
+    // (hundreds of MB at 100 spatial orbitals): no kernel runs unless both
+    // allocations succeeded
     double *wsum = nullptr;
     int32_t *scratch = nullptr;
-    cudaMalloc(&wsum, ntab * sizeof(double));
-    cudaMalloc(&scratch, (size_t)blocks * threads * 2 * n * sizeof(int32_t));
+    if (cudaMalloc(&wsum, ntab * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&scratch, (size_t)blocks * threads * 2 * n * sizeof(int32_t)) != cudaSuccess) {
+        const cudaError_t err = cudaGetLastError();  // clears the allocation error
+        if (wsum) cudaFree(wsum);
+        if (scratch) cudaFree(scratch);
+        return err == cudaSuccess ? (int)cudaErrorMemoryAllocation : (int)err;
+    }
     k_pchb_tables<<<blocks, threads, 0, e.stream>>>(e.sys, (double *)e.sys.alias_bias, (int32_t *)e.sys.alias_alias,
                                                     (double *)e.sys.alias_prob, (uint8_t *)e.sys.alias_present, wsum,
                                                     scratch);
@@ -429,9 +464,10 @@ void launch_pchb_build(Engine &e) {
     k_alias_rec<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, n, e.sys.alias_thr, e.sys.alias_prob,
                                               e.sys.alias_inv, e.sys.alias_alias, e.sys.tgt_pair,
                                               (AliasRec *)e.sys.alias_rec);
-    cudaStreamSynchronize(e.stream);
+    const cudaError_t err = cudaStreamSynchronize(e.stream);
     cudaFree(wsum);
     cudaFree(scratch);
+    return (int)err;
 }
 
 }  // namespace neci

@@ -117,6 +117,37 @@ class Engine:
         cd = np.ascontiguousarray(core_dets, dtype=np.int64)
         check(self.lib.neci_gpu_set_core_space(self.ctx, ptr(cd), cd.shape[0], precision))
 
+    def select_core(self, n_core: int, precision: int = capi.PREC_FP64) -> np.ndarray:
+        """Selects the n_core most populated determinants on the device
+        (neci_gpu_select_core) and makes them the core space; returns them."""
+        out = np.zeros((n_core, self.W), dtype=np.int64)
+        n = C.c_int64()
+        check(self.lib.neci_gpu_select_core(self.ctx, n_core, precision, ptr(out), C.byref(n)))
+        return out[: n.value]
+
+    def set_option(self, option: int, value: int):
+        check(self.lib.neci_gpu_set_option(self.ctx, option, value))
+
+    def autotune(self, params: capi.IterParams, steps_per_setting: int = 3):
+        """neci_gpu_autotune: times the candidate settings on live steps and
+        keeps the fastest.  Returns (stats of the steps run, the tuning kept);
+        the caller advances params.iter by len(stats)."""
+        cap = 16 * (steps_per_setting + 1)
+        arr = (capi.IterStats * cap)()
+        n = C.c_int32()
+        t = capi.Tuning()
+        check(self.lib.neci_gpu_autotune(self.ctx, C.byref(params), steps_per_setting, C.cast(arr, C.c_void_p),
+                                         cap, C.byref(n), C.byref(t)))
+        return list(arr[: n.value]), t
+
+    def tuning(self) -> capi.Tuning:
+        t = capi.Tuning()
+        check(self.lib.neci_gpu_get_tuning(self.ctx, C.byref(t)))
+        return t
+
+    def set_tuning(self, t: capi.Tuning):
+        check(self.lib.neci_gpu_set_tuning(self.ctx, C.byref(t)))
+
     def core_nnz(self) -> int:
         n = C.c_int64()
         check(self.lib.neci_gpu_core_nnz(self.ctx, C.byref(n)))

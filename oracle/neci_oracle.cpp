@@ -160,6 +160,15 @@ inline i64 as_word(double d) { i64 w; std::memcpy(&w, &d, 8); return w; }
 
 inline double fsign(double a, double b) { return b >= 0.0 ? std::fabs(a) : -std::fabs(a); }  // Fortran sign(a,b)
 
+// Partial sums of one core row in the core projection: the smallest power of
+// two G with 4 G at least the mean row length, at most 32 (the engine's
+// core_group_size).
+static int core_group_size(long long nnz, long long n_core) {
+    int g = 1;
+    while (g < 32 && 4ll * g * n_core < nnz) g <<= 1;
+    return g;
+}
+
 struct Oracle {
     neci_gpu_system sys{};
     int W = 1, L = 1, R = 3;  // det words, sign words, row words
@@ -609,7 +618,11 @@ struct Oracle {
     }
 
     // CreateSingleExcit (GenRandSymExcitNUMod.F90:1118-1243), C1 symmetry,
-    // tCycleOrbs = .false.: electron by rejection, hole by rejection.
+    // tCycleOrbs = .false.: the electron by rejection.  The hole is uniform
+    // over the unoccupied orbitals of the electron's spin, as the reference's
+    // rejection loop makes it (a uniform orbital of that spin, drawn again
+    // while occupied), but drawn as an index into those orbitals: one draw
+    // where the loop takes a variable number, the same distribution and pgen.
     // pgen returned including pSingles (UniformSingles_t / gen_exc_sd).
     template <typename Real>
     bool create_single_excit(const i64 *ilut, const std::vector<int> &nI, Stream &rng, Gen<Real> &g) const {
@@ -629,14 +642,16 @@ struct Oracle {
             if (nexcit != 0) break;
         }
         if (nexcit == 0) { g.pgen = 0; return false; }
-        int orb = 0;
-        bool found = false;
-        for (int attempts = 0; attempts <= 250; ++attempts) {
-            const int chosen = (int)uniform_index(rng, (u32)norbs);
-            orb = 2 * (chosen + 1) - (ispn - 1);
-            if (!orb_occ(ilut, orb)) { found = true; break; }
+        // the c-th (0-based) unoccupied orbital of spin ispn, in increasing order
+        const int c = (int)uniform_index(rng, (u32)nexcit);
+        int orb = 0, seen = 0;
+        for (int p = 1; p <= norbs && !orb; ++p) {
+            const int o = 2 * p - (ispn - 1);
+            if (orb_occ(ilut, o)) continue;
+            if (seen == c) orb = o;
+            ++seen;
         }
-        if (!found) { g.pgen = 0; return false; }
+        if (!orb) { g.pgen = 0; return false; }
         int e[2];
         make_single(nI, g.nJ, eleci, orb, e, g.par);
         g.ex[0][0] = e[0]; g.ex[1][0] = e[1];
@@ -1295,16 +1310,27 @@ struct IterRun {
         }
         st.n_spawned = (i64)spawns.size();
 
-        // ---- determ_projection_no_death (semi_stoch_procs.F90:290-365)
+        // ---- determ_projection_no_death (semi_stoch_procs.F90:290-365):
+        // y_i = -tau sum_j H_ij x_j.  The sum of a row is taken in G partial
+        // sums (G from the mean row length, as the engine's core kernel does):
+        // partial l adds the row's elements l, l+G, l+2G, ... in order with
+        // fused multiply-adds, then the partials are added pairwise, offsets
+        // G/2, G/4, ..., 1, into partial 0.
         std::vector<double> y(partial.size(), 0.0);
         if (semistoch) {
             const size_t nc = o.core_slots.size();
+            const int G = core_group_size((i64)o.core_val.size(), (i64)nc);
+            double part[32];
             for (size_t i = 0; i < nc; ++i) {
                 for (int k = 0; k < L; ++k) {
-                    double acc = 0.0;
-                    for (i64 e = o.core_rowptr[i]; e < o.core_rowptr[i + 1]; ++e)
-                        acc -= o.core_val[e] * partial[o.core_col[e] * L + k];
-                    y[i * L + k] = acc * p.tau;
+                    for (int l = 0; l < G; ++l) {
+                        part[l] = 0.0;
+                        for (i64 e = o.core_rowptr[i] + l; e < o.core_rowptr[i + 1]; e += G)
+                            part[l] = std::fma(-o.core_val[e], partial[o.core_col[e] * L + k], part[l]);
+                    }
+                    for (int off = G / 2; off > 0; off >>= 1)
+                        for (int l = 0; l < off; ++l) part[l] = part[l] + part[l + off];
+                    y[i * L + k] = part[0] * p.tau;
                 }
             }
         }

@@ -2,6 +2,9 @@
 own test inputs and recorded outputs (run where the reference tree exists;
 the fixtures are committed so that the tests do not need it).
 
+Usage: python make_golden.py REFERENCE_ROOT   (the root of a NECI checkout;
+the environment variable NECI_REFERENCE_ROOT may give it instead).
+
 * hehe_fcidump.npz -- integrals of test_suite/neci/serial/HeHe_Davidson_Direct_CI
   (FCIDUMP) and the exact ground-state energy NECI's Davidson printed for it
   ("GROUND E" in that directory's benchmark output).
@@ -30,7 +33,19 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE.parents[1]))
 from neci_stable_gb300.systems import read_fcidump  # noqa: E402
 
-REF = Path("/root/reference/test_suite/neci")
+
+
+def reference_suite(argv) -> Path:
+    """test_suite/neci of the NECI tree named on the command line or by
+    NECI_REFERENCE_ROOT."""
+    import os
+    root = argv[1] if len(argv) > 1 else os.environ.get("NECI_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit("usage: make_golden.py REFERENCE_ROOT (or set NECI_REFERENCE_ROOT)")
+    suite = Path(root) / "test_suite" / "neci"
+    if not suite.is_dir():
+        raise SystemExit(f"{suite} does not exist")
+    return suite
 
 
 def orbsym(path):
@@ -72,6 +87,7 @@ def save_pops(name, src_dir, binary):
 
 
 if __name__ == "__main__":
+    REF = reference_suite(sys.argv)
     save_pops("pops_text_li2.npz", REF / "tau_search" / "start_val" / "from_popsfile", binary=False)
     save_pops("pops_bin_ne.npz", REF / "serial" / "Ne_adi_Pops_min_si", binary=True)
     save_pops("pops_bin_beh_dneci.npz", REF.parent / "dneci" / "rdm" / "BeH_open_shell_dyn_core", binary=True)

@@ -57,6 +57,6 @@ def _c_layout(struct_name):
 
 @pytest.mark.parametrize("cls,name", [(capi.System, "neci_gpu_system"), (capi.IterParams, "neci_gpu_iter_params"),
                                       (capi.IterStats, "neci_gpu_iter_stats"),
-                                      (capi.TauStats, "neci_gpu_tau_stats")])
+                                      (capi.TauStats, "neci_gpu_tau_stats"), (capi.Tuning, "neci_gpu_tuning")])
 def test_struct_sizes_match_header(cls, name):
     assert C.sizeof(cls) == _c_layout(name)
