@@ -622,6 +622,41 @@ def run_reference(args, rank, world):
     }
 
 
+def profile_case(args):
+    """A short run for profilers: the headline molecule at --walkers walkers
+    with the excitation biases and tau where NECI's conventional tau search
+    leaves them on this workload (pSingles 0.53, pParallel 0.29, tau 0.023),
+    --equil FP64 steps with the shift following the population, then --steps
+    steps of the case named by --profile-case: fp64, mixed (FP32 spawn
+    amplitudes) or sort (the sort form of the annihilation)."""
+    import numpy as np
+    from neci_stable_gb300 import build as b
+    from neci_stable_gb300 import capi
+    from neci_stable_gb300.engine import Engine
+    b.build()
+    eng = Engine(workload_spec(), int(3 * args.walkers), int(4 * args.walkers))
+    eng.set_excit_biases(0.53, 0.29)
+    eng.start_from_reference(initial_part=args.walkers)
+    p = capi.default_params(tau=0.023, seed=5, iter=1)
+    shift, old = 0.0, args.walkers
+    for _ in range(args.equil // 10):
+        st = eng.iterate_n(p, 10)
+        p.iter += 10
+        parts = st[-1].tot_parts[0]
+        shift -= 0.1 * math.log(parts / old) / (p.tau * 10)
+        old = parts
+        p.diag_sft[0] = shift
+    if args.profile_case == "mixed":
+        p.precision = capi.PREC_MIXED
+    if args.profile_case == "sort":
+        eng.set_option(capi.OPT_ANNIHILATION, capi.ANN_SORT)
+    st = eng.iterate_n(p, args.steps)[-1]
+    print(json.dumps({"profile_case": args.profile_case, "walkers": st.tot_parts[0], "n_attempts": st.n_attempts,
+                      "n_spawned": st.n_spawned, "n_unique": st.n_unique, "n_new": st.n_new,
+                      "tot_walkers": st.tot_walkers}))
+    eng.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -637,7 +672,14 @@ def main():
     ap.add_argument("--instances", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=20)
     ap.add_argument("--batch-equil", type=int, default=200)
+    ap.add_argument("--profile-case", choices=["fp64", "mixed", "sort"], default=None,
+                    help="a short run of one case for a profiler (no timing, no JSON bench line)")
     args = ap.parse_args()
+    if args.profile_case:
+        if args.walkers is None:
+            args.walkers = 2e6
+        profile_case(args)
+        return
     args.warmup = max(args.warmup, 3)
     if args.walkers is None:
         args.walkers = WORKLOADS[args.workload]["walkers"]

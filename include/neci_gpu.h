@@ -209,13 +209,15 @@ int32_t neci_gpu_iterate_timed(neci_gpu_ctx *ctx, const neci_gpu_iter_params *pa
 
 /* Batched steps: n_iter iterations of each of n_ctx independent contexts
  * (one system and walker list each, e.g. instances of different size or
- * replica pairs), all on one device.  Each context runs its step graph on its
- * own stream, so the GPU executes the instances side by side; the result of
- * every instance is the same as when it is stepped alone.  params holds one
- * record per context; stats receives n_iter records per context (context-major);
- * *device_ms (may be NULL) the CUDA-event time of the whole batch.  The
- * reference runs such instances as separate jobs (replicas: the dneci/mneci
- * builds, CMakeLists.txt:97-106). */
+ * replica pairs), all on one device.  A step of the whole batch is one CUDA
+ * graph with one branch per context (its step's kernels), launched once per
+ * step, so the GPU executes the instances side by side; the graph is kept by
+ * the first context and rebuilt when a context's configuration changes.  The
+ * result of every instance is the same as when it is stepped alone.  params
+ * holds one record per context; stats receives n_iter records per context
+ * (context-major); *device_ms (may be NULL) the CUDA-event time of the whole
+ * batch.  The reference runs such instances as separate jobs (replicas: the
+ * dneci/mneci builds, CMakeLists.txt:97-106). */
 int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gpu_iter_params *params,
                                int32_t n_iter, neci_gpu_iter_stats *stats, double *device_ms);
 
@@ -378,7 +380,8 @@ int32_t neci_gpu_set_option(neci_gpu_ctx *ctx, int32_t option, int32_t value);
 typedef struct {
     int32_t annihilation;         /* NECI_ANN_HASH or NECI_ANN_SORT                            */
     int32_t spawn_blocks_per_sm;  /* blocks of 128 threads per SM in the spawn kernel's grid,
-                                     1..8 (8: every block the registers allow)                 */
+                                     1..16 (8, the default, is every block its registers
+                                     allow; more only queue behind the resident ones)         */
     int32_t table_shift;          /* hash form: the compression table of a step holds at least
                                      2^table_shift buckets per spawn onto an absent
                                      determinant (load factor 2^-table_shift), 1..4            */

@@ -4,6 +4,7 @@
 // host<->device copies and the launch sequence of one iteration (captured
 // once into a CUDA graph and replayed every step).
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstdio>
@@ -143,10 +144,18 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream); });
     stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, e.st.n_core > 0 ? 1 : 0); });
     if (e.sys.rdm) stage(e, K_RDM, [&] { launch_rdm(e, e.stream); });
-    stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, advance); });
+    stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, e.d_stat_pos, advance); });
 }
 
 // Destroys the cached step graphs (after any change the kernels see by value).
+// A value no context's step graphs have had before, in this process: a
+// batch graph built on a context that was freed (and whose address was
+// reused) can never match a new one.
+unsigned long long fresh_graph_version() {
+    static std::atomic<unsigned long long> counter{1};
+    return counter.fetch_add(1);
+}
+
 void drop_graphs(Engine &e) {
     for (int k = 0; k < 2; ++k)
         if (e.graphs[k]) {
@@ -154,6 +163,7 @@ void drop_graphs(Engine &e) {
             e.graphs[k] = nullptr;
         }
     e.graph = nullptr;
+    e.graph_version = fresh_graph_version();
 }
 
 // Makes e.graph the step graph of the current precision; one graph per
@@ -169,7 +179,7 @@ int ensure_graph(Engine &e) {
     if (!e.graphs[k]) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
-        step_sequence(e, e.d_stats + e.max_stats, 1);  // scratch record, copied out per step
+        step_sequence(e, e.d_stats, 1);  // each replay writes the next record (d_stat_pos)
         CK(cudaStreamEndCapture(e.stream, &g));
         CK(cudaGraphInstantiate(&e.graphs[k], g, 0));
         cudaGraphDestroy(g);
@@ -288,6 +298,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(e.d_params, 1);
     e.max_stats = 4096;
     A(e.d_stats, (size_t)e.max_stats + 1);
+    A(e.d_stat_pos, 1);
 #undef A
     if (rc == NECI_GPU_OK) {
         if (cudaMallocHost(&e.h_params, sizeof(IterParams)) != cudaSuccess ||
@@ -299,6 +310,9 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
         e.h_params->t_trunc_initiator = 1;  // CompressSpawnedList defaults for an initiator run
         e.h_params->t_init_coherent_rule = 1;
         for (int k = 0; k < 2 * K_NUM; ++k) cudaEventCreate(&e.ev[k]);
+        cudaEventCreateWithFlags(&e.fork_ev, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&e.join_ev, cudaEventDisableTiming);
+        e.graph_version = fresh_graph_version();
         if (cudaStreamSynchronize(e.stream) != cudaSuccess) rc = fail(NECI_GPU_ERR_CUDA, "sync after init");
     }
     if (rc == NECI_GPU_OK && configure_kernels(e) != 0)
@@ -317,6 +331,9 @@ int32_t neci_gpu_free(neci_gpu_ctx *ctx) {
     cudaSetDevice(e.device);
     if (e.stream) cudaStreamSynchronize(e.stream);
     drop_graphs(e);
+    if (e.batch_graph) cudaGraphExecDestroy(e.batch_graph);
+    if (e.fork_ev) cudaEventDestroy(e.fork_ev);
+    if (e.join_ev) cudaEventDestroy(e.join_ev);
     for (void *p : e.allocs) cudaFree(p);
     if (e.h_params) cudaFreeHost(e.h_params);
     if (e.h_stats) cudaFreeHost(e.h_stats);
@@ -381,8 +398,14 @@ int32_t neci_gpu_set_umat(neci_gpu_ctx *ctx, const double *u, int64_t len) {
     if (int r = dalloc(e, &jr32, n3)) return r;
     if (int r = dalloc(e, &kr32, n3)) return r;
     launch_build_jk(e, jr, kr, jr32, kr32);
+    double *jm = nullptr, *km = nullptr;
+    if (int r = dalloc(e, &jm, (size_t)e.sys.nBI * e.sys.nBI)) return r;
+    if (int r = dalloc(e, &km, (size_t)e.sys.nBI * e.sys.nBI)) return r;
+    launch_build_jkmat(e, jm, km);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e.stream));
+    e.sys.jmat = jm;
+    e.sys.kmat = km;
     e.sys.jrow = jr;
     e.sys.jkrow = kr;
     e.sys.jrow32 = jr32;
@@ -798,15 +821,12 @@ static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_
         if (!e.profiling)
             if (int r = ensure_graph(e)) return r;
         const int batch = std::min(n_iter - done, e.max_stats);
+        CK(cudaMemsetAsync(e.d_stat_pos, 0, sizeof(int), e.stream));
         if (device_ms) CK(cudaEventRecord(e.ev[0], e.stream));
         if (e.profiling) {
-            for (int i = 0; i < batch; ++i) step_sequence(e, e.d_stats + i, 1);
+            for (int i = 0; i < batch; ++i) step_sequence(e, e.d_stats, 1);
         } else {
-            for (int i = 0; i < batch; ++i) {
-                CK(cudaGraphLaunch(e.graph, e.stream));
-                CK(cudaMemcpyAsync(e.d_stats + i, e.d_stats + e.max_stats, sizeof(neci_gpu_iter_stats),
-                                   cudaMemcpyDeviceToDevice, e.stream));
-            }
+            for (int i = 0; i < batch; ++i) CK(cudaGraphLaunch(e.graph, e.stream));
         }
         if (device_ms) CK(cudaEventRecord(e.ev[1], e.stream));
         CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats) * batch, cudaMemcpyDeviceToHost, e.stream));
@@ -862,36 +882,66 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
     }
     CK(cudaSetDevice(dev));
+    Engine &e0 = ctxs[0]->e;
+    // What every branch captures: its context's kernels as its parameters and
+    // state choose them (precision, sweep instance, core space; the rest
+    // changes the context's graph version)
+    std::vector<std::pair<const void *, unsigned long long>> key;
     for (int c = 0; c < n_ctx; ++c) {
         Engine &e = ctxs[c]->e;
         copy_params(*e.h_params, params[c]);
-        CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
-        if (int r = ensure_graph(e)) return r;
+        const unsigned long long v = e.graph_version * 8 + (e.h_params->precision == NECI_PREC_MIXED ? 4 : 0) +
+                                     (sweep_fast(*e.h_params) ? 2 : 0) + (e.st.n_core > 0 ? 1 : 0);
+        key.push_back({(const void *)ctxs[c], v});
     }
-    // a start event on the first context's stream that every stream waits on,
-    // and every stream's end recorded back onto it, brackets the whole batch
-    Engine &e0 = ctxs[0]->e;
-    CK(cudaEventRecord(e0.ev[0], e0.stream));
-    for (int c = 1; c < n_ctx; ++c) CK(cudaStreamWaitEvent(ctxs[c]->e.stream, e0.ev[0], 0));
-    // issue step by step across contexts so that the streams advance together
-    for (int i = 0; i < n_iter; ++i)
-        for (int c = 0; c < n_ctx; ++c) {
-            Engine &e = ctxs[c]->e;
-            CK(cudaGraphLaunch(e.graph, e.stream));
-            CK(cudaMemcpyAsync(e.d_stats + i, e.d_stats + e.max_stats, sizeof(neci_gpu_iter_stats),
-                               cudaMemcpyDeviceToDevice, e.stream));
+    if (!e0.batch_graph || e0.batch_key != key) {
+        // One graph for a step of the whole batch: the first context's stream
+        // forks to every other context's stream, each stream captures its
+        // context's step, and all join back; the instances run side by side
+        // and the batch is one launch per step.
+        if (e0.batch_graph) {
+            cudaGraphExecDestroy(e0.batch_graph);
+            e0.batch_graph = nullptr;
         }
+        e0.batch_key.clear();
+        CK(cudaStreamBeginCapture(e0.stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t ce = cudaEventRecord(e0.fork_ev, e0.stream);
+        for (int c = 1; c < n_ctx && ce == cudaSuccess; ++c) ce = cudaStreamWaitEvent(ctxs[c]->e.stream, e0.fork_ev, 0);
+        if (ce == cudaSuccess)
+            for (int c = 0; c < n_ctx; ++c) step_sequence(ctxs[c]->e, ctxs[c]->e.d_stats, 1);
+        for (int c = 1; c < n_ctx && ce == cudaSuccess; ++c) {
+            Engine &e = ctxs[c]->e;
+            ce = cudaEventRecord(e.join_ev, e.stream);
+            if (ce == cudaSuccess) ce = cudaStreamWaitEvent(e0.stream, e.join_ev, 0);
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ee = cudaStreamEndCapture(e0.stream, &g);  // ends the capture whatever happened
+        if (ce == cudaSuccess) ce = ee;
+        if (ce == cudaSuccess) ce = cudaGraphInstantiate(&e0.batch_graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (ce != cudaSuccess) {
+            e0.batch_graph = nullptr;
+            (void)cudaGetLastError();
+            return fail(NECI_GPU_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(ce));
+        }
+        e0.batch_key = key;
+    }
+    // parameters in, record counters reset, then one launch per step; the
+    // whole batch runs in the first context's stream order
+    for (int c = 0; c < n_ctx; ++c) {
+        Engine &e = ctxs[c]->e;
+        CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e0.stream));
+        CK(cudaMemsetAsync(e.d_stat_pos, 0, sizeof(int), e0.stream));
+    }
+    CK(cudaEventRecord(e0.ev[0], e0.stream));
+    for (int i = 0; i < n_iter; ++i) CK(cudaGraphLaunch(e0.batch_graph, e0.stream));
+    CK(cudaEventRecord(e0.ev[1], e0.stream));
     for (int c = 0; c < n_ctx; ++c) {
         Engine &e = ctxs[c]->e;
         CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats) * n_iter, cudaMemcpyDeviceToHost,
-                           e.stream));
-        if (c > 0) {
-            CK(cudaEventRecord(e.ev[1], e.stream));
-            CK(cudaStreamWaitEvent(e0.stream, e.ev[1], 0));
-        }
+                           e0.stream));
     }
-    CK(cudaEventRecord(e0.ev[1], e0.stream));
-    for (int c = 0; c < n_ctx; ++c) CK(cudaStreamSynchronize(ctxs[c]->e.stream));
+    CK(cudaStreamSynchronize(e0.stream));
     CK(cudaGetLastError());
     if (device_ms) {
         float ms = 0.0f;
@@ -936,7 +986,7 @@ int32_t neci_gpu_annihilate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, co
     e.fuse_mode = mode;
     launch_ann_insert(e, e.stream);
     launch_merge_stats(e, e.stream, 0);
-    launch_final(e, e.stream, e.d_stats, 0);
+    launch_final(e, e.stream, e.d_stats, nullptr, 0);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats), cudaMemcpyDeviceToHost, e.stream));
     CK(cudaStreamSynchronize(e.stream));
@@ -1108,6 +1158,7 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     dfree(e, st.core_col);
     dfree(e, st.core_val);
     dfree(e, st.core_val32);
+    dfree(e, st.core_dets);
     if (!st.core_of_slot) {
         if (int r = dalloc(e, &st.core_of_slot, (size_t)st.max_walkers)) return r;
     }
@@ -1126,6 +1177,8 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     if (int r = dalloc(e, &st.core_x, (size_t)n_core * L)) return r;
     if (int r = dalloc(e, &st.core_y, (size_t)n_core * L)) return r;
     if (int r = dalloc(e, &st.core_rowptr, (size_t)n_core + 1)) return r;
+    if (int r = dalloc(e, &st.core_dets, (size_t)n_core * e.sys.W)) return r;
+    CK(cudaMemcpyAsync(st.core_dets, dcore, (size_t)n_core * e.sys.W * 8, cudaMemcpyDeviceToDevice, e.stream));
     if (int r = dalloc(e, &tmp.counts, (size_t)n_core)) return r;
     long long *const counts = tmp.counts;
     CK(cudaMemsetAsync(&st.ctl->err, 0, sizeof(int), e.stream));
@@ -1191,9 +1244,9 @@ int alloc_sort_buffers(Engine &e) {
 // again with them).
 int apply_tuning(Engine &e, const neci_gpu_tuning &t) {
     if ((t.annihilation != NECI_ANN_HASH && t.annihilation != NECI_ANN_SORT) || t.spawn_blocks_per_sm < 1 ||
-        t.spawn_blocks_per_sm > 8 || t.table_shift < 1 || t.table_shift > 4 || t.sort_blocks_per_sm < 1 ||
+        t.spawn_blocks_per_sm > 16 || t.table_shift < 1 || t.table_shift > 4 || t.sort_blocks_per_sm < 1 ||
         t.sort_blocks_per_sm > 4)
-        return fail(NECI_GPU_ERR_INVALID, "tuning out of range: annihilation NECI_ANN_*, spawn blocks per SM 1..8, "
+        return fail(NECI_GPU_ERR_INVALID, "tuning out of range: annihilation NECI_ANN_*, spawn blocks per SM 1..16, "
                                           "table shift 1..4, sort blocks per SM 1..4");
     e.sort_bpsm = t.sort_blocks_per_sm;
     if (t.annihilation == NECI_ANN_SORT)

@@ -136,6 +136,11 @@ struct DevSys {
     // FP32 copies are the FP64 values rounded once
     const double *jrow, *jkrow;
     const float *jrow32, *jkrow32;
+    // Coulomb and exchange integrals of spatial orbital pairs for the
+    // diagonal element: jmat[(i-1) n + (j-1)] = <ij|ij>, kmat[...] = <ij|ji>,
+    // the UMAT values sltcnd_0 reads, in n^2 doubles each (L1-resident for
+    // n up to about 64)
+    const double *jmat, *kmat;
     // 1/p_gen of a uniform single with `count` allowed (electron, hole)
     // pairs: [count] = count * (1 / pSingles), FP64 and FP32
     const double *inv_single;
@@ -202,6 +207,7 @@ struct DevState {
     double *core_x, *core_y;
     long long *core_rowptr;
     int core_group;                // lanes that sum one core row (core_group_size)
+    long long *core_dets;          // W words of each core determinant (2-RDM core pairs)
     // sort form of the annihilation: 32-bit sort keys and record indices
     // (two buffers each, ping-ponged by the radix passes), the 64-bit NECI
     // hash of every record, per-block digit counts of a radix pass, and the
@@ -273,6 +279,35 @@ __host__ __device__ inline void philox_block(const uint32_t ctr[4], const uint32
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
+// Two Philox-4x32-10 blocks of one key, computed side by side: the rounds of
+// the two counters are independent, so their multiply-xor chains overlap
+// instead of following each other (each block equals philox_block's).
+__host__ __device__ inline void philox_pair(const uint32_t ctr_a[4], const uint32_t ctr_b[4], const uint32_t key[2],
+                                            uint32_t out_a[4], uint32_t out_b[4]) {
+    uint32_t a0 = ctr_a[0], a1 = ctr_a[1], a2 = ctr_a[2], a3 = ctr_a[3];
+    uint32_t b0 = ctr_b[0], b1 = ctr_b[1], b2 = ctr_b[2], b3 = ctr_b[3];
+    uint32_t k0 = key[0], k1 = key[1];
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const unsigned long long pa0 = (unsigned long long)0xD2511F53u * a0;
+        const unsigned long long pa1 = (unsigned long long)0xCD9E8D57u * a2;
+        const unsigned long long pb0 = (unsigned long long)0xD2511F53u * b0;
+        const unsigned long long pb1 = (unsigned long long)0xCD9E8D57u * b2;
+        a0 = (uint32_t)(pa1 >> 32) ^ a1 ^ k0;
+        a1 = (uint32_t)pa1;
+        a2 = (uint32_t)(pa0 >> 32) ^ a3 ^ k1;
+        a3 = (uint32_t)pa0;
+        b0 = (uint32_t)(pb1 >> 32) ^ b1 ^ k0;
+        b1 = (uint32_t)pb1;
+        b2 = (uint32_t)(pb0 >> 32) ^ b3 ^ k1;
+        b3 = (uint32_t)pb0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out_a[0] = a0; out_a[1] = a1; out_a[2] = a2; out_a[3] = a3;
+    out_b[0] = b0; out_b[1] = b1; out_b[2] = b2; out_b[3] = b3;
+}
+
 __host__ __device__ inline unsigned long long splitmix64(unsigned long long x) {
     x += 0x9E3779B97F4A7C15ull;
     unsigned long long z = x;
@@ -292,10 +327,11 @@ __host__ __device__ inline unsigned long long det_key(const unsigned long long *
 
 // One stream of 64-bit draws for (determinant, iteration, purpose, run,
 // attempt).  Every draw consumes one 64-bit value; a Philox block gives two.
+// The draws not yet taken are buf[4 - have .. 3].
 struct Stream {
     uint32_t key[2];
     uint32_t ctr[4];
-    unsigned long long buf[2];
+    unsigned long long buf[4];
     int have;
     __device__ inline Stream(unsigned long long dkey, long long iter, uint32_t purpose, uint32_t run, uint32_t attempt) {
         key[0] = (uint32_t)dkey;
@@ -311,13 +347,30 @@ struct Stream {
             uint32_t o[4];
             philox_block(ctr, key, o);
             ctr[1] += 1;
-            buf[0] = ((unsigned long long)o[1] << 32) | o[0];
-            buf[1] = ((unsigned long long)o[3] << 32) | o[2];
+            buf[2] = ((unsigned long long)o[1] << 32) | o[0];
+            buf[3] = ((unsigned long long)o[3] << 32) | o[2];
             have = 2;
         }
-        const unsigned long long v = (have == 2) ? buf[0] : buf[1];
+        // buf[4 - have] by selects: an array indexed at run time would live
+        // in local memory
+        const unsigned long long v = have == 4 ? buf[0] : (have == 3 ? buf[1] : (have == 2 ? buf[2] : buf[3]));
         --have;
         return v;
+    }
+    // When no draw is left, the next two blocks at once (philox_pair): a
+    // caller that will take four more draws gets them with the two blocks'
+    // round chains overlapped.  The draws are the same as one block at a time.
+    __device__ inline void fill_pair() {
+        if (have != 0) return;
+        uint32_t c2[4] = {ctr[0], ctr[1] + 1u, ctr[2], ctr[3]};
+        uint32_t o[4], q[4];
+        philox_pair(ctr, c2, key, o, q);
+        ctr[1] += 2;
+        buf[0] = ((unsigned long long)o[1] << 32) | o[0];
+        buf[1] = ((unsigned long long)o[3] << 32) | o[2];
+        buf[2] = ((unsigned long long)q[1] << 32) | q[0];
+        buf[3] = ((unsigned long long)q[3] << 32) | q[2];
+        have = 4;
     }
     // genrand_real2 equivalent: a double in [0, 1) from 53 bits
     __device__ inline double next() { return (double)(next64() >> 11) * 0x1.0p-53; }
@@ -325,7 +378,7 @@ struct Stream {
     // rest of the first Philox block): the next draw returns `second`.
     __device__ inline void resume_second(unsigned long long second) {
         ctr[1] = 1;
-        buf[1] = second;
+        buf[3] = second;
         have = 1;
     }
 };
@@ -597,14 +650,15 @@ __device__ inline double sltcnd_0(const DevSys &s, const unsigned long long *d, 
             const int oi = wi * 64 + __ffsll((long long)xi);
             xi &= xi - 1;
             double t = 0.0;
+            const size_t ri = (size_t)(spat(oi) - 1) * s.nBI - 1;
             NECI_FOR_WORDS(wj, W) {
                 if (wj < wi) continue;
                 unsigned long long xj = wj == wi ? xi : d[wj];  // the electrons after i
                 while (xj) {
                     const int oj = wj * 64 + __ffsll((long long)xj);
                     xj &= xj - 1;
-                    t += umat_el(s, spat(oi), spat(oj), spat(oi), spat(oj));
-                    if (beta(oi) == beta(oj)) hel_tmp -= umat_el(s, spat(oi), spat(oj), spat(oj), spat(oi));
+                    t += __ldg(&s.jmat[ri + spat(oj)]);  // <ij|ij>
+                    if (beta(oi) == beta(oj)) hel_tmp -= __ldg(&s.kmat[ri + spat(oj)]);  // <ij|ji>
                 }
             }
             hel_doub += t;  // the last electron adds t = 0

@@ -245,6 +245,9 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
     // Both spin cases run the same instructions (selects, no branches), so a
     // warp whose lanes drew different cases stays converged.
     const bool par = rng.next64() < s.thr_bias;
+    // the pair index, the exchange draw, the alias draw and the spawn's
+    // rounding draw follow: two Philox blocks, computed side by side
+    rng.fill_pair();
     e.cls = par ? TC_PAR : TC_OPP;
     const int idx = (int)uniform_index(rng, par ? (unsigned)(aa + bb) : (unsigned)(s.nOccAlpha * s.nOccBeta));
     // parallel pair: positions a1 > a2 among the electrons of one spin

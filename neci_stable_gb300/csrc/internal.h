@@ -57,6 +57,15 @@ struct Engine {
     neci_gpu_iter_stats *d_stats = nullptr;  // per-step records
     neci_gpu_iter_stats *h_stats = nullptr;  // pinned
     int max_stats = 0;
+    int *d_stat_pos = nullptr;               // the next record a step writes (k_final)
+    // changes with every drop of the step graphs (a batch graph built on them
+    // is rebuilt)
+    unsigned long long graph_version = 0;
+    // a batch graph (neci_gpu_iterate_batch) kept by the batch's first
+    // context: every instance's step as one branch, and what it was built for
+    cudaGraphExec_t batch_graph = nullptr;
+    std::vector<std::pair<const void *, unsigned long long>> batch_key;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::vector<void *> allocs;
     bool have_ref = false, have_pchb = false;
     double *inv_single = nullptr;  // device table of DevSys::inv_single
@@ -96,7 +105,7 @@ void launch_ann_probe(Engine &e, cudaStream_t s);
 void launch_ann_compress(Engine &e, cudaStream_t s);
 void launch_ann_insert(Engine &e, cudaStream_t s);
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core);
-void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter);
+void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter);
 void launch_rdm(Engine &e, cudaStream_t s);
 
 // sort form of the annihilation and core selection (sort_kernels.cu)
@@ -128,5 +137,6 @@ void launch_core_fill(Engine &e, const long long *core_dets, long long n_core);
 // nothing when its scratch cannot be allocated
 int launch_pchb_build(Engine &e);
 void launch_build_jk(Engine &e, double *jrow, double *jkrow, float *jrow32, float *jkrow32);
+void launch_build_jkmat(Engine &e, double *jmat, double *kmat);
 
 }  // namespace neci

@@ -1270,6 +1270,38 @@ __global__ void __launch_bounds__(256) k_rdm_offdiag(DevSys s, DevState st) {
     }
 }
 
+// Pairs of core determinants (fill_RDM_offdiag_deterministic,
+// rdm_filling.F90:947-1111): spawns between core determinants do not happen
+// (the deterministic projection replaces them), so every stored off-diagonal
+// element (i, j) of the core Hamiltonian adds, with parent i and child j,
+//   1/2 (x_i^1 C_j^2 + x_i^2 C_j^1),
+// the expectation of what the two runs' spawns from i onto j would add:
+// x_i the parent's amplitudes at the start of the step (the core vector), C_j
+// the child's after annihilation.  NECI adds C_i^2 C_j^1 per ordered pair,
+// with averaged signs; over both orders the sums agree, and the host
+// symmetrises.  One warp per core row.
+__global__ void __launch_bounds__(256) k_rdm_core(DevSys s, DevState st) {
+    if (halted(st)) return;
+    const int W = s.W, R = s.R;
+    const int lane = threadIdx.x & 31;
+    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long i = warp; i < st.n_core; i += nwarps) {
+        unsigned long long pd[kMaxWords];
+        NECI_FOR_WORDS(w, W) pd[w] = (unsigned long long)st.core_dets[i * W + w];
+        const double x1 = st.core_x[i * 2], x2 = st.core_x[i * 2 + 1];
+        for (long long e = st.core_rowptr[i] + lane; e < st.core_rowptr[i + 1]; e += 32) {
+            const long long j = st.core_col[e];
+            const long long *rj = st.dets + st.core_slot[j] * R;
+            const double c = 0.5 * (x1 * word_to_double(rj[W + 1]) + x2 * word_to_double(rj[W]));
+            if (c == 0.0) continue;
+            unsigned long long cd[kMaxWords];
+            NECI_FOR_WORDS(w, W) cd[w] = (unsigned long long)st.core_dets[j * W + w];
+            rdm_add_pair(s, st, pd, cd, c);
+        }
+    }
+}
+
 // Diagonal terms; per-block sums in shared memory when npair doubles fit.
 __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use_shared) {
     if (halted(st)) return;
@@ -1305,8 +1337,18 @@ __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use
 // ===========================================================================
 // k_final: write the step's stats record.
 // ===========================================================================
-__global__ void k_final(DevState st, neci_gpu_iter_stats *out, IterParams *pp, int advance_iter, long long n_core) {
+// The record goes to out[*pos] (and *pos advances, up to max_out - 1) when
+// pos is given: the step graph is the same for every step of a batch, and
+// each step's record lands in its own place.
+__global__ void k_final(DevState st, neci_gpu_iter_stats *base, int *pos, int max_out, IterParams *pp,
+                        int advance_iter, long long n_core) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    neci_gpu_iter_stats *out = base;
+    if (pos) {
+        const int k = *pos;
+        out = base + (k < max_out ? k : max_out - 1);
+        *pos = k + 1;
+    }
     Control *c = st.ctl;
     if (c->halted) {
         // a previous step failed: report its status again, change nothing
@@ -1476,13 +1518,14 @@ void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
 void launch_rdm(Engine &e, cudaStream_t s) {
     if (!e.sys.rdm) return;
     k_rdm_offdiag<<<grid_spawns(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
+    if (e.st.n_core > 0) k_rdm_core<<<clamp_grid(e.st.n_core / 8 + 1, e.num_sms * 8), 256, 0, s>>>(e.sys, e.st);
     const size_t shm = (size_t)e.sys.npair * sizeof(double);
     const int use_shared = shm <= 48 * 1024 ? 1 : 0;  // the default dynamic shared-memory limit
     k_rdm_diag<<<grid_slots(e), 256, use_shared ? shm : 0, s>>>(e.sys, e.st, use_shared);
 }
 
-void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int advance_iter) {
-    k_final<<<1, 32, 0, s>>>(e.st, out, e.d_params, advance_iter, e.st.n_core);
+void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter) {
+    k_final<<<1, 32, 0, s>>>(e.st, out, pos, e.max_stats, e.d_params, advance_iter, e.st.n_core);
 }
 
 }  // namespace neci

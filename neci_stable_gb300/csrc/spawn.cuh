@@ -260,8 +260,15 @@ __device__ inline Stream load_queued(const DevSys &s, const DevState &st, const 
 // nBasis is a multiple of 64.  Excitations are generated on NW words; the
 // determinant key, the records and the row offsets use all RW.  NW = RW = 0
 // is the instance for any size, with the counts read from the system.
+// Resident blocks of 128 threads per SM the spawn kernel is compiled for:
+// its register cap is 65536 / (128 x this).
+#ifndef NECI_SPAWN_BLOCKS_PER_SM
+#define NECI_SPAWN_BLOCKS_PER_SM 8
+#endif
+
 template <typename Real, int GEN, int NW, int RW, bool QD>
-__global__ void __launch_bounds__(128, 8) k_spawn(DevSys s, DevState st, const IterParams *pp, int fuse_probe) {
+__global__ void __launch_bounds__(128, NECI_SPAWN_BLOCKS_PER_SM)
+    k_spawn(DevSys s, DevState st, const IterParams *pp, int fuse_probe) {
     if (halted(st)) return;
     // lattice systems only: their singles spawn often enough to fill the
     // lookup's lanes; the molecular instances carry no fused code

@@ -285,6 +285,17 @@ __global__ void k_build_jk(DevSys s, double *jrow, double *jkrow, float *jrow32,
     }
 }
 
+// The Coulomb and exchange tables of the diagonal element (DevSys::jmat, kmat).
+__global__ void k_build_jkmat(DevSys s, double *jmat, double *kmat) {
+    const int n = s.nBI;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < (long long)n * n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(t / n) + 1, j = (int)(t % n) + 1;
+        jmat[t] = s.umat[umat_ind(i, j, i, j) - 1];
+        kmat[t] = s.umat[umat_ind(i, j, j, i) - 1];
+    }
+}
+
 __global__ void k_pchb_tables(DevSys s, double *bias, int32_t *alias, double *prob, uint8_t *present,
                               double *wsum, int32_t *scratch) {
     const long long ntab = s.ijMax * 3;
@@ -430,6 +441,10 @@ void launch_build_jk(Engine &e, double *jrow, double *jkrow, float *jrow32, floa
     const long long n = e.sys.nBI;
     const int grid = (int)std::min<long long>((n * n * n + 255) / 256, 4096);
     k_build_jk<<<grid, 256, 0, e.stream>>>(e.sys, jrow, jkrow, jrow32, jkrow32);
+}
+void launch_build_jkmat(Engine &e, double *jmat, double *kmat) {
+    const long long n = e.sys.nBI;
+    k_build_jkmat<<<(int)std::min<long long>((n * n + 255) / 256, 1024), 256, 0, e.stream>>>(e.sys, jmat, kmat);
 }
 
 int launch_pchb_build(Engine &e) {

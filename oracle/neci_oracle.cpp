@@ -1126,6 +1126,21 @@ struct IterRun {
             o.decode_bit_det(ev.parent.data(), nI);
             rdm_add_pair(nI, nJ, 0.5 * ev.w * cj);
         }
+        // core pairs (fill_RDM_offdiag_deterministic, rdm_filling.F90:947-1111):
+        // every stored off-diagonal element (i, j) of the core Hamiltonian, with
+        // parent i at its amplitudes before the step and child j after it,
+        // adds 1/2 (x_i^1 C_j^2 + x_i^2 C_j^1), what the two runs' spawns from
+        // i onto j would add in expectation (those spawns are not made)
+        for (size_t i = 0; i < o.core_slots.size(); ++i) {
+            o.decode_bit_det(o.row(o.core_slots[i]), nI);
+            for (i64 e = o.core_rowptr[i]; e < o.core_rowptr[i + 1]; ++e) {
+                const i64 *rj = o.row(o.core_slots[o.core_col[e]]);
+                const double c = 0.5 * (partial[i * 2] * o.get_sign(rj, 1) + partial[i * 2 + 1] * o.get_sign(rj, 0));
+                if (c == 0.0) continue;
+                o.decode_bit_det(rj, nJ);
+                rdm_add_pair(nI, nJ, c);
+            }
+        }
         for (i64 j = 0; j < o.TotWalkers; ++j) {
             const i64 *r = o.row(j);
             const double prod = o.get_sign(r, 0) * o.get_sign(r, 1);

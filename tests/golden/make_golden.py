@@ -13,6 +13,10 @@ the environment variable NECI_REFERENCE_ROOT may give it instead).
   its blocking error that NECI's run recorded ("Total projected energy"),
   plus the core energy after freezing ("ECORE now") and the reference
   energy ("<D0|H|D0>=") that the same run printed.
+* rdm_fci_core.npz -- integrals of test_suite/dneci/rdm/full_CI+AAS+RDMs
+  (FCIDUMP: 6 spatial orbitals, 6 electrons) and the 2-RDM energy that NECI's
+  two recorded runs printed ("*TOTAL ENERGY* CALCULATED USING THE *REDUCED
+  DENSITY MATRICES*"), with the whole space as the semistochastic core.
 * pops_*.npz -- POPSFILEs that NECI wrote in its test suite (text
   test_suite/neci/tau_search/start_val/from_popsfile/POPSFILE; binary
   POPSFILEHEAD/POPSFILEBIN of test_suite/neci/serial/Ne_adi_Pops_min_si and
@@ -69,6 +73,20 @@ def save(name, src_dir, pattern, key, extra=None):
     print(name, h.shape, vals, more)
 
 
+def save_rdm(name, src_dir):
+    """The FCIDUMP of an RDM test and the RDM energy of each recorded run."""
+    fcidump = src_dir / "FCIDUMP"
+    h, eri, ecore, nelec, ms2 = read_fcidump(fcidump)
+    energies = []
+    for bench in sorted(glob.glob(str(src_dir / "benchmark*"))):
+        text = open(bench).read()
+        m = re.search(r"\*TOTAL ENERGY\* CALCULATED USING THE \*REDUCED DENSITY MATRICES\*:\s*(-?[\d.]+E[+-]\d+)", text)
+        energies.append(float(m.group(1)))
+    np.savez_compressed(HERE / name, h=h, eri=eri.astype(np.float64), ecore=ecore, nelec=nelec, ms2=ms2,
+                        orbsym=orbsym(fcidump), rdm_energy=np.array(energies))
+    print(name, h.shape, energies)
+
+
 def save_pops(name, src_dir, binary):
     import hashlib
     from neci_stable_gb300 import popsfile
@@ -88,6 +106,7 @@ def save_pops(name, src_dir, binary):
 
 if __name__ == "__main__":
     REF = reference_suite(sys.argv)
+    save_rdm("rdm_fci_core.npz", REF.parent / "dneci" / "rdm" / "full_CI+AAS+RDMs")
     save_pops("pops_text_li2.npz", REF / "tau_search" / "start_val" / "from_popsfile", binary=False)
     save_pops("pops_bin_ne.npz", REF / "serial" / "Ne_adi_Pops_min_si", binary=True)
     save_pops("pops_bin_beh_dneci.npz", REF.parent / "dneci" / "rdm" / "BeH_open_shell_dyn_core", binary=True)
