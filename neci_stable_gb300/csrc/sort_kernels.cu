@@ -20,7 +20,7 @@
 //                its sums, counts and initiator bits in acc/meta (the found
 //                branch, merged by k_merge_stats), an absent one becomes a
 //                new unique determinant for k_ann_insert
-//   k_sk_long    the same for longer runs, one warp per run
+//   k_sk_long    the same for longer runs, one block per run
 // The result is the hash form's, bit for bit: the same sums, the same flag
 // rules (FindResidualParticle's coherent rule and initiator bits, from the
 // per-run counts) and the same statistics.
@@ -207,84 +207,134 @@ __global__ void __launch_bounds__(256) k_sk_group(DevSys s, DevState st, int loo
 }
 
 // ---------------------------------------------------------------------------
-// k_sk_long: runs longer than kShortRun, one warp per run.  The run's end is
-// found 32 positions at a time; then groups are formed round by round: the
-// first element not yet in a group leads, every element with its
-// determinant joins (marked in bit 31 of its index), and the group's sums are
-// reduced across the warp.  A run of one determinant (the usual case: one
-// determinant with many spawns) takes one round.
+// k_sk_long: runs longer than kShortRun, one block per run.
+// The run's end is found by warp 0 with a 32-way search: probes 1, 32,
+// 1024, ... positions apart until one holds another key, then 32-way
+// refinement (two probes per factor of 32 in the run's length).  Groups are
+// then formed round by round: the first element not yet in a group leads,
+// the whole block compares every element of the run with it, marks the
+// members (bit 31 of the index) and sums them; the smallest position of an
+// element that is neither marked nor a member leads the next round.  A run
+// of one determinant (the usual case: one determinant with many spawns, the
+// reference above all) takes one round, whose pass is spread over the block.
 // ---------------------------------------------------------------------------
+constexpr int kLongThreads = 256;
+constexpr int kLongItems = 4;  // elements per thread in flight in a pass
+
 template <int LR>
-__global__ void __launch_bounds__(256) k_sk_long(DevSys s, DevState st, int lookup, int cur) {
+__global__ void __launch_bounds__(kLongThreads) k_sk_long(DevSys s, DevState st, int lookup, int cur) {
     if (halted(st)) return;
+    constexpr int NW = kLongThreads / 32;
+    __shared__ long long s_p1, s_next[NW];
+    __shared__ unsigned long long s_q[NW][2], s_c[NW][2], s_nrec[NW];
+    __shared__ uint32_t s_init[NW];
     Control *c = st.ctl;
     const long long n = spawn_count(st);
     const uint32_t *key = st.sk_key[cur];
     uint32_t *val = st.sk_val[cur];
     const int W = s.W, R = s.R;
     constexpr int L = LR;
-    const int lane = threadIdx.x & 31;
-    const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-    const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const unsigned long long nlong = min(c->n_long, (unsigned long long)st.max_spawned);
-    for (unsigned long long r = warp; r < nlong; r += nwarps) {  // warp-uniform
+    constexpr long long kNone = 0x7FFFFFFFFFFFFFFFll;
+    for (unsigned long long r = blockIdx.x; r < nlong; r += gridDim.x) {  // block-uniform
         const long long p0 = (long long)st.sk_long[r];
-        const uint32_t k0 = key[p0];
-        // the run's end: the first position past p0 with another key (the keys
-        // are sorted; the first kShortRun + 1 positions are known to hold k0)
-        long long p1 = n;
-        for (long long base = p0 + kShortRun + 1; base < n; base += 32) {
-            const long long q = base + lane;
-            const unsigned int m = __ballot_sync(0xffffffffu, q >= n || key[q] != k0);
-            if (m) {
-                p1 = min(n, base + __ffs((int)m) - 1);
-                break;
-            }
-        }
-        for (long long rounds = 0; rounds <= p1 - p0; ++rounds) {  // at most one group per element
-            // the first element not yet in a group
-            long long f = -1;
-            for (long long base = p0; base < p1; base += 32) {
-                const long long q = base + lane;
-                const unsigned int m = __ballot_sync(0xffffffffu, q < p1 && !(val[q] & 0x80000000u));
+        if (wid == 0) {
+            const uint32_t k0 = key[p0];
+            // key[lo] == k0 throughout; the first position with another key
+            // (or n) lies in (lo, lo + 32 * step] once a probe has found one
+            long long lo = p0 + kShortRun, step = 1;
+            for (;;) {
+                const long long q = lo + (long long)(lane + 1) * step;
+                const unsigned int m = __ballot_sync(0xffffffffu, q >= n || key[q] != k0);
                 if (m) {
-                    f = base + __ffs((int)m) - 1;
+                    lo += (long long)(__ffs((int)m) - 1) * step;
                     break;
                 }
+                lo += 32 * step;
+                step *= 32;
             }
-            if (f < 0) break;  // every element is in a group
+            while (step > 1) {  // the probe at lo + step is known to differ
+                step /= 32;
+                const long long q = lo + (long long)(lane + 1) * step;
+                const unsigned int m = __ballot_sync(0xffffffffu, q >= n || key[q] != k0);
+                lo += (long long)(__ffs((int)m) - 1) * step;
+            }
+            if (lane == 0) s_p1 = lo + 1;
+        }
+        __syncthreads();
+        const long long p1 = s_p1;
+        long long f = p0;
+        for (;;) {  // block-uniform rounds: one group each
+            // the lead's index: an unmarked element, so its mark bit is clear
+            // (masked all the same: members of this round are marked meanwhile)
             const long long lead = (long long)(val[f] & 0x7FFFFFFFu);
             unsigned long long dl[kMaxWords];
             NECI_FOR_WORDS(w, W) dl[w] = (unsigned long long)st.spawn[lead * R + w];
-            __syncwarp();  // every lane has read val[f] before it is marked
             Group g = {{0, 0}, {0u, 0u}, 0u};
-            for (long long q = f + lane; q < p1; q += 32) {
-                const uint32_t v = val[q];
-                if (v & 0x80000000u) continue;
-                const long long *re = st.spawn + (long long)v * R;
-                if (!det_eq(dl, re, W)) continue;
-                val[q] = v | 0x80000000u;
-                group_add(g, re, W, L);
+            long long next = kNone;
+            for (long long base = f + threadIdx.x; base < p1; base += kLongThreads * kLongItems) {
+                uint32_t v[kLongItems];
+#pragma unroll
+                for (int j = 0; j < kLongItems; ++j) {
+                    const long long q = base + (long long)j * kLongThreads;
+                    v[j] = q < p1 ? val[q] : 0x80000000u;  // past the end: treated as marked
+                }
+#pragma unroll
+                for (int j = 0; j < kLongItems; ++j) {
+                    if (v[j] & 0x80000000u) continue;
+                    const long long q = base + (long long)j * kLongThreads;
+                    const long long *re = st.spawn + (long long)v[j] * R;
+                    if (!det_eq(dl, re, W)) {
+                        next = min(next, q);
+                        continue;
+                    }
+                    val[q] = v[j] | 0x80000000u;
+                    group_add(g, re, W, L);
+                }
             }
-            // the group's sums over the warp (two's-complement wrap, as the atomics)
-            Group t;
+            // the group's sums over the block (two's-complement wrap, as the atomics)
+            uint32_t init = 0u;
             NECI_FOR_RUNS(k, L) {
-                t.q[k] = (long long)warp_sum_u((unsigned long long)g.q[k]);
-                const unsigned long long cn = warp_sum_u((unsigned long long)(g.cnt[k] & 0x7FFFFFFFu));
-                const bool init = __any_sync(0xffffffffu, (g.cnt[k] & 0x80000000u) != 0u);
-                t.cnt[k] = (uint32_t)cn | (init ? 0x80000000u : 0u);
+                const unsigned long long qs = warp_sum_u((unsigned long long)g.q[k]);
+                const unsigned long long cs = warp_sum_u((unsigned long long)(g.cnt[k] & 0x7FFFFFFFu));
+                if (__any_sync(0xffffffffu, (g.cnt[k] & 0x80000000u) != 0u)) init |= 1u << k;
+                if (lane == 0) {
+                    s_q[wid][k] = qs;
+                    s_c[wid][k] = cs;
+                }
             }
-            if (L < 2) {
-                t.q[1] = 0;
-                t.cnt[1] = 0u;
-            }
-            t.nrec = (uint32_t)warp_sum_u((unsigned long long)g.nrec);
+            const unsigned long long nr = warp_sum_u((unsigned long long)g.nrec);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) next = min(next, __shfl_xor_sync(0xffffffffu, next, o));
             if (lane == 0) {
+                s_nrec[wid] = nr;
+                s_init[wid] = init;
+                s_next[wid] = next;
+            }
+            __syncthreads();
+            next = kNone;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) next = min(next, s_next[w]);
+            if (threadIdx.x == 0) {
+                Group t = {{0, 0}, {0u, 0u}, 0u};
+                uint32_t ini = 0u;
+                for (int w = 0; w < NW; ++w) {
+                    NECI_FOR_RUNS(k, L) {
+                        t.q[k] = (long long)((unsigned long long)t.q[k] + s_q[w][k]);
+                        t.cnt[k] += (uint32_t)s_c[w][k];
+                    }
+                    t.nrec += (uint32_t)s_nrec[w];
+                    ini |= s_init[w];
+                }
+                NECI_FOR_RUNS(k, L) if (ini & (1u << k)) t.cnt[k] |= 0x80000000u;
                 const long long slot = lookup ? hash_find(st, dl, W, R, st.sk_h[lead], c) : -1;
                 if (slot >= 0) group_found(st, slot, t, L);
                 else group_absent(st, atomicAdd(&c->n_reps, 1ull), lead, t, L);
             }
-            __syncwarp();
+            __syncthreads();  // the shared sums and s_next are read before the next round writes them
+            if (next == kNone) break;
+            f = next;
         }
     }
 }
@@ -314,10 +364,10 @@ int launch_sort_radix(Engine &e, cudaStream_t s) {
 void launch_sort_group(Engine &e, cudaStream_t s, int lookup, int cur) {
     if (e.sys.L == 2) {
         k_sk_group<2><<<sk_grid(e, 8), 256, 0, s>>>(e.sys, e.st, lookup, cur);
-        k_sk_long<2><<<e.num_sms * 2, 256, 0, s>>>(e.sys, e.st, lookup, cur);
+        k_sk_long<2><<<e.num_sms * 4, kLongThreads, 0, s>>>(e.sys, e.st, lookup, cur);
     } else {
         k_sk_group<1><<<sk_grid(e, 8), 256, 0, s>>>(e.sys, e.st, lookup, cur);
-        k_sk_long<1><<<e.num_sms * 2, 256, 0, s>>>(e.sys, e.st, lookup, cur);
+        k_sk_long<1><<<e.num_sms * 4, kLongThreads, 0, s>>>(e.sys, e.st, lookup, cur);
     }
 }
 
