@@ -371,6 +371,16 @@ int32_t neci_gpu_core_nnz(neci_gpu_ctx *ctx, int64_t *nnz);
                             equal determinants reduced as runs: CompressSpawnedList's
                             sort and FindResidualParticle (Annihilation.F90:273,
                             551-634)                                                  */
+#define NECI_OPT_CORE_SEGMENT 2  /* core projection (determ_projection_no_death,
+                                    semi_stoch_procs.F90:290-365): elements per lane of
+                                    a segment of a core row, 1..65536, default 64.  A
+                                    row is summed in segments of G times this many
+                                    elements (G lanes per segment), whose sums are added
+                                    in order, so that long rows are spread over many
+                                    lanes.  The one option that changes the order of
+                                    additions, and so the last bits of the projection;
+                                    it takes effect at the next neci_gpu_set_core_space
+                                    or neci_gpu_select_core.                          */
 int32_t neci_gpu_set_option(neci_gpu_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- autotuning -----------------------------------------------------------

@@ -35,6 +35,7 @@ OPT_FUSE_PROBE = 0
 OPT_ANNIHILATION = 1
 ANN_HASH = 0
 ANN_SORT = 1
+OPT_CORE_SEGMENT = 2
 FLAG_INITIATOR = (13, 14)
 FLAG_DETERMINISTIC = (19, 20)
 SPAWN_FIXED_BITS = 32

@@ -1159,6 +1159,11 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     dfree(e, st.core_val);
     dfree(e, st.core_val32);
     dfree(e, st.core_dets);
+    dfree(e, st.core_seg_row);
+    dfree(e, st.core_seg_first);
+    dfree(e, st.core_seg_y);
+    dfree(e, st.core_multi);
+    st.n_core_seg = st.n_core_multi = 0;
     if (!st.core_of_slot) {
         if (int r = dalloc(e, &st.core_of_slot, (size_t)st.max_walkers)) return r;
     }
@@ -1201,8 +1206,34 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     if (int r = dalloc(e, &st.core_col, (size_t)nnz)) return r;
     if (int r = dalloc(e, &st.core_val, (size_t)nnz)) return r;
     if (int r = dalloc(e, &st.core_val32, (size_t)nnz)) return r;
+    // segments of the rows: core_segment_len(G, per_lane) elements at most,
+    // one for an empty row
+    const int G = core_group_size(nnz, n_core);
+    const long long S = core_segment_len(G, e.core_seg_lane);
+    std::vector<long long> sfirst(n_core + 1, 0);
+    std::vector<int32_t> multi;
+    for (long long i = 0; i < n_core; ++i) {
+        const long long ns = hc[i] > S ? (hc[i] + S - 1) / S : 1;
+        sfirst[i + 1] = sfirst[i] + ns;
+        if (ns > 1) multi.push_back((int32_t)i);
+    }
+    const long long nseg = sfirst[n_core];
+    std::vector<int32_t> srow(nseg);
+    for (long long i = 0; i < n_core; ++i)
+        for (long long k = sfirst[i]; k < sfirst[i + 1]; ++k) srow[k] = (int32_t)i;
+    if (int r = dalloc(e, &st.core_seg_row, (size_t)nseg)) return r;
+    if (int r = dalloc(e, &st.core_seg_first, (size_t)n_core + 1)) return r;
+    if (int r = dalloc(e, &st.core_seg_y, (size_t)(multi.empty() ? 1 : nseg) * L)) return r;
+    if (int r = dalloc(e, &st.core_multi, multi.empty() ? (size_t)1 : multi.size())) return r;
+    CK(cudaMemcpyAsync(st.core_seg_row, srow.data(), (size_t)nseg * 4, cudaMemcpyHostToDevice, e.stream));
+    CK(cudaMemcpyAsync(st.core_seg_first, sfirst.data(), (size_t)(n_core + 1) * 8, cudaMemcpyHostToDevice, e.stream));
+    if (!multi.empty())
+        CK(cudaMemcpyAsync(st.core_multi, multi.data(), multi.size() * 4, cudaMemcpyHostToDevice, e.stream));
     st.n_core = n_core;
-    st.core_group = core_group_size(nnz, n_core);
+    st.core_group = G;
+    st.n_core_seg = nseg;
+    st.core_seg_len = S;
+    st.n_core_multi = (long long)multi.size();
     launch_core_fill(e, dcore, n_core);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e.stream));
@@ -1416,6 +1447,11 @@ int32_t neci_gpu_set_option(neci_gpu_ctx *ctx, int32_t option, int32_t value) {
             if (int r = alloc_sort_buffers(e)) return r;
         e.ann_mode = value;
         drop_graphs(e);
+        return NECI_GPU_OK;
+    }
+    if (option == NECI_OPT_CORE_SEGMENT) {
+        if (value < 1 || value > 65536) return fail(NECI_GPU_ERR_INVALID, "NECI_OPT_CORE_SEGMENT takes 1..65536");
+        e.core_seg_lane = value;  // used by the next core_build
         return NECI_GPU_OK;
     }
     return fail(NECI_GPU_ERR_INVALID, "unknown option");

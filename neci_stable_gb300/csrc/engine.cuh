@@ -207,6 +207,15 @@ struct DevState {
     double *core_x, *core_y;
     long long *core_rowptr;
     int core_group;                // lanes that sum one core row (core_group_size)
+    // segments of the core rows, core_segment_len elements at most: the row
+    // of each segment, each row's first segment (n_core + 1 entries), the
+    // partial sums of the segments of rows with more than one, and those rows
+    long long n_core_seg, n_core_multi;
+    long long core_seg_len;        // elements of a segment, core_segment_len
+    int32_t *core_seg_row;
+    long long *core_seg_first;
+    double *core_seg_y;
+    int32_t *core_multi;
     long long *core_dets;          // W words of each core determinant (2-RDM core pairs)
     // sort form of the annihilation: 32-bit sort keys and record indices
     // (two buffers each, ping-ponged by the radix passes), the 64-bit NECI
@@ -232,6 +241,14 @@ __host__ __device__ inline int core_group_size(long long nnz, long long n_core) 
     while (g < 32 && 4ll * g * n_core < nnz) g <<= 1;
     return g;
 }
+
+// Elements of a core row that one group of G lanes sums as one segment
+// (per_lane each, 64 unless set by NECI_OPT_CORE_SEGMENT).  A longer row is
+// split into segments from its start; their partial sums are added in
+// segment order, so that a row of any length is spread over several groups
+// in a defined order.
+constexpr int kCoreSegmentPerLane = 64;
+__host__ __device__ constexpr long long core_segment_len(int G, int per_lane) { return (long long)per_lane * G; }
 
 // Slots in use, never above the allocation (a step that overflowed the list
 // leaves TotWalkers above it).

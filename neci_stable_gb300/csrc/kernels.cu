@@ -596,17 +596,23 @@ __global__ void k_expand(DevState st) {
 
 // ===========================================================================
 // k_core: y = -tau H_offdiag x over the core rows (determ_projection_no_death,
-// semi_stoch_procs.F90:290-365).  Each row is summed by a group of G lanes (a
-// power of two chosen at set-up from the mean row length, core_group_size):
-// lane l of the group accumulates the row's elements l, l+G, l+2G, ... in
-// order, and the group's G partial sums are added in a fixed tree (offsets
-// G/2, G/4, ..., 1).  FP64: fused multiply-adds acc = fma(-H_ij, x_j, acc),
-// which the oracle restates in the same order, so the projection is
-// bit-exact.  Mixed precision: FP32 values and products with compensated
-// (TwoSum) FP32 accumulation per lane, each lane's hi + lo then summed in
-// FP64 by the same tree.  Four elements of a lane are loaded before their
-// products are accumulated (in element order), so that a lane keeps four
-// independent gathers in flight.
+// semi_stoch_procs.F90:290-365).  The rows are cut into segments of at most
+// core_segment_len(G, per_lane) elements, and each segment is summed by a group of G
+// lanes (a power of two chosen at set-up from the mean row length,
+// core_group_size): lane l of the group accumulates the segment's elements
+// l, l+G, l+2G, ... in order, and the group's G partial sums are added in a
+// fixed tree (offsets G/2, G/4, ..., 1).  A row of one segment gets
+// y = tau * (the tree's sum) at once; the segments of a longer row leave
+// their sums in core_seg_y, and k_core_sum adds them in segment order, so
+// that a row with tens of thousands of elements (the reference's, in a
+// molecular core) is spread over many groups instead of holding one.
+// FP64: fused multiply-adds acc = fma(-H_ij, x_j, acc), which the oracle
+// restates in the same order, so the projection is bit-exact.  Mixed
+// precision: FP32 values and products with compensated (TwoSum) FP32
+// accumulation per lane, each lane's hi + lo then summed in FP64 by the same
+// tree.  Four elements of a lane are loaded before their products are
+// accumulated (in element order), so that a lane keeps four independent
+// gathers in flight.
 // ===========================================================================
 template <int G, bool MIXED>
 __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterParams *pp) {
@@ -616,14 +622,24 @@ __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterP
     const int gl = threadIdx.x & (G - 1);
     const long long grp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const long long ngrp = ((long long)gridDim.x * blockDim.x) / G;
-    const long long nrows = st.n_core;
+    const long long nseg = st.n_core_seg;
+    const long long S = st.core_seg_len;
     // every lane runs the same number of rounds (the tree's shuffles are warp-wide)
-    const long long nround = ((nrows + ngrp - 1) / ngrp) * ngrp;
+    const long long nround = ((nseg + ngrp - 1) / ngrp) * ngrp;
     const int32_t *col = st.core_col;
     const double *xv = st.core_x;
-    for (long long i = grp; i < nround; i += ngrp) {
-        const bool valid = i < nrows;
-        const long long e0 = valid ? st.core_rowptr[i] : 0, e1 = valid ? st.core_rowptr[i + 1] : 0;
+    for (long long sg = grp; sg < nround; sg += ngrp) {
+        const bool valid = sg < nseg;
+        long long row = 0, e0 = 0, e1 = 0;
+        bool single = true;
+        if (valid) {
+            row = st.core_seg_row[sg];
+            const long long f = st.core_seg_first[row], fn = st.core_seg_first[row + 1];
+            const long long r1 = st.core_rowptr[row + 1];
+            e0 = st.core_rowptr[row] + (sg - f) * S;
+            e1 = min(e0 + S, r1);
+            single = fn - f == 1;
+        }
         double acc[2] = {0.0, 0.0};
         float hi[2] = {0.0f, 0.0f}, lo[2] = {0.0f, 0.0f};
         auto add = [&](long long e, int c) {
@@ -653,7 +669,28 @@ __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterP
             double t = MIXED ? (double)hi[k] + (double)lo[k] : acc[k];
 #pragma unroll
             for (int o = G / 2; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o, G);
-            if (gl == 0 && valid) st.core_y[i * L + k] = t * tau;
+            if (gl == 0 && valid) {
+                if (single) st.core_y[row * L + k] = t * tau;
+                else st.core_seg_y[sg * L + k] = t;
+            }
+        }
+    }
+}
+
+// The rows of more than one segment: their segments' sums added in segment
+// order, then multiplied by tau (one thread per row).
+__global__ void __launch_bounds__(256) k_core_sum(DevSys s, DevState st, const IterParams *pp) {
+    if (halted(st)) return;
+    const int L = s.L;
+    const double tau = pp->tau;
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < st.n_core_multi;
+         m += (long long)gridDim.x * blockDim.x) {
+        const long long row = st.core_multi[m];
+        const long long f = st.core_seg_first[row], fn = st.core_seg_first[row + 1];
+        NECI_FOR_RUNS(k, L) {
+            double t = st.core_seg_y[f * L + k];
+            for (long long sg = f + 1; sg < fn; ++sg) t += st.core_seg_y[sg * L + k];
+            st.core_y[row * L + k] = t * tau;
         }
     }
 }
@@ -1279,18 +1316,22 @@ __global__ void __launch_bounds__(256) k_rdm_offdiag(DevSys s, DevState st) {
 // x_i the parent's amplitudes at the start of the step (the core vector), C_j
 // the child's after annihilation.  NECI adds C_i^2 C_j^1 per ordered pair,
 // with averaged signs; over both orders the sums agree, and the host
-// symmetrises.  One warp per core row.
+// symmetrises.  One warp per segment of a core row (the segments of k_core).
 __global__ void __launch_bounds__(256) k_rdm_core(DevSys s, DevState st) {
     if (halted(st)) return;
     const int W = s.W, R = s.R;
     const int lane = threadIdx.x & 31;
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    for (long long i = warp; i < st.n_core; i += nwarps) {
+    const long long S = st.core_seg_len;
+    for (long long sg = warp; sg < st.n_core_seg; sg += nwarps) {
+        const long long i = st.core_seg_row[sg];
+        const long long e0 = st.core_rowptr[i] + (sg - st.core_seg_first[i]) * S;
+        const long long e1 = min(e0 + S, st.core_rowptr[i + 1]);
         unsigned long long pd[kMaxWords];
         NECI_FOR_WORDS(w, W) pd[w] = (unsigned long long)st.core_dets[i * W + w];
         const double x1 = st.core_x[i * 2], x2 = st.core_x[i * 2 + 1];
-        for (long long e = st.core_rowptr[i] + lane; e < st.core_rowptr[i + 1]; e += 32) {
+        for (long long e = e0 + lane; e < e1; e += 32) {
             const long long j = st.core_col[e];
             const long long *rj = st.dets + st.core_slot[j] * R;
             const double c = 0.5 * (x1 * word_to_double(rj[W + 1]) + x2 * word_to_double(rj[W]));
@@ -1481,9 +1522,11 @@ void launch_sweep(Engine &e, cudaStream_t s) {
 void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256, e.occ_expand), 256, 0, s>>>(e.st); }
 template <int G>
 static void launch_core_g(Engine &e, cudaStream_t s) {
-    const int grid = clamp_grid(e.st.n_core * G / 256 + 1, e.num_sms * 8);
+    const int grid = clamp_grid(e.st.n_core_seg * G / 256 + 1, e.num_sms * 8);
     if (e.h_params->precision == NECI_PREC_MIXED) k_core<G, true><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
     else k_core<G, false><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
+    if (e.st.n_core_multi > 0)
+        k_core_sum<<<clamp_grid(e.st.n_core_multi / 256 + 1, e.num_sms), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_core(Engine &e, cudaStream_t s) {
     if (e.st.n_core <= 0) return;
@@ -1518,7 +1561,7 @@ void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
 void launch_rdm(Engine &e, cudaStream_t s) {
     if (!e.sys.rdm) return;
     k_rdm_offdiag<<<grid_spawns(e, 256), 256, (e.sys.nbasis + 1) * sizeof(int32_t), s>>>(e.sys, e.st);
-    if (e.st.n_core > 0) k_rdm_core<<<clamp_grid(e.st.n_core / 8 + 1, e.num_sms * 8), 256, 0, s>>>(e.sys, e.st);
+    if (e.st.n_core > 0) k_rdm_core<<<clamp_grid(e.st.n_core_seg / 8 + 1, e.num_sms * 8), 256, 0, s>>>(e.sys, e.st);
     const size_t shm = (size_t)e.sys.npair * sizeof(double);
     const int use_shared = shm <= 48 * 1024 ? 1 : 0;  // the default dynamic shared-memory limit
     k_rdm_diag<<<grid_slots(e), 256, use_shared ? shm : 0, s>>>(e.sys, e.st, use_shared);

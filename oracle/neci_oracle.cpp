@@ -169,6 +169,11 @@ static int core_group_size(long long nnz, long long n_core) {
     return g;
 }
 
+// Elements of a core row summed as one segment (the engine's
+// core_segment_len): per_lane per partial sum, 64 unless set
+// (NECI_OPT_CORE_SEGMENT).
+static long long core_segment_len(int G, int per_lane) { return (long long)per_lane * G; }
+
 struct Oracle {
     neci_gpu_system sys{};
     int W = 1, L = 1, R = 3;  // det words, sign words, row words
@@ -228,6 +233,7 @@ struct Oracle {
     // core space
     std::vector<i64> core_slots;      // slot of each core det
     std::vector<i64> core_rowptr, core_col;
+    int core_seg_lane = 64;  // elements per partial sum of a core-row segment
     std::vector<double> core_val;     // off-diagonal H_ij
     std::vector<double> core_diag;    // H_ii - Hii
 
@@ -1326,26 +1332,35 @@ struct IterRun {
         st.n_spawned = (i64)spawns.size();
 
         // ---- determ_projection_no_death (semi_stoch_procs.F90:290-365):
-        // y_i = -tau sum_j H_ij x_j.  The sum of a row is taken in G partial
-        // sums (G from the mean row length, as the engine's core kernel does):
-        // partial l adds the row's elements l, l+G, l+2G, ... in order with
-        // fused multiply-adds, then the partials are added pairwise, offsets
-        // G/2, G/4, ..., 1, into partial 0.
+        // y_i = -tau sum_j H_ij x_j.  A row is cut into segments of
+        // core_segment_len(G) elements from its start (G from the mean row
+        // length, as the engine's core kernel does).  A segment is summed in G
+        // partial sums: partial l adds the segment's elements l, l+G, l+2G,
+        // ... in order with fused multiply-adds, then the partials are added
+        // pairwise, offsets G/2, G/4, ..., 1, into partial 0.  The segments'
+        // sums are added in segment order and the total multiplied by tau.
         std::vector<double> y(partial.size(), 0.0);
         if (semistoch) {
             const size_t nc = o.core_slots.size();
             const int G = core_group_size((i64)o.core_val.size(), (i64)nc);
+            const i64 S = core_segment_len(G, o.core_seg_lane);
             double part[32];
             for (size_t i = 0; i < nc; ++i) {
+                const i64 r0 = o.core_rowptr[i], r1 = o.core_rowptr[i + 1];
                 for (int k = 0; k < L; ++k) {
-                    for (int l = 0; l < G; ++l) {
-                        part[l] = 0.0;
-                        for (i64 e = o.core_rowptr[i] + l; e < o.core_rowptr[i + 1]; e += G)
-                            part[l] = std::fma(-o.core_val[e], partial[o.core_col[e] * L + k], part[l]);
+                    double tot = 0.0;
+                    for (i64 s0 = r0; s0 == r0 || s0 < r1; s0 += S) {
+                        const i64 s1 = std::min(s0 + S, r1);
+                        for (int l = 0; l < G; ++l) {
+                            part[l] = 0.0;
+                            for (i64 e = s0 + l; e < s1; e += G)
+                                part[l] = std::fma(-o.core_val[e], partial[o.core_col[e] * L + k], part[l]);
+                        }
+                        for (int off = G / 2; off > 0; off >>= 1)
+                            for (int l = 0; l < off; ++l) part[l] = part[l] + part[l + off];
+                        tot = s0 == r0 ? part[0] : tot + part[0];
                     }
-                    for (int off = G / 2; off > 0; off >>= 1)
-                        for (int l = 0; l < off; ++l) part[l] = part[l] + part[l + off];
-                    y[i * L + k] = part[0] * p.tau;
+                    y[i * L + k] = tot * p.tau;
                 }
             }
         }
@@ -2018,6 +2033,11 @@ int32_t orc_init_alias(const double *w, int64_t n, double *bias, int32_t *alias)
     Oracle o;
     std::vector<double> arr(w, w + n);
     o.init_alias(arr, bias, alias);
+    return NECI_GPU_OK;
+}
+int32_t orc_set_core_segment(void *h, int32_t per_lane) {
+    if (per_lane < 1 || per_lane > 65536) return NECI_GPU_ERR_INVALID;
+    ((Oracle *)h)->core_seg_lane = per_lane;
     return NECI_GPU_OK;
 }
 int32_t orc_set_core_space(void *h, const int64_t *core, int64_t n_core) {

@@ -43,6 +43,7 @@ def _load():
         "orc_init_pchb": [_P],
         "orc_set_excit_biases": [_P, C.c_double, C.c_double],
         "orc_set_tau_search": [_P, C.c_int32],
+        "orc_set_core_segment": [_P, C.c_int32],
         "orc_set_rdm_sampling": [_P, C.c_int32],
         "orc_get_rdm": [_P, _P, C.c_int64, C.c_int32],
         "orc_get_tau_stats": [_P, C.POINTER(capi.TauStats), C.c_int32],
@@ -224,6 +225,11 @@ class Oracle:
         _ok(lib().orc_calc_pgen(self.h, _ptr(np.ascontiguousarray(det, dtype=np.int64)),
                                 _ptr(np.ascontiguousarray(child, dtype=np.int64)), C.byref(out)))
         return out.value
+
+    def set_core_segment(self, per_lane: int):
+        """Elements per partial sum of a core-row segment (the engine's
+        NECI_OPT_CORE_SEGMENT); applies to the next set_core_space."""
+        _ok(lib().orc_set_core_segment(self.h, per_lane))
 
     def set_core_space(self, core):
         c = np.ascontiguousarray(core, dtype=np.int64)

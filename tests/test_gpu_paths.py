@@ -266,6 +266,9 @@ def test_fused_lookup_option_is_for_lattices_only():
         eng.set_option(capi.OPT_ANNIHILATION, 7)
     with pytest.raises(capi.NeciGpuError):
         eng.set_option(99, 0)
+    for bad in (0, 65537):
+        with pytest.raises(capi.NeciGpuError):
+            eng.set_option(capi.OPT_CORE_SEGMENT, bad)
 
 
 # ------------------------------------------------- a parent of > 65536 attempts
@@ -386,13 +389,17 @@ def test_autotune_steps_are_ordinary_steps(name, pop, tau):
 
 
 # --------------------------------------------------- 2-RDM with a core space
-@pytest.mark.parametrize("name", ["hub10x2", "mol12x2"])
-def test_rdm_with_core_space_matches_oracle(name):
+@pytest.mark.parametrize("name,seg", [("hub10x2", None), ("mol12x2", None), ("mol12x2", 1)])
+def test_rdm_with_core_space_matches_oracle(name, seg):
     """2-RDM sampling of a replica pair with a semistochastic core: the device
     2-RDM (spawn pairs, core pairs and the diagonal) equals the oracle's after
     every step, up to the order of the FP64 atomic sums; the walker lists stay
-    bit-exact."""
+    bit-exact.  seg = 1: core rows summed (and their RDM pairs taken) in
+    segments of one element per lane."""
     spec, eng, orc = pair(name)
+    if seg is not None:
+        eng.set_option(capi.OPT_CORE_SEGMENT, seg)
+        orc.set_core_segment(seg)
     W, L = spec.W, spec.lenof_sign
     eng.start_from_reference(initial_part=60.0)
     for it in range(1, 11):

@@ -117,11 +117,18 @@ def test_ring10_configuration_converges():
         assert 0.05 < r["proje"] - e0 < 0.35, (r, e0)
 
 
+@pytest.mark.parametrize("seg", [None, 1])
 @pytest.mark.parametrize("precision,rtol", [(capi.PREC_FP64, 1e-12), (capi.PREC_MIXED, 2e-6)])
-def test_semistochastic_core_projection(precision, rtol):
+def test_semistochastic_core_projection(precision, rtol, seg):
+    """Steps with a core space against the oracle.  seg = 1 sets one element
+    per lane per segment of a core row (NECI_OPT_CORE_SEGMENT), so that almost
+    every row is summed in several segments added in order by k_core_sum."""
     spec = hubbard10()
     eng = Engine(spec, max_walkers=200_000, max_spawned=400_000)
     orc = Oracle(spec, 200_000, 400_000, hii=eng.hii)
+    if seg is not None:
+        eng.set_option(capi.OPT_CORE_SEGMENT, seg)
+        orc.set_core_segment(seg)
     eng.start_from_reference(initial_part=200.0)
     p = capi.default_params(tau=0.02, seed=77)
     for it in range(1, 16):  # grow a population first
