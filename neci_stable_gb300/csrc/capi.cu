@@ -288,6 +288,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.cand_h, (size_t)st.max_spawned);
     A(st.spawn_hash, (size_t)st.spawn_hash_n);
     A(st.reps, (size_t)st.max_spawned);
+    A(st.place, (size_t)st.max_spawned);
     A(st.rep_bucket, (size_t)st.max_spawned);
     A(st.rep_q, (size_t)st.max_spawned * s.L);
     A(st.rep_cnt, (size_t)st.max_spawned * (s.L + 1));
@@ -1159,7 +1160,7 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     dfree(e, st.core_val);
     dfree(e, st.core_val32);
     dfree(e, st.core_dets);
-    dfree(e, st.core_seg_row);
+    dfree(e, st.core_seg);
     dfree(e, st.core_seg_first);
     dfree(e, st.core_seg_y);
     dfree(e, st.core_multi);
@@ -1218,14 +1219,19 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
         if (ns > 1) multi.push_back((int32_t)i);
     }
     const long long nseg = sfirst[n_core];
-    std::vector<int32_t> srow(nseg);
+    std::vector<CoreSeg> segs(nseg);
     for (long long i = 0; i < n_core; ++i)
-        for (long long k = sfirst[i]; k < sfirst[i + 1]; ++k) srow[k] = (int32_t)i;
-    if (int r = dalloc(e, &st.core_seg_row, (size_t)nseg)) return r;
+        for (long long k = sfirst[i]; k < sfirst[i + 1]; ++k) {
+            const long long e0 = rp[i] + (k - sfirst[i]) * S;
+            const long long e1 = std::min(e0 + S, rp[i + 1]);
+            const bool many = sfirst[i + 1] - sfirst[i] > 1;
+            segs[k] = CoreSeg{e0, (int32_t)(e1 - e0), (int32_t)((uint32_t)i | (many ? 0x80000000u : 0u))};
+        }
+    if (int r = dalloc(e, &st.core_seg, (size_t)nseg)) return r;
     if (int r = dalloc(e, &st.core_seg_first, (size_t)n_core + 1)) return r;
     if (int r = dalloc(e, &st.core_seg_y, (size_t)(multi.empty() ? 1 : nseg) * L)) return r;
     if (int r = dalloc(e, &st.core_multi, multi.empty() ? (size_t)1 : multi.size())) return r;
-    CK(cudaMemcpyAsync(st.core_seg_row, srow.data(), (size_t)nseg * 4, cudaMemcpyHostToDevice, e.stream));
+    CK(cudaMemcpyAsync(st.core_seg, segs.data(), (size_t)nseg * sizeof(CoreSeg), cudaMemcpyHostToDevice, e.stream));
     CK(cudaMemcpyAsync(st.core_seg_first, sfirst.data(), (size_t)(n_core + 1) * 8, cudaMemcpyHostToDevice, e.stream));
     if (!multi.empty())
         CK(cudaMemcpyAsync(st.core_multi, multi.data(), multi.size() * 4, cudaMemcpyHostToDevice, e.stream));

@@ -58,6 +58,7 @@ struct Control {
     unsigned long long n_big;           // parents expanded by k_expand
     unsigned long long n_huge;          // parents expanded by the whole grid
     unsigned long long n_long;          // sort annihilation: runs of equal keys left to k_sk_long
+    unsigned long long n_place;         // new determinants k_ann_decide leaves to k_ann_place
     unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
@@ -75,6 +76,14 @@ struct Control {
     unsigned long long tau_gamma[4];    // per TauClass
     unsigned long long tau_cnt[4];
     unsigned long long tau_death;       // max_death_cpt
+};
+
+// One segment of a core row: its first element, its length, its row, and
+// whether the row has other segments (one 16-byte load).
+struct __align__(16) CoreSeg {
+    long long e0;
+    int32_t len;
+    int32_t row;  // bit 31: the row has more than one segment
 };
 
 // Excitation classes of the conventional tau search
@@ -188,6 +197,7 @@ struct DevState {
     unsigned long long spawn_hash_n;
     int comp_shift;                // the table in use holds >= 2^comp_shift buckets per candidate
     uint32_t *reps;                // candidate position of each unique new determinant
+    uint32_t *place;               // candidate positions of the new determinants to place
     uint32_t *rep_bucket;
     long long *rep_q;              // per candidate*L fixed-point sums
     uint32_t *rep_cnt;             // per candidate*L counts | initiator bit 31
@@ -207,12 +217,13 @@ struct DevState {
     double *core_x, *core_y;
     long long *core_rowptr;
     int core_group;                // lanes that sum one core row (core_group_size)
-    // segments of the core rows, core_segment_len elements at most: the row
-    // of each segment, each row's first segment (n_core + 1 entries), the
-    // partial sums of the segments of rows with more than one, and those rows
+    // segments of the core rows, core_segment_len elements at most: each
+    // segment's range and row, each row's first segment (n_core + 1 entries),
+    // the partial sums of the segments of rows with more than one, and those
+    // rows
     long long n_core_seg, n_core_multi;
     long long core_seg_len;        // elements of a segment, core_segment_len
-    int32_t *core_seg_row;
+    struct CoreSeg *core_seg;
     long long *core_seg_first;
     double *core_seg_y;
     int32_t *core_multi;

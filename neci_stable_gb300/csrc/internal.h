@@ -39,7 +39,7 @@ struct Engine {
     int num_sms = 152;
     // resident blocks per SM of the grid-stride spawn-list kernels (their
     // grids fill the GPU once; the latency-bound hash passes want every warp)
-    int occ_probe = 4, occ_compress = 4, occ_insert = 8, occ_expand = 4;
+    int occ_probe = 4, occ_compress = 4, occ_insert = 4, occ_place = 8, occ_expand = 4;
     // pass 1 of the annihilation runs inside the spawn kernel (chosen from the
     // last step's spawn rate; see update_fuse_probe)
     bool fuse_probe = false;

@@ -22,14 +22,17 @@
 //   k_ann_compress pass 2 (CompressSpawnedList, Annihilation.F90:249):
 //                  candidates are merged per determinant in a second
 //                  open-addressing table keyed on the spawn records
-//   k_ann_insert   pass 3 (AnnihilateSpawnedParts not-found branch,
-//                  :1191-1290): initiator abort, stochRoundSpawn,
-//                  diagonal elements, AddNewHashDet
+//   k_ann_decide   pass 3 (AnnihilateSpawnedParts not-found branch,
+//                  :1191-1290): initiator abort, stochRoundSpawn; the
+//                  survivors are listed for
+//   k_ann_place    AddNewHashDet: slots, rows, hash buckets, diagonal
+//                  elements, one new determinant per thread
 //   k_merge_stats  deterministic_annihilation + AnnihilateSpawnedParts
 //                  found branch + CalcHashTableStats (load_balancer.fpp:646)
 //                  in one sweep over the slots
 //   k_final        collect estimators into the step's stats record
 #include <cstdio>
+#include <type_traits>
 
 #include "engine.cuh"
 #include "excitgen.cuh"
@@ -51,6 +54,7 @@ __global__ void k_begin(DevState st) {
         c->n_big = 0;
         c->n_huge = 0;
         c->n_long = 0;
+        c->n_place = 0;
         for (int k = 0; k < 2; ++k) {
             c->abs_q[k] = 0; c->abs_s[k] = 0;
             c->nborn[k] = c->ndied[k] = c->nannihil[k] = c->naborted[k] = c->nremoved[k] = 0.0;
@@ -610,61 +614,71 @@ __global__ void k_expand(DevState st) {
 // restates in the same order, so the projection is bit-exact.  Mixed
 // precision: FP32 values and products with compensated (TwoSum) FP32
 // accumulation per lane, each lane's hi + lo then summed in FP64 by the same
-// tree.  Four elements of a lane are loaded before their products are
-// accumulated (in element order), so that a lane keeps four independent
-// gathers in flight.
+// tree.  kCoreDepth elements of a lane are loaded before their products are
+// accumulated (in element order), so that a lane keeps that many independent
+// loads and gathers in flight.
 // ===========================================================================
+// Elements a lane loads before it accumulates them (in element order): its
+// column indices and values first, then the gathers of x.
+constexpr int kCoreDepth = 8;
+
 template <int G, bool MIXED>
 __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
+    using VT = typename std::conditional<MIXED, float, double>::type;
     const int L = s.L;
     const double tau = pp->tau;
     const int gl = threadIdx.x & (G - 1);
     const long long grp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) / G;
     const long long ngrp = ((long long)gridDim.x * blockDim.x) / G;
     const long long nseg = st.n_core_seg;
-    const long long S = st.core_seg_len;
     // every lane runs the same number of rounds (the tree's shuffles are warp-wide)
     const long long nround = ((nseg + ngrp - 1) / ngrp) * ngrp;
     const int32_t *col = st.core_col;
+    const VT *val = MIXED ? (const VT *)st.core_val32 : (const VT *)st.core_val;
     const double *xv = st.core_x;
     for (long long sg = grp; sg < nround; sg += ngrp) {
         const bool valid = sg < nseg;
-        long long row = 0, e0 = 0, e1 = 0;
-        bool single = true;
-        if (valid) {
-            row = st.core_seg_row[sg];
-            const long long f = st.core_seg_first[row], fn = st.core_seg_first[row + 1];
-            const long long r1 = st.core_rowptr[row + 1];
-            e0 = st.core_rowptr[row] + (sg - f) * S;
-            e1 = min(e0 + S, r1);
-            single = fn - f == 1;
-        }
+        CoreSeg seg = {0, 0, 0};
+        if (valid) seg = st.core_seg[sg];
+        const long long e1 = seg.e0 + seg.len;
         double acc[2] = {0.0, 0.0};
         float hi[2] = {0.0f, 0.0f}, lo[2] = {0.0f, 0.0f};
-        auto add = [&](long long e, int c) {
-            NECI_FOR_RUNS(k, L) {
-                const double x = xv[(long long)c * L + k];
-                if (!MIXED) {
-                    acc[k] = fma(-st.core_val[e], x, acc[k]);
-                } else {
-                    const float term = -__fmul_rn(st.core_val32[e], (float)x);
-                    const float t = __fadd_rn(hi[k], term);
-                    lo[k] = fabsf(hi[k]) >= fabsf(term) ? __fadd_rn(lo[k], __fadd_rn(__fsub_rn(hi[k], t), term))
-                                                        : __fadd_rn(lo[k], __fadd_rn(__fsub_rn(term, t), hi[k]));
-                    hi[k] = t;
-                }
+        auto add = [&](int k, VT v, double x) {
+            if (!MIXED) {
+                acc[k] = fma(-(double)v, x, acc[k]);
+            } else {
+                const float term = -__fmul_rn((float)v, (float)x);
+                const float t = __fadd_rn(hi[k], term);
+                lo[k] = fabsf(hi[k]) >= fabsf(term) ? __fadd_rn(lo[k], __fadd_rn(__fsub_rn(hi[k], t), term))
+                                                    : __fadd_rn(lo[k], __fadd_rn(__fsub_rn(term, t), hi[k]));
+                hi[k] = t;
             }
         };
-        long long e = e0 + gl;
-        for (; e + 3 * G < e1; e += 4 * G) {
-            const int c0 = col[e], c1 = col[e + G], c2 = col[e + 2 * G], c3 = col[e + 3 * G];
-            add(e, c0);
-            add(e + G, c1);
-            add(e + 2 * G, c2);
-            add(e + 3 * G, c3);
+        long long e = seg.e0 + gl;
+        for (; e + (kCoreDepth - 1) * G < e1; e += kCoreDepth * G) {
+            int cc[kCoreDepth];
+            VT vv[kCoreDepth];
+#pragma unroll
+            for (int j = 0; j < kCoreDepth; ++j) {
+                cc[j] = col[e + j * G];
+                vv[j] = val[e + j * G];
+            }
+            NECI_FOR_RUNS(k, L) {
+                double xx[kCoreDepth];
+#pragma unroll
+                for (int j = 0; j < kCoreDepth; ++j) xx[j] = xv[(long long)cc[j] * L + k];
+#pragma unroll
+                for (int j = 0; j < kCoreDepth; ++j) add(k, vv[j], xx[j]);
+            }
         }
-        for (; e < e1; e += G) add(e, col[e]);
+        for (; e < e1; e += G) {
+            const int cj = col[e];
+            const VT vj = val[e];
+            NECI_FOR_RUNS(k, L) add(k, vj, xv[(long long)cj * L + k]);
+        }
+        const long long row = seg.row & 0x7FFFFFFF;
+        const bool single = seg.row >= 0;
         NECI_FOR_RUNS(k, L) {
             double t = MIXED ? (double)hi[k] + (double)lo[k] : acc[k];
 #pragma unroll
@@ -857,63 +871,57 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
 }
 
 // ===========================================================================
-// Annihilation pass 3: unique new determinants -> CurrentDets.
+// Annihilation pass 3: unique new determinants -> CurrentDets, in two
+// kernels.  k_ann_decide takes every unique determinant not in the list
+// (AnnihilateSpawnedParts' not-found branch with the compressed flags of
+// CompressSpawnedList/FindResidualParticle): its summed amplitude, the
+// initiator abort, stochRoundSpawn, and appends the survivors to a list.
+// k_ann_place gives each survivor a slot (AddNewHashDet), writes its row and
+// hash bucket and computes H_jj - Hii and <D0|H|D_j>, one determinant per
+// thread: the O(nel^2) diagonal sum runs on GB300's 1/64-rate FP64 pipe, and
+// spread over the lanes of the decisions it would hold every lane of a warp
+// that had one survivor.
 // ===========================================================================
 // LR: lenof_sign of the instance (1, or 2 for a replica pair).
 template <int LR>
-__global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, const IterParams *pp) {
+__global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
-    const long long n = (long long)c->n_reps;
+    // the appends count past the allocation when it overflows (SPAWN_FULL is
+    // reported at the end of the step): only the entries written are read
+    const long long n = (long long)min(c->n_reps, (unsigned long long)st.max_spawned);
     const int W = s.W, R = s.R;
     constexpr int L = LR;
     double a_ab[2] = {0, 0}, a_rm[2] = {0, 0}, a_born[2] = {0, 0};
-    unsigned long long a_s[2] = {0, 0};
+    unsigned long long a_s[2] = {0, 0}, a_nz = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const long long nround = ((n + stride - 1) / stride) * stride;
-    long long a_tomb = 0;  // tombstones taken over by the insertions (a negative count)
-    unsigned long long a_new = 0, a_nz = 0;
-    // the round's new determinants (blockDim.x = 128: four warps)
-    __shared__ int nq_w[2][4];
-    __shared__ long long q_slot[128];
-    __shared__ unsigned long long q_det[kMaxWords][128];
-    int round = 0;
     for (long long ri = blockIdx.x * (long long)blockDim.x + threadIdx.x; ri < nround; ri += stride) {
-        bool inserted = false, want = false;
-        long long new_slot = -1;
-        unsigned long long wd[kMaxWords];
-        double ws[2] = {0.0, 0.0};
-        long long wflags = 0, wci = 0;
+        bool want = false;
+        long long ci = 0;
+        double ss[2] = {0.0, 0.0};
+        long long flags = 0;
         if (ri < n) {
-            const long long ci = st.reps[ri];
+            ci = st.reps[ri];
             const uint32_t rb = st.rep_bucket[ri];
             if (rb != kNoBucket) st.spawn_hash[rb] = kEmpty;  // leave the table clean
-            const long long i = st.cand[ci];
-            const long long *rec = st.spawn + i * R;
-            unsigned long long d[kMaxWords];
-            NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
+            const long long *rec = st.spawn + (long long)st.cand[ci] * R;
             long long q[2] = {0, 0};
             uint32_t cnt[2] = {0, 0};
             NECI_FOR_RUNS(k, L) {
                 q[k] = st.rep_q[ci * L + k];
                 cnt[k] = st.rep_cnt[ci * (L + 1) + k];
-                st.rep_q[ci * L + k] = 0;
-                st.rep_cnt[ci * (L + 1) + k] = 0;
             }
             const uint32_t nrec = st.rep_cnt[ci * (L + 1) + L];
-            st.rep_cnt[ci * (L + 1) + L] = 0;
             // compressed flags (CompressSpawnedList / FindResidualParticle)
-            long long flags;
             if (nrec == 1) {
                 flags = rec[W + L];
-            } else {
-                flags = 0;
-                if (p.t_trunc_initiator)
-                    NECI_FOR_RUNS(k, L) {
-                        const bool coh = p.t_init_coherent_rule && (cnt[k] & 0x7FFFFFFFu) >= 2u;
-                        if (coh || (cnt[k] & 0x80000000u)) flags |= 1ll << init_flag_bit(k);
-                    }
+            } else if (p.t_trunc_initiator) {
+                NECI_FOR_RUNS(k, L) {
+                    const bool coh = p.t_init_coherent_rule && (cnt[k] & 0x7FFFFFFFu) >= 2u;
+                    if (coh || (cnt[k] & 0x80000000u)) flags |= 1ll << init_flag_bit(k);
+                }
             }
             bool zero = true;
             NECI_FOR_RUNS(k, L) {
@@ -922,13 +930,16 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
             }
             a_nz += zero ? 0ull : 1ull;
             if (!zero) {
-                double ss[2] = {from_fixed(q[0]), from_fixed(q[1])};
+                ss[0] = from_fixed(q[0]);
+                ss[1] = from_fixed(q[1]);
                 if (p.t_trunc_initiator)
                     NECI_FOR_RUNS(k, L)
                         if (!test_bit(flags, init_flag_bit(k))) { a_ab[k] += fabs(ss[k]); ss[k] = 0.0; }
                 bool unocc = true;
                 NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) unocc = false;
                 if (!unocc) {
+                    unsigned long long d[kMaxWords];
+                    NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
                     const unsigned long long dkey = det_key(d, W, p.seed);
                     NECI_FOR_RUNS(k, L) {
                         // stochRoundSpawn (Annihilation.F90:1354-1418)
@@ -941,102 +952,103 @@ __global__ void __launch_bounds__(128, 8) k_ann_insert(DevSys s, DevState st, co
                             else { a_born[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
                         }
                     }
-                    unocc = true;
-                    NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) unocc = false;
-                }
-                if (!unocc) {
-                    // AddNewHashDet (load_balancer.fpp:514-629): a slot below
-                    want = true;
-                    NECI_FOR_WORDS(w, W) wd[w] = d[w];
-                    ws[0] = ss[0];
-                    ws[1] = ss[1];
-                    wflags = flags;
-                    wci = ci;
+                    NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) want = true;
                 }
             }
+            // the sums are consumed: cleared for the next step, or, for a
+            // survivor, replaced by its signs (as double bits) and its flag
+            // word (low half in the record count's place, high half in the
+            // first run's count) for k_ann_place, which clears them
+            NECI_FOR_RUNS(k, L) {
+                st.rep_q[ci * L + k] = want ? double_to_word(ss[k]) : 0ll;
+                st.rep_cnt[ci * (L + 1) + k] = 0u;
+            }
+            if (want) st.rep_cnt[ci * (L + 1)] = (uint32_t)((unsigned long long)flags >> 32);
+            st.rep_cnt[ci * (L + 1) + L] = want ? (uint32_t)flags : 0u;
         }
-        // Slots for the new determinants of the warp: the next holes of the
-        // free list (one atomic on its cursor), then fresh slots at the end
-        // of the list (one atomic on TotWalkers) when the holes run out.
-        {
-            const int lane = threadIdx.x & 31;
-            const unsigned int ballot = __ballot_sync(0xffffffffu, want);
-            const unsigned int nwant = __popc(ballot);
-            const unsigned int rank = __popc(ballot & ((1u << lane) - 1u));
-            unsigned long long t0 = 0, f0 = 0;
-            const unsigned long long nfree = c->n_free;
-            if (nwant) {
-                const int leader = __ffs(ballot) - 1;
-                if (lane == leader) {
-                    t0 = atomicAdd(&c->free_taken, (unsigned long long)nwant);
-                    const unsigned long long from_free = t0 >= nfree ? 0ull : min(nfree - t0, (unsigned long long)nwant);
-                    if (nwant > from_free) f0 = atomicAdd(&c->tot_walkers, (unsigned long long)(nwant - from_free));
-                }
-                t0 = __shfl_sync(0xffffffffu, t0, leader);
-                f0 = __shfl_sync(0xffffffffu, f0, leader);
-            }
-            if (want) {
-                const unsigned long long t = t0 + rank;
-                const unsigned long long first_fresh = t0 >= nfree ? t0 : nfree;  // the first t that gets a fresh slot
-                const long long slot = t < nfree ? (long long)st.free_list[t] : (long long)(f0 + (t - first_fresh));
-                if (slot + 1 >= st.max_walkers) {
-                    set_err(c, NECI_GPU_ERR_LIST_FULL);
-                } else {
-                    long long *o = st.dets + slot * R;
-                    NECI_FOR_WORDS(w, W) o[w] = (long long)wd[w];
-                    NECI_FOR_RUNS(k, L) o[W + k] = double_to_word(ws[k]);
-                    o[W + L] = wflags & ~1ll;
-                    if (st.n_core > 0) st.core_of_slot[slot] = -1;
-                    a_tomb -= hash_insert(st, slot, st.cand_h[wci], c);
-                    inserted = true;
-                    new_slot = slot;
-                }
-            }
+        const unsigned long long pos = warp_append1(&c->n_place, want);
+        if (want) {
+            if (pos < (unsigned long long)st.max_spawned) st.place[pos] = (uint32_t)ci;
+            else set_err(c, NECI_GPU_ERR_SPAWN_FULL);
         }
-        a_new += inserted ? 1ull : 0ull;
-        // H_jj - Hii and <D0|H|D_j> of the round's new determinants, computed
-        // over a compacted list by consecutive threads: in place, the lanes
-        // without a new determinant would hold GB300's 1/64-rate FP64 pipe
-        // through the O(nel^2) diagonal sum as well.  List positions come
-        // from per-warp counts (by round parity), so no shared counter is
-        // read and written in the same round; the next round writes the list
-        // only after its first barrier, when this round's reads are done.
-        {
-            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-            const unsigned int mb = __ballot_sync(0xffffffffu, inserted);
-            if (lane == 0) nq_w[round & 1][wid] = __popc(mb);
-            __syncthreads();
-            int before = 0, total = 0;
-#pragma unroll
-            for (int w2 = 0; w2 < 4; ++w2) {
-                const int x = nq_w[round & 1][w2];
-                before += w2 < wid ? x : 0;
-                total += x;
-            }
-            if (inserted) {
-                const int i = before + __popc(mb & ((1u << lane) - 1u));
-                q_slot[i] = new_slot;
-                NECI_FOR_WORDS(w, W) q_det[w][i] = wd[w];
-            }
-            __syncthreads();
-            if ((int)threadIdx.x < total) {
-                unsigned long long d[kMaxWords];
-                NECI_FOR_WORDS(w, W) d[w] = q_det[w][threadIdx.x];
-                const long long sl = q_slot[threadIdx.x];
-                st.diagH[sl] = diag_helement(s, d) - s.hii;
-                const int ic = excit_level(s.ilut_ref, d, W);
-                st.offdiagH[sl] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
-            }
-        }
-        ++round;
     }
     double v[6] = {a_ab[0], a_ab[1], a_rm[0], a_rm[1], a_born[0], a_born[1]};
     double *const dst[6] = {&c->naborted[0], &c->naborted[1], &c->nremoved[0], &c->nremoved[1],
                             &c->nborn[0], &c->nborn[1]};
     block_add<6>(v, dst, L);
-    unsigned long long u[5] = {a_s[0], a_s[1], (unsigned long long)a_tomb, a_new, a_nz};  // two's complement for -count
-    unsigned long long *const du[5] = {&c->abs_s[0], &c->abs_s[1], &c->n_tomb, &c->n_new, &c->n_reps_nz};
-    block_add_u<5>(u, du);
+    unsigned long long u[3] = {a_s[0], a_s[1], a_nz};
+    unsigned long long *const du[3] = {&c->abs_s[0], &c->abs_s[1], &c->n_reps_nz};
+    block_add_u<3>(u, du);
+}
+
+template <int LR>
+__global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st) {
+    if (halted(st)) return;
+    Control *c = st.ctl;
+    const long long n = (long long)min(c->n_place, (unsigned long long)st.max_spawned);
+    const int W = s.W, R = s.R;
+    constexpr int L = LR;
+    const int lane = threadIdx.x & 31;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const long long nround = ((n + stride - 1) / stride) * stride;
+    long long a_tomb = 0;  // tombstones taken over by the insertions (a negative count)
+    unsigned long long a_new = 0;
+    for (long long pi = blockIdx.x * (long long)blockDim.x + threadIdx.x; pi < nround; pi += stride) {
+        const bool want = pi < n;
+        long long ci = 0;
+        if (want) ci = st.place[pi];
+        // Slots for the warp's determinants: the next holes of the free list
+        // (one atomic on its cursor), then fresh slots at the end of the list
+        // (one atomic on TotWalkers) when the holes run out.
+        const unsigned int ballot = __ballot_sync(0xffffffffu, want);
+        const unsigned int nwant = __popc(ballot);
+        const unsigned int rank = __popc(ballot & ((1u << lane) - 1u));
+        unsigned long long t0 = 0, f0 = 0;
+        const unsigned long long nfree = c->n_free;
+        if (nwant) {
+            const int leader = __ffs(ballot) - 1;
+            if (lane == leader) {
+                t0 = atomicAdd(&c->free_taken, (unsigned long long)nwant);
+                const unsigned long long from_free = t0 >= nfree ? 0ull : min(nfree - t0, (unsigned long long)nwant);
+                if (nwant > from_free) f0 = atomicAdd(&c->tot_walkers, (unsigned long long)(nwant - from_free));
+            }
+            t0 = __shfl_sync(0xffffffffu, t0, leader);
+            f0 = __shfl_sync(0xffffffffu, f0, leader);
+        }
+        if (!want) continue;
+        const unsigned long long t = t0 + rank;
+        const unsigned long long first_fresh = t0 >= nfree ? t0 : nfree;  // the first t that gets a fresh slot
+        const long long slot = t < nfree ? (long long)st.free_list[t] : (long long)(f0 + (t - first_fresh));
+        long long ws[2] = {0, 0};
+        NECI_FOR_RUNS(k, L) {
+            ws[k] = st.rep_q[ci * L + k];
+            st.rep_q[ci * L + k] = 0;
+        }
+        const long long flags = (long long)(((unsigned long long)st.rep_cnt[ci * (L + 1)] << 32) |
+                                            st.rep_cnt[ci * (L + 1) + L]);
+        st.rep_cnt[ci * (L + 1)] = 0u;
+        st.rep_cnt[ci * (L + 1) + L] = 0u;
+        if (slot + 1 >= st.max_walkers) {
+            set_err(c, NECI_GPU_ERR_LIST_FULL);
+            continue;
+        }
+        const long long *rec = st.spawn + (long long)st.cand[ci] * R;
+        unsigned long long d[kMaxWords];
+        NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
+        long long *o = st.dets + slot * R;
+        NECI_FOR_WORDS(w, W) o[w] = (long long)d[w];
+        NECI_FOR_RUNS(k, L) o[W + k] = ws[k];
+        o[W + L] = flags & ~1ll;
+        if (st.n_core > 0) st.core_of_slot[slot] = -1;
+        a_tomb -= hash_insert(st, slot, st.cand_h[ci], c);
+        ++a_new;
+        st.diagH[slot] = diag_helement(s, d) - s.hii;
+        const int ic = excit_level(s.ilut_ref, d, W);
+        st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
+    }
+    unsigned long long u[2] = {(unsigned long long)a_tomb, a_new};  // two's complement for -count
+    unsigned long long *const du[2] = {&c->n_tomb, &c->n_new};
+    block_add_u<2>(u, du);
 }
 
 // ===========================================================================
@@ -1323,11 +1335,10 @@ __global__ void __launch_bounds__(256) k_rdm_core(DevSys s, DevState st) {
     const int lane = threadIdx.x & 31;
     const long long warp = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
     const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-    const long long S = st.core_seg_len;
     for (long long sg = warp; sg < st.n_core_seg; sg += nwarps) {
-        const long long i = st.core_seg_row[sg];
-        const long long e0 = st.core_rowptr[i] + (sg - st.core_seg_first[i]) * S;
-        const long long e1 = min(e0 + S, st.core_rowptr[i + 1]);
+        const CoreSeg seg = st.core_seg[sg];
+        const long long i = seg.row & 0x7FFFFFFF;
+        const long long e0 = seg.e0, e1 = seg.e0 + seg.len;
         unsigned long long pd[kMaxWords];
         NECI_FOR_WORDS(w, W) pd[w] = (unsigned long long)st.core_dets[i * W + w];
         const double x1 = st.core_x[i * 2], x2 = st.core_x[i * 2 + 1];
@@ -1501,7 +1512,8 @@ int configure_kernels(Engine &e) {
     const size_t rh2 = (size_t)(kMaxWords * 64 + 1) * sizeof(int32_t);
     e.occ_probe = occ((const void *)k_ann_probe<1>, (const void *)k_ann_probe<2>, 256, rh2);
     e.occ_compress = occ((const void *)k_ann_compress<1>, (const void *)k_ann_compress<2>, 256, 0);
-    e.occ_insert = occ((const void *)k_ann_insert<1>, (const void *)k_ann_insert<2>, 128, 0);
+    e.occ_insert = occ((const void *)k_ann_decide<1>, (const void *)k_ann_decide<2>, 256, 0);
+    e.occ_place = occ((const void *)k_ann_place<1>, (const void *)k_ann_place<2>, 128, 0);
     e.occ_expand = occ((const void *)k_expand, (const void *)k_expand, 256, 0);
     (void)cudaGetLastError();
     return 0;
@@ -1549,8 +1561,14 @@ void launch_ann_compress(Engine &e, cudaStream_t s) {
     else k_ann_compress<1><<<grid_spawns(e, 256, e.occ_compress), 256, 0, s>>>(e.sys, e.st);
 }
 void launch_ann_insert(Engine &e, cudaStream_t s) {
-    if (e.sys.L == 2) k_ann_insert<2><<<grid_spawns(e, 128, e.occ_insert), 128, 0, s>>>(e.sys, e.st, e.d_params);
-    else k_ann_insert<1><<<grid_spawns(e, 128, e.occ_insert), 128, 0, s>>>(e.sys, e.st, e.d_params);
+    const int gp = clamp_grid(e.st.max_spawned / 128 + 1, e.num_sms * e.occ_place);
+    if (e.sys.L == 2) {
+        k_ann_decide<2><<<grid_spawns(e, 256, e.occ_insert), 256, 0, s>>>(e.sys, e.st, e.d_params);
+        k_ann_place<2><<<gp, 128, 0, s>>>(e.sys, e.st);
+    } else {
+        k_ann_decide<1><<<grid_spawns(e, 256, e.occ_insert), 256, 0, s>>>(e.sys, e.st, e.d_params);
+        k_ann_place<1><<<gp, 128, 0, s>>>(e.sys, e.st);
+    }
 }
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
     if (e.sys.L == 2)

@@ -19,7 +19,7 @@
 //                looked up once in the walker hash: a found determinant gets
 //                its sums, counts and initiator bits in acc/meta (the found
 //                branch, merged by k_merge_stats), an absent one becomes a
-//                new unique determinant for k_ann_insert
+//                new unique determinant for k_ann_decide
 //   k_sk_long    the same for longer runs, one block per run
 // The result is the hash form's, bit for bit: the same sums, the same flag
 // rules (FindResidualParticle's coherent rule and initiator bits, from the
@@ -119,7 +119,7 @@ __device__ inline void group_found(const DevState &st, long long slot, const Gro
 }
 
 // A group whose determinant is absent: unique determinant number pos for
-// k_ann_insert (candidate pos = record `lead`, its sums in rep_q/rep_cnt).
+// k_ann_decide (candidate pos = record `lead`, its sums in rep_q/rep_cnt).
 __device__ inline void group_absent(const DevState &st, unsigned long long pos, long long lead, const Group &g, int L) {
     if (pos >= (unsigned long long)st.max_spawned) {
         set_err(st.ctl, NECI_GPU_ERR_SPAWN_FULL);
