@@ -1154,6 +1154,7 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     st.n_core = 0;
     dfree(e, st.core_slot);
     dfree(e, st.core_x);
+    dfree(e, st.core_x32);
     dfree(e, st.core_y);
     dfree(e, st.core_rowptr);
     dfree(e, st.core_col);
@@ -1181,6 +1182,7 @@ int core_build(Engine &e, const long long *dcore, long long n_core) {
     } tmp{e};
     if (int r = dalloc(e, &st.core_slot, (size_t)n_core)) return r;
     if (int r = dalloc(e, &st.core_x, (size_t)n_core * L)) return r;
+    if (int r = dalloc(e, &st.core_x32, (size_t)n_core * L)) return r;
     if (int r = dalloc(e, &st.core_y, (size_t)n_core * L)) return r;
     if (int r = dalloc(e, &st.core_rowptr, (size_t)n_core + 1)) return r;
     if (int r = dalloc(e, &st.core_dets, (size_t)n_core * e.sys.W)) return r;

@@ -215,6 +215,7 @@ struct DevState {
     long long *spawn_par;
     double *rdm2;
     double *core_x, *core_y;
+    float *core_x32;               // core_x rounded to FP32, written in mixed-precision steps
     long long *core_rowptr;
     int core_group;                // lanes that sum one core row (core_group_size)
     // segments of the core rows, core_segment_len elements at most: each

@@ -376,6 +376,8 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
             if (core) {
                 const int ci = st.core_of_slot[j];
                 NECI_FOR_RUNS(k, L) st.core_x[(long long)ci * L + k] = C[k];
+                if (p.precision == NECI_PREC_MIXED)
+                    NECI_FOR_RUNS(k, L) st.core_x32[(long long)ci * L + k] = (float)C[k];
             }
         }
         // holes go to the free list (FciMCPar.F90:1415-1427)
@@ -619,11 +621,18 @@ __global__ void k_expand(DevState st) {
 // loads and gathers in flight.
 // ===========================================================================
 // Elements a lane loads before it accumulates them (in element order): its
-// column indices and values first, then the gathers of x.
-constexpr int kCoreDepth = 8;
+// column indices and values first, then the gathers of x; and the resident
+// blocks of 256 threads per SM the kernel is compiled for.
+#ifndef NECI_CORE_DEPTH
+#define NECI_CORE_DEPTH 8
+#endif
+#ifndef NECI_CORE_BLOCKS_PER_SM
+#define NECI_CORE_BLOCKS_PER_SM 4
+#endif
+constexpr int kCoreDepth = NECI_CORE_DEPTH;
 
 template <int G, bool MIXED>
-__global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterParams *pp) {
+__global__ void __launch_bounds__(256, NECI_CORE_BLOCKS_PER_SM) k_core(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     using VT = typename std::conditional<MIXED, float, double>::type;
     const int L = s.L;
@@ -636,7 +645,9 @@ __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterP
     const long long nround = ((nseg + ngrp - 1) / ngrp) * ngrp;
     const int32_t *col = st.core_col;
     const VT *val = MIXED ? (const VT *)st.core_val32 : (const VT *)st.core_val;
-    const double *xv = st.core_x;
+    // x in the precision of the products: the FP32 copy the sweep wrote in a
+    // mixed-precision step (the same rounding as converting here)
+    const VT *xv = MIXED ? (const VT *)st.core_x32 : (const VT *)st.core_x;
     for (long long sg = grp; sg < nround; sg += ngrp) {
         const bool valid = sg < nseg;
         CoreSeg seg = {0, 0, 0};
@@ -644,9 +655,9 @@ __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterP
         const long long e1 = seg.e0 + seg.len;
         double acc[2] = {0.0, 0.0};
         float hi[2] = {0.0f, 0.0f}, lo[2] = {0.0f, 0.0f};
-        auto add = [&](int k, VT v, double x) {
+        auto add = [&](int k, VT v, VT x) {
             if (!MIXED) {
-                acc[k] = fma(-(double)v, x, acc[k]);
+                acc[k] = fma(-(double)v, (double)x, acc[k]);
             } else {
                 const float term = -__fmul_rn((float)v, (float)x);
                 const float t = __fadd_rn(hi[k], term);
@@ -655,27 +666,28 @@ __global__ void __launch_bounds__(256) k_core(DevSys s, DevState st, const IterP
                 hi[k] = t;
             }
         };
-        long long e = seg.e0 + gl;
-        for (; e + (kCoreDepth - 1) * G < e1; e += kCoreDepth * G) {
+        // kCoreDepth elements of the lane per pass, the last pass predicated
+        // (its elements past the segment's end are neither loaded nor added)
+        for (long long e = seg.e0 + gl; e < e1; e += kCoreDepth * G) {
+            const long long left = (e1 - e + G - 1) / G;  // the lane's elements from e on
+            const int nv = left < kCoreDepth ? (int)left : kCoreDepth;
+            const int32_t *cp = col + e;
+            const VT *vp = val + e;
             int cc[kCoreDepth];
             VT vv[kCoreDepth];
 #pragma unroll
             for (int j = 0; j < kCoreDepth; ++j) {
-                cc[j] = col[e + j * G];
-                vv[j] = val[e + j * G];
+                cc[j] = j < nv ? cp[j * G] : 0;
+                vv[j] = j < nv ? vp[j * G] : (VT)0;
             }
             NECI_FOR_RUNS(k, L) {
-                double xx[kCoreDepth];
+                VT xx[kCoreDepth];
 #pragma unroll
-                for (int j = 0; j < kCoreDepth; ++j) xx[j] = xv[(long long)cc[j] * L + k];
+                for (int j = 0; j < kCoreDepth; ++j) xx[j] = j < nv ? xv[cc[j] * L + k] : (VT)0;
 #pragma unroll
-                for (int j = 0; j < kCoreDepth; ++j) add(k, vv[j], xx[j]);
+                for (int j = 0; j < kCoreDepth; ++j)
+                    if (j < nv) add(k, vv[j], xx[j]);
             }
-        }
-        for (; e < e1; e += G) {
-            const int cj = col[e];
-            const VT vj = val[e];
-            NECI_FOR_RUNS(k, L) add(k, vj, xv[(long long)cj * L + k]);
         }
         const long long row = seg.row & 0x7FFFFFFF;
         const bool single = seg.row >= 0;
