@@ -52,7 +52,6 @@ struct Engine {
     int spawn_occ = 8;
     int sort_bpsm = 2;
     int core_seg_lane = kCoreSegmentPerLane;  // NECI_OPT_CORE_SEGMENT
-    size_t core_smem = 0;                     // shared memory of the core kernel's copy of x (bytes)
     cudaStream_t stream = nullptr;
     IterParams *d_params = nullptr;
     IterParams *h_params = nullptr;          // pinned

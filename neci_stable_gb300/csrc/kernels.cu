@@ -621,24 +621,20 @@ __global__ void k_expand(DevState st) {
 // loads and gathers in flight.
 // ===========================================================================
 // Elements a lane loads before it accumulates them (in element order): its
-// column indices and values first, then the gathers of x.
+// column indices and values first, then the gathers of x; and the resident
+// blocks of 256 threads per SM the kernel is compiled for.
 #ifndef NECI_CORE_DEPTH
 #define NECI_CORE_DEPTH 8
 #endif
+#ifndef NECI_CORE_BLOCKS_PER_SM
+#define NECI_CORE_BLOCKS_PER_SM 4
+#endif
 constexpr int kCoreDepth = NECI_CORE_DEPTH;
-// One block of kCoreThreads per SM; the first nsx entries of x (all of it
-// when it fits) are copied into the block's shared memory, where random
-// gathers cost a few bank cycles instead of an L1 line each: gathers of x
-// through L1 ran at about one line per clock per SM, which bounded the
-// kernel (the gathered element does not change, so neither does any sum).
-constexpr int kCoreThreads = 1024;
 
 template <int G, bool MIXED>
-__global__ void __launch_bounds__(kCoreThreads, 1) k_core(DevSys s, DevState st, const IterParams *pp, long long nsx) {
+__global__ void __launch_bounds__(256, NECI_CORE_BLOCKS_PER_SM) k_core(DevSys s, DevState st, const IterParams *pp) {
     if (halted(st)) return;
     using VT = typename std::conditional<MIXED, float, double>::type;
-    extern __shared__ __align__(16) unsigned char core_smem[];
-    VT *sx = (VT *)core_smem;
     const int L = s.L;
     const double tau = pp->tau;
     const int gl = threadIdx.x & (G - 1);
@@ -652,15 +648,6 @@ __global__ void __launch_bounds__(kCoreThreads, 1) k_core(DevSys s, DevState st,
     // x in the precision of the products: the FP32 copy the sweep wrote in a
     // mixed-precision step (the same rounding as converting here)
     const VT *xv = MIXED ? (const VT *)st.core_x32 : (const VT *)st.core_x;
-    {
-        // nsx entries: 16-byte copies, then the remainder
-        constexpr int per16 = 16 / sizeof(VT);
-        const long long n16 = nsx / per16;
-        for (long long i = threadIdx.x; i < n16; i += blockDim.x)
-            reinterpret_cast<int4 *>(sx)[i] = reinterpret_cast<const int4 *>(xv)[i];
-        for (long long i = n16 * per16 + threadIdx.x; i < nsx; i += blockDim.x) sx[i] = xv[i];
-        __syncthreads();
-    }
     for (long long sg = grp; sg < nround; sg += ngrp) {
         const bool valid = sg < nseg;
         CoreSeg seg = {0, 0, 0};
@@ -696,10 +683,7 @@ __global__ void __launch_bounds__(kCoreThreads, 1) k_core(DevSys s, DevState st,
             NECI_FOR_RUNS(k, L) {
                 VT xx[kCoreDepth];
 #pragma unroll
-                for (int j = 0; j < kCoreDepth; ++j) {
-                    const int xi = cc[j] * L + k;
-                    xx[j] = j < nv ? (xi < nsx ? sx[xi] : xv[xi]) : (VT)0;
-                }
+                for (int j = 0; j < kCoreDepth; ++j) xx[j] = j < nv ? xv[cc[j] * L + k] : (VT)0;
 #pragma unroll
                 for (int j = 0; j < kCoreDepth; ++j)
                     if (j < nv) add(k, vv[j], xx[j]);
@@ -1529,20 +1513,6 @@ int configure_kernels(Engine &e) {
         return 1;
     if (cudaFuncSetAttribute(k_merge_stats<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, merge_max) != cudaSuccess)
         return 1;
-    // the core kernel's copy of x: as much of the opt-in shared memory of a
-    // block as the device has, up to 200 KB
-    {
-        int optin = 0;
-        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e.device) != cudaSuccess) optin = 48 * 1024;
-        e.core_smem = (size_t)(optin < 200 * 1024 ? optin : 200 * 1024) & ~(size_t)15;
-        const void *fs[] = {(const void *)k_core<1, false>, (const void *)k_core<2, false>, (const void *)k_core<4, false>,
-                            (const void *)k_core<8, false>, (const void *)k_core<16, false>, (const void *)k_core<32, false>,
-                            (const void *)k_core<1, true>, (const void *)k_core<2, true>, (const void *)k_core<4, true>,
-                            (const void *)k_core<8, true>, (const void *)k_core<16, true>, (const void *)k_core<32, true>};
-        for (const void *f : fs)
-            if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e.core_smem) != cudaSuccess)
-                return 1;
-    }
     // resident blocks per SM of each instance (the smaller of the two run counts)
     auto occ = [](const void *f1, const void *f2, int threads, size_t smem) {
         int a = 0, b = 0;
@@ -1576,14 +1546,9 @@ void launch_sweep(Engine &e, cudaStream_t s) {
 void launch_expand(Engine &e, cudaStream_t s) { k_expand<<<grid_spawns(e, 256, e.occ_expand), 256, 0, s>>>(e.st); }
 template <int G>
 static void launch_core_g(Engine &e, cudaStream_t s) {
-    const long long want = e.st.n_core_seg * G / kCoreThreads + 1;
-    const int grid = (int)(want < e.num_sms ? want : e.num_sms);
-    const bool mixed = e.h_params->precision == NECI_PREC_MIXED;
-    const size_t vsz = mixed ? sizeof(float) : sizeof(double);
-    long long nsx = (long long)(e.core_smem / vsz);
-    if (nsx > e.st.n_core * e.sys.L) nsx = e.st.n_core * e.sys.L;
-    if (mixed) k_core<G, true><<<grid, kCoreThreads, nsx * vsz, s>>>(e.sys, e.st, e.d_params, nsx);
-    else k_core<G, false><<<grid, kCoreThreads, nsx * vsz, s>>>(e.sys, e.st, e.d_params, nsx);
+    const int grid = clamp_grid(e.st.n_core_seg * G / 256 + 1, e.num_sms * 8);
+    if (e.h_params->precision == NECI_PREC_MIXED) k_core<G, true><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
+    else k_core<G, false><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
     if (e.st.n_core_multi > 0)
         k_core_sum<<<clamp_grid(e.st.n_core_multi / 256 + 1, e.num_sms), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
