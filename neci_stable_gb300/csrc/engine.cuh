@@ -246,11 +246,15 @@ struct DevState {
 };
 
 // Lanes that sum one row of the core Hamiltonian in k_core: the smallest
-// power of two G with 4 G at least the mean row length, at most 32 (so a
-// lane takes about four elements of a row); 1 sums a row in one thread.
+// power of two G with NECI_CORE_LANE_ELEMS * G at least the mean row length,
+// at most 32 (so a lane takes about that many elements of a row); 1 sums a
+// row in one thread.
+#ifndef NECI_CORE_LANE_ELEMS
+#define NECI_CORE_LANE_ELEMS 4
+#endif
 __host__ __device__ inline int core_group_size(long long nnz, long long n_core) {
     int g = 1;
-    while (g < 32 && 4ll * g * n_core < nnz) g <<= 1;
+    while (g < 32 && (long long)NECI_CORE_LANE_ELEMS * g * n_core < nnz) g <<= 1;
     return g;
 }
 
