@@ -282,7 +282,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.att, (size_t)st.max_att);
     A(st.big, (size_t)st.max_big * 3);
     A(st.huge, (size_t)kMaxHuge * 3);
-    A(st.acc, (size_t)st.max_walkers * s.L);
+    A(st.acc, (size_t)(st.max_walkers + kStagePad) * s.L);
     A(st.meta, (size_t)(st.max_walkers + kStagePad) * s.L);
     A(st.cand, (size_t)st.max_spawned);
     A(st.cand_h, (size_t)st.max_spawned);

@@ -1080,11 +1080,12 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
     double a_tp[2] = {0, 0}, a_norm[2] = {0, 0};
     unsigned long long a_s[2] = {0, 0}, a_occ = 0, a_holes = 0, a_found = 0, a_tomb = 0;
     // Tiles staged into shared memory by TMA bulk copies as in k_sweep: the
-    // rows and the per-slot spawn counts (meta) of the tile.
+    // rows, the per-slot spawn counts (meta) and the per-slot spawn sums
+    // (acc) of the tile, so that no global load waits in a slot's path.
     extern __shared__ __align__(16) unsigned char merge_smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int stage_ok;
-    const size_t stage_bytes = (size_t)kStageTile * (R * 8 + L * 4);
+    const size_t stage_bytes = (size_t)kStageTile * (R * 8 + L * 4 + L * 8);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -1097,14 +1098,15 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
         const int rows = stage_rows(tile, n);
         if (rows == 0) return;
         unsigned char *base = merge_smem + (k & 1) * stage_bytes;
-        const uint32_t br = (uint32_t)rows * R * 8, bm = (uint32_t)rows * L * 4;
+        const uint32_t br = (uint32_t)rows * R * 8, bm = (uint32_t)rows * L * 4, ba = (uint32_t)rows * L * 8;
         fence_proxy_async_smem();
-        mbar_expect_tx(&bars[k & 1], br + bm);
+        mbar_expect_tx(&bars[k & 1], br + bm + ba);
         bulk_g2s(base, st.dets + tile * kStageTile * R, br, &bars[k & 1]);
         bulk_g2s(base + (size_t)kStageTile * R * 8, st.meta + tile * kStageTile * L, bm, &bars[k & 1]);
+        bulk_g2s(base + (size_t)kStageTile * (R * 8 + L * 4), st.acc + tile * kStageTile * L, ba, &bars[k & 1]);
     };
-    // one slot: its row (global, for writes), staged row and staged meta
-    auto body = [&](long long j, const long long *sr, const uint32_t *sm) {
+    // one slot: its row (global, for writes), staged row, meta and acc
+    auto body = [&](long long j, const long long *sr, const uint32_t *sm, const long long *sa) {
         long long *r = st.dets + j * R;
         const long long flags = sr[W + L];
         const bool core = st.n_core > 0 && is_core_flags(flags);
@@ -1133,7 +1135,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
             double S[2] = {0.0, 0.0};
             bool nz = false;  // a block of the compressed list (CompressSpawnedList drops zero sums)
             NECI_FOR_RUNS(k, L) {
-                const long long q = st.acc[j * L + k];
+                const long long q = sa[k];
                 st.acc[j * L + k] = 0;
                 st.meta[j * L + k] = 0;
                 a_s[k] += (unsigned long long)(q < 0 ? -q : q);
@@ -1235,7 +1237,8 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
         const long long j = tile * kStageTile + threadIdx.x;
         if (j < n)
             body(j, (const long long *)sbase + (size_t)threadIdx.x * R,
-                 (const uint32_t *)(sbase + (size_t)kStageTile * R * 8) + (size_t)threadIdx.x * L);
+                 (const uint32_t *)(sbase + (size_t)kStageTile * R * 8) + (size_t)threadIdx.x * L,
+                 (const long long *)(sbase + (size_t)kStageTile * (R * 8 + L * 4)) + (size_t)threadIdx.x * L);
         __syncthreads();  // this round's stage is refilled two rounds on
     }
     double v[12] = {a_born[0], a_born[1], a_ann[0], a_ann[1], a_ab[0], a_ab[1], a_rm[0], a_rm[1],
@@ -1494,7 +1497,7 @@ void launch_rehash(Engine &e, cudaStream_t s) {
 
 // Dynamic shared memory of the staged sweeps: two stages of a tile.
 static size_t sweep_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R + 2) * 8; }
-static size_t merge_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R * 8 + e.sys.L * 4); }
+static size_t merge_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R * 8 + e.sys.L * 12); }
 
 int configure_kernels(Engine &e) {
     // The stages and the block reductions' shared arrays pass the default
@@ -1503,7 +1506,7 @@ int configure_kernels(Engine &e) {
     // (kMaxWords det words, two signs, a flag word), never lowered.
     const int rmax = kMaxWords + 2 + 1;
     const int sweep_max = 2 * kStageTile * (rmax + 2) * 8;
-    const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 4);
+    const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 12);
     if (cudaFuncSetAttribute(k_sweep<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
         cudaFuncSetAttribute(k_sweep<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
         cudaFuncSetAttribute(k_sweep<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
