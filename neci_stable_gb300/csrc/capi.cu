@@ -131,54 +131,10 @@ void annihilation_passes(Engine &e, int lookup) {
     stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
 }
 
-// While a step graph is captured: the compaction and the rehash (seven
-// launches that do nothing in almost every step) go into the bodies of two
-// conditional nodes, whose conditions a one-thread kernel sets from the
-// flags of the last step, so that a step that needs neither launches
-// neither.
-static int maintenance_nodes(Engine &e) {
-    cudaStreamCaptureStatus cs;
-    cudaGraph_t g;
-    if (cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, &g) != cudaSuccess) return 1;
-    cudaGraphConditionalHandle h[2];
-    for (int i = 0; i < 2; ++i)
-        if (cudaGraphConditionalHandleCreate(&h[i], g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return 1;
-    launch_maint_cond(e, e.stream, h[0], h[1]);
-    for (int i = 0; i < 2; ++i) {
-        const cudaGraphNode_t *deps;
-        const cudaGraphEdgeData *edata;
-        size_t nd;
-        if (cudaStreamGetCaptureInfo(e.stream, &cs, nullptr, &g, &deps, &edata, &nd) != cudaSuccess) return 1;
-        cudaGraphNodeParams p = {};
-        p.type = cudaGraphNodeTypeConditional;
-        p.conditional.handle = h[i];
-        p.conditional.type = cudaGraphCondTypeIf;
-        p.conditional.size = 1;
-        cudaGraphNode_t node;
-        if (cudaGraphAddNode(&node, g, deps, edata, nd, &p) != cudaSuccess) return 1;
-        if (cudaStreamBeginCaptureToGraph(e.side, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
-                                          cudaStreamCaptureModeThreadLocal) != cudaSuccess)
-            return 1;
-        if (i == 0) launch_compact(e, e.side);
-        else launch_rehash(e, e.side);
-        cudaGraph_t body;
-        if (cudaStreamEndCapture(e.side, &body) != cudaSuccess) return 1;
-        if (cudaStreamUpdateCaptureDependencies(e.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies) !=
-            cudaSuccess)
-            return 1;
-    }
-    return 0;
-}
-
 // The launch sequence of one PerformFCIMCycPar step.
 void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (!e.profiling && cudaStreamIsCapturing(e.stream, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive) {
-        if (maintenance_nodes(e)) e.capture_err = 1;
-    } else {
-        stage(e, K_COMPACT, [&] { launch_compact(e, e.stream); });
-        stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
-    }
+    stage(e, K_COMPACT, [&] { launch_compact(e, e.stream); });
+    stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
     stage(e, K_BEGIN, [&] { launch_begin(e, e.stream); });
     stage(e, K_SWEEP, [&] { launch_sweep(e, e.stream); });
     stage(e, K_EXPAND, [&] { launch_expand(e, e.stream); });
@@ -223,13 +179,8 @@ int ensure_graph(Engine &e) {
     if (!e.graphs[k]) {
         cudaGraph_t g;
         CK(cudaStreamBeginCapture(e.stream, cudaStreamCaptureModeThreadLocal));
-        e.capture_err = 0;
         step_sequence(e, e.d_stats, 1);  // each replay writes the next record (d_stat_pos)
         CK(cudaStreamEndCapture(e.stream, &g));
-        if (e.capture_err) {
-            cudaGraphDestroy(g);
-            return fail(NECI_GPU_ERR_CUDA, "capture of the step graph's conditional nodes failed");
-        }
         CK(cudaGraphInstantiate(&e.graphs[k], g, 0));
         cudaGraphDestroy(g);
         e.graph_core[k] = core;
@@ -290,12 +241,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     if (ce != cudaSuccess) { delete ctx; return fail(NECI_GPU_ERR_CUDA, cudaGetErrorString(ce)); }
     cudaDeviceGetAttribute(&e.num_sms, cudaDevAttrMultiProcessorCount, device);
     ce = cudaStreamCreateWithFlags(&e.stream, cudaStreamNonBlocking);
-    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking);
-    if (ce != cudaSuccess) {
-        if (e.stream) cudaStreamDestroy(e.stream);
-        delete ctx;
-        return fail(NECI_GPU_ERR_CUDA, cudaGetErrorString(ce));
-    }
+    if (ce != cudaSuccess) { delete ctx; return fail(NECI_GPU_ERR_CUDA, cudaGetErrorString(ce)); }
     DevSys &s = e.sys;
     s.nel = sys->nel;
     s.nbasis = sys->nbasis;
@@ -394,7 +340,6 @@ int32_t neci_gpu_free(neci_gpu_ctx *ctx) {
     if (e.h_stats) cudaFreeHost(e.h_stats);
     for (int k = 0; k < 2 * K_NUM; ++k)
         if (e.ev[k]) cudaEventDestroy(e.ev[k]);
-    if (e.side) cudaStreamDestroy(e.side);
     if (e.stream) cudaStreamDestroy(e.stream);
     delete ctx;
     return NECI_GPU_OK;
@@ -964,11 +909,7 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         cudaError_t ce = cudaEventRecord(e0.fork_ev, e0.stream);
         for (int c = 1; c < n_ctx && ce == cudaSuccess; ++c) ce = cudaStreamWaitEvent(ctxs[c]->e.stream, e0.fork_ev, 0);
         if (ce == cudaSuccess)
-            for (int c = 0; c < n_ctx; ++c) {
-                ctxs[c]->e.capture_err = 0;
-                step_sequence(ctxs[c]->e, ctxs[c]->e.d_stats, 1);
-                if (ctxs[c]->e.capture_err) ce = cudaErrorStreamCaptureInvalidated;
-            }
+            for (int c = 0; c < n_ctx; ++c) step_sequence(ctxs[c]->e, ctxs[c]->e.d_stats, 1);
         for (int c = 1; c < n_ctx && ce == cudaSuccess; ++c) {
             Engine &e = ctxs[c]->e;
             ce = cudaEventRecord(e.join_ev, e.stream);

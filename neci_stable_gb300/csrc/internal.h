@@ -53,9 +53,6 @@ struct Engine {
     int sort_bpsm = 2;
     int core_seg_lane = kCoreSegmentPerLane;  // NECI_OPT_CORE_SEGMENT
     cudaStream_t stream = nullptr;
-    // captures the bodies of the step graph's conditional nodes
-    cudaStream_t side = nullptr;
-    int capture_err = 0;                     // a failure while a step graph was captured
     IterParams *d_params = nullptr;
     IterParams *h_params = nullptr;          // pinned
     neci_gpu_iter_stats *d_stats = nullptr;  // per-step records
@@ -99,7 +96,6 @@ inline bool fused_lookup(const Engine &e) {
 void launch_begin(Engine &e, cudaStream_t s);
 void launch_rehash(Engine &e, cudaStream_t s);
 void launch_compact(Engine &e, cudaStream_t s);
-void launch_maint_cond(Engine &e, cudaStream_t s, cudaGraphConditionalHandle compact, cudaGraphConditionalHandle rehash);
 void launch_sweep(Engine &e, cudaStream_t s);
 // sets the per-kernel launch attributes a context needs (non-zero: failure)
 int configure_kernels(Engine &e);

@@ -219,18 +219,6 @@ __global__ void k_compact_move(DevSys s, DevState st) {
 }
 
 // Closes the compaction: TotWalkers = K, the hash is rebuilt next.
-// The conditions of the step graph's two maintenance nodes, from the flags
-// the last step's k_final set: compaction, and the rebuild of the walker
-// hash (which a compaction implies).  The kernels inside check the flags
-// again, so that the same launches run correctly outside a graph.
-__global__ void k_maint_cond(DevState st, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle hr) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const Control *c = st.ctl;
-    const bool live = c->halted == 0;
-    cudaGraphSetConditional(hc, live && c->compact ? 1u : 0u);
-    cudaGraphSetConditional(hr, live && (c->compact || c->rehash) ? 1u : 0u);
-}
-
 __global__ void k_compact_done(DevState st) {
     if (halted(st)) return;
     Control *c = st.ctl;
@@ -1500,10 +1488,6 @@ void launch_compact(Engine &e, cudaStream_t s) {
     k_compact_holes<<<grid, kCompactTile, 0, s>>>(e.sys, e.st);
     k_compact_move<<<grid_slots(e), 256, 0, s>>>(e.sys, e.st);
     k_compact_done<<<1, 32, 0, s>>>(e.st);
-}
-
-void launch_maint_cond(Engine &e, cudaStream_t s, cudaGraphConditionalHandle hc, cudaGraphConditionalHandle hr) {
-    k_maint_cond<<<1, 32, 0, s>>>(e.st, hc, hr);
 }
 
 void launch_rehash(Engine &e, cudaStream_t s) {
