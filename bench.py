@@ -42,17 +42,17 @@ N_ORB, N_EL, SEED = 24, 10, 20240601
 TARGET_WALKERS = 1.0e7
 BLOOM = 3.0
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture of
-# this workload at 1e7 walkers) per unit of work, for roofline.traffic:
-# kernel -> (bytes per unit, step count that is the unit).
-# The spawn kernel is bound by instruction issue, not by HBM: one ncu capture
-# of it on this workload (profiles/spawn_n24_pchb_2e6.md), reported beside its
-# HBM roofline.
-NCU_SPAWN_ISSUE = {"issue_active": 0.571, "alu_pipe": 0.563, "fp64_pipe": 0.398, "warps_active": 0.431,
-                   "lanes_per_instruction": 18.1, "dram_bytes_per_attempt": 14.6}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, ncu captures of
+# this workload: profiles/step_kernels_n24_pchb_1e7.md, and for the spawn
+# kernel profiles/spawn_fp64_n24_2e6.md) per unit of work, for
+# roofline.traffic: kernel -> (bytes per unit, step count that is the unit).
+# The spawn kernel is bound by instruction issue, not by HBM: its issue
+# figures from the same capture are reported beside its HBM roofline.
+NCU_SPAWN_ISSUE = {"issue_active": 0.605, "alu_pipe": 0.544, "fp64_pipe": 0.326, "warps_active": 0.436,
+                   "lanes_per_instruction": 24.4, "dram_bytes_per_attempt": 14.0}
 
 NCU_DRAM_BYTES_PER_UNIT = {
-    "spawn": (14.6, "n_attempts"),
+    "spawn": (14.0, "n_attempts"),
     "sweep": (47.2, "tot_walkers"),
     "merge_stats": (38.3, "tot_walkers"),
     "ann_probe": (102.3, "n_spawned"),
