@@ -131,7 +131,31 @@ void annihilation_passes(Engine &e, int lookup) {
     stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
 }
 
-// The launch sequence of one PerformFCIMCycPar step.
+// The passes of a step's annihilation that write the found branch (acc,
+// meta): the probe of the hash form (unless the spawn kernel did it), or the
+// sort form with its grouping, which also lists the new determinants.
+void lookup_passes(Engine &e) {
+    if (e.ann_mode == NECI_ANN_SORT) {
+        annihilation_passes(e, 1);
+        return;
+    }
+    if (!fused_lookup(e)) stage(e, K_ANN_PROBE, [&] { launch_ann_probe(e, e.stream); });
+}
+
+// The compression of the hash form (the sort form has none left).
+void compress_pass(Engine &e) {
+    if (e.ann_mode != NECI_ANN_SORT) stage(e, K_ANN_COMPRESS, [&] { launch_ann_compress(e, e.stream); });
+}
+
+// The launch sequence of one PerformFCIMCycPar step.  After the walker-hash
+// lookup of the spawns (the found branch in acc/meta) the step has two
+// independent branches: the determinants not found (compression, decision,
+// placement) and the merge sweep over the slots the step began with, which
+// skips the slots the sweep freed (the only ones a placement can fill).  The
+// placement accounts for its own determinants' statistics, so the two run
+// side by side on two streams (in the step graph, two branches), and in
+// either order give the same list and the same counts.  With profiling on
+// they run one after the other on the step's stream.
 void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_COMPACT, [&] { launch_compact(e, e.stream); });
     stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
@@ -140,11 +164,23 @@ void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
     stage(e, K_EXPAND, [&] { launch_expand(e, e.stream); });
     stage(e, K_SPAWN, [&] { launch_spawn(e, e.stream); });
     if (e.st.n_core > 0) stage(e, K_CORE, [&] { launch_core(e, e.stream); });
-    annihilation_passes(e, 1);
-    stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream); });
-    stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, e.st.n_core > 0 ? 1 : 0); });
+    const int with_core = e.st.n_core > 0 ? 1 : 0;
+    lookup_passes(e);
+    if (e.profiling) {
+        compress_pass(e);
+        stage(e, K_ANN_INSERT, [&] { launch_ann_insert(e, e.stream, 1); });
+        stage(e, K_MERGE_STATS, [&] { launch_merge_stats(e, e.stream, with_core, 1); });
+    } else {
+        cudaEventRecord(e.branch_ev, e.stream);
+        cudaStreamWaitEvent(e.side, e.branch_ev, 0);
+        launch_merge_stats(e, e.side, with_core, 1);
+        cudaEventRecord(e.merge_ev, e.side);
+        compress_pass(e);
+        launch_ann_insert(e, e.stream, 1);
+        cudaStreamWaitEvent(e.stream, e.merge_ev, 0);
+    }
     if (e.sys.rdm) stage(e, K_RDM, [&] { launch_rdm(e, e.stream); });
-    stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, e.d_stat_pos, advance); });
+    stage(e, K_FINAL, [&] { launch_final(e, e.stream, out, e.d_stat_pos, advance, 1); });
 }
 
 // Destroys the cached step graphs (after any change the kernels see by value).
@@ -278,6 +314,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.hash, (size_t)st.hash_n);
     A(st.slot_bucket, (size_t)st.max_walkers);
     A(st.free_list, (size_t)st.max_walkers + 1);
+    A(st.hole_mark, (size_t)st.max_walkers + kStagePad);
     A(st.spawn, (size_t)st.max_spawned * s.R);
     A(st.att, (size_t)st.max_att);
     A(st.big, (size_t)st.max_big * 3);
@@ -313,6 +350,10 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
         for (int k = 0; k < 2 * K_NUM; ++k) cudaEventCreate(&e.ev[k]);
         cudaEventCreateWithFlags(&e.fork_ev, cudaEventDisableTiming);
         cudaEventCreateWithFlags(&e.join_ev, cudaEventDisableTiming);
+        if (cudaEventCreateWithFlags(&e.branch_ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&e.merge_ev, cudaEventDisableTiming) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&e.side, cudaStreamNonBlocking) != cudaSuccess)
+            rc = fail(NECI_GPU_ERR_CUDA, "stream or event creation failed");
         e.graph_version = fresh_graph_version();
         if (cudaStreamSynchronize(e.stream) != cudaSuccess) rc = fail(NECI_GPU_ERR_CUDA, "sync after init");
     }
@@ -335,6 +376,9 @@ int32_t neci_gpu_free(neci_gpu_ctx *ctx) {
     if (e.batch_graph) cudaGraphExecDestroy(e.batch_graph);
     if (e.fork_ev) cudaEventDestroy(e.fork_ev);
     if (e.join_ev) cudaEventDestroy(e.join_ev);
+    if (e.branch_ev) cudaEventDestroy(e.branch_ev);
+    if (e.merge_ev) cudaEventDestroy(e.merge_ev);
+    if (e.side) cudaStreamDestroy(e.side);
     for (void *p : e.allocs) cudaFree(p);
     if (e.h_params) cudaFreeHost(e.h_params);
     if (e.h_stats) cudaFreeHost(e.h_stats);
@@ -985,9 +1029,9 @@ int32_t neci_gpu_annihilate(neci_gpu_ctx *ctx, const neci_gpu_iter_params *p, co
     annihilation_passes(e, 1);
     e.fuse_probe = fused;
     e.fuse_mode = mode;
-    launch_ann_insert(e, e.stream);
-    launch_merge_stats(e, e.stream, 0);
-    launch_final(e, e.stream, e.d_stats, nullptr, 0);
+    launch_ann_insert(e, e.stream, 0);
+    launch_merge_stats(e, e.stream, 0, 0);
+    launch_final(e, e.stream, e.d_stats, nullptr, 0, 0);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(e.h_stats, e.d_stats, sizeof(neci_gpu_iter_stats), cudaMemcpyDeviceToHost, e.stream));
     CK(cudaStreamSynchronize(e.stream));

@@ -59,6 +59,7 @@ struct Control {
     unsigned long long n_huge;          // parents expanded by the whole grid
     unsigned long long n_long;          // sort annihilation: runs of equal keys left to k_sk_long
     unsigned long long n_place;         // new determinants k_ann_decide leaves to k_ann_place
+    unsigned long long n_pre;           // slots in use before this step's new determinants
     unsigned long long abs_q[2];        // sum |q| of all spawn records (fixed point)
     unsigned long long abs_s[2];        // sum |sum q| of the unique spawned determinants
     int err;
@@ -182,6 +183,7 @@ struct DevState {
     uint32_t *hash;                // walker hash: slot+1, kEmpty, kTomb
     unsigned long long hash_n;     // buckets (power of two)
     uint32_t *slot_bucket;         // bucket holding each slot
+    uint8_t *hole_mark;            // 1: the slot went to this step's free list (k_sweep)
     int32_t *free_list;
     long long max_walkers, max_spawned, max_att;
     long long *spawn;              // spawn records

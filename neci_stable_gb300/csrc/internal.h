@@ -67,6 +67,10 @@ struct Engine {
     cudaGraphExec_t batch_graph = nullptr;
     std::vector<std::pair<const void *, unsigned long long>> batch_key;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    // the step's two branches after the walker-hash lookup (new determinants;
+    // the merge sweep), on stream and side
+    cudaStream_t side = nullptr;
+    cudaEvent_t branch_ev = nullptr, merge_ev = nullptr;
     std::vector<void *> allocs;
     bool have_ref = false, have_pchb = false;
     double *inv_single = nullptr;  // device table of DevSys::inv_single
@@ -104,9 +108,9 @@ void launch_spawn(Engine &e, cudaStream_t s);
 void launch_core(Engine &e, cudaStream_t s);
 void launch_ann_probe(Engine &e, cudaStream_t s);
 void launch_ann_compress(Engine &e, cudaStream_t s);
-void launch_ann_insert(Engine &e, cudaStream_t s);
-void launch_merge_stats(Engine &e, cudaStream_t s, int with_core);
-void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter);
+void launch_ann_insert(Engine &e, cudaStream_t s, int split);
+void launch_merge_stats(Engine &e, cudaStream_t s, int with_core, int split);
+void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter, int split);
 void launch_rdm(Engine &e, cudaStream_t s);
 
 // sort form of the annihilation and core selection (sort_kernels.cu)

@@ -55,6 +55,7 @@ __global__ void k_begin(DevState st) {
         c->n_huge = 0;
         c->n_long = 0;
         c->n_place = 0;
+        c->n_pre = c->tot_walkers;
         for (int k = 0; k < 2; ++k) {
             c->abs_q[k] = 0; c->abs_s[k] = 0;
             c->nborn[k] = c->ndied[k] = c->nannihil[k] = c->naborted[k] = c->nremoved[k] = 0.0;
@@ -489,6 +490,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
         {
             const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
             const bool want = hole || freed;
+            if (live) st.hole_mark[j] = want ? 1 : 0;
             const unsigned int mf = __ballot_sync(0xffffffffu, want);
             unsigned int nat = 0;
             NECI_FOR_RUNS(k, L) nat += nsp[k];
@@ -993,10 +995,14 @@ __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const
     block_add_u<3>(u, du);
 }
 
+// split: the merge sweep skips the new determinants (it runs beside this
+// kernel), so their |C| and C^2 (TotParts, norm) and the reference's sign
+// are taken here.
 template <int LR>
-__global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st) {
+__global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st, int split) {
     if (halted(st)) return;
     Control *c = st.ctl;
+    double a_tp[2] = {0.0, 0.0}, a_norm[2] = {0.0, 0.0};
     const long long n = (long long)min(c->n_place, (unsigned long long)st.max_spawned);
     const int W = s.W, R = s.R;
     constexpr int L = LR;
@@ -1054,6 +1060,16 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st) {
         if (st.n_core > 0) st.core_of_slot[slot] = -1;
         a_tomb -= hash_insert(st, slot, st.cand_h[ci], c);
         ++a_new;
+        if (split) {
+            bool is_ref = true;
+            NECI_FOR_WORDS(w, W) if (d[w] != s.ilut_ref[w]) is_ref = false;
+            NECI_FOR_RUNS(k, L) {
+                const double v = word_to_double(ws[k]);
+                a_tp[k] += fabs(v);
+                a_norm[k] += v * v;
+                if (is_ref) c->noat_hf[k] = v;
+            }
+        }
         st.diagH[slot] = diag_helement(s, d) - s.hii;
         const int ic = excit_level(s.ilut_ref, d, W);
         st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
@@ -1061,6 +1077,11 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st) {
     unsigned long long u[2] = {(unsigned long long)a_tomb, a_new};  // two's complement for -count
     unsigned long long *const du[2] = {&c->n_tomb, &c->n_new};
     block_add_u<2>(u, du);
+    if (split) {
+        double v[4] = {a_tp[0], a_tp[1], a_norm[0], a_norm[1]};
+        double *const dst[4] = {&c->tot_parts[0], &c->tot_parts[1], &c->norm[0], &c->norm[1]};
+        block_add<4>(v, dst, L);
+    }
 }
 
 // ===========================================================================
@@ -1069,11 +1090,15 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st) {
 // ===========================================================================
 // LR: lenof_sign of the instance (1, or 2 for a replica pair).
 template <int LR>
-__global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core) {
+__global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, const IterParams *pp, int with_core,
+                                                        int split) {
     if (halted(st)) return;
     const IterParams p = *pp;
     Control *c = st.ctl;
-    const long long n = (long long)min(c->tot_walkers, (unsigned long long)st.max_walkers);
+    // split: the slots the step began with, less those its sweep freed
+    // (k_ann_place fills some of them and counts its own determinants), so
+    // that the placement may run at the same time
+    const long long n = (long long)min(split ? c->n_pre : c->tot_walkers, (unsigned long long)st.max_walkers);
     const int W = s.W, R = s.R;
     constexpr int L = LR;
     double a_born[2] = {0, 0}, a_ann[2] = {0, 0}, a_ab[2] = {0, 0}, a_rm[2] = {0, 0};
@@ -1235,7 +1260,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
             }
         }
         const long long j = tile * kStageTile + threadIdx.x;
-        if (j < n)
+        if (j < n && !(split && st.hole_mark[j]))
             body(j, (const long long *)sbase + (size_t)threadIdx.x * R,
                  (const uint32_t *)(sbase + (size_t)kStageTile * R * 8) + (size_t)threadIdx.x * L,
                  (const long long *)(sbase + (size_t)kStageTile * (R * 8 + L * 4)) + (size_t)threadIdx.x * L);
@@ -1407,8 +1432,11 @@ __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use
 // The record goes to out[*pos] (and *pos advances, up to max_out - 1) when
 // pos is given: the step graph is the same for every step of a batch, and
 // each step's record lands in its own place.
+// split: the merge sweep counted the slots the step began with less the
+// freed ones; the new determinants are occupied, and the freed slots the
+// placement did not fill are holes.
 __global__ void k_final(DevState st, neci_gpu_iter_stats *base, int *pos, int max_out, IterParams *pp,
-                        int advance_iter, long long n_core) {
+                        int advance_iter, long long n_core, int split) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     neci_gpu_iter_stats *out = base;
     if (pos) {
@@ -1425,6 +1453,11 @@ __global__ void k_final(DevState st, neci_gpu_iter_stats *base, int *pos, int ma
         return;
     }
     if (c->tot_walkers > (unsigned long long)st.max_walkers) c->tot_walkers = (unsigned long long)st.max_walkers;
+    if (split) {
+        const unsigned long long used = c->free_taken < c->n_free ? c->free_taken : c->n_free;
+        c->n_occupied += c->n_new;
+        c->n_holes += c->n_free - used;
+    }
     neci_gpu_iter_stats r;
     for (int k = 0; k < 2; ++k) {
         r.nborn[k] = c->nborn[k];
@@ -1575,21 +1608,23 @@ void launch_ann_compress(Engine &e, cudaStream_t s) {
     if (e.sys.L == 2) k_ann_compress<2><<<grid_spawns(e, 256, e.occ_compress), 256, 0, s>>>(e.sys, e.st);
     else k_ann_compress<1><<<grid_spawns(e, 256, e.occ_compress), 256, 0, s>>>(e.sys, e.st);
 }
-void launch_ann_insert(Engine &e, cudaStream_t s) {
+void launch_ann_insert(Engine &e, cudaStream_t s, int split) {
     const int gp = clamp_grid(e.st.max_spawned / 128 + 1, e.num_sms * e.occ_place);
     if (e.sys.L == 2) {
         k_ann_decide<2><<<grid_spawns(e, 256, e.occ_insert), 256, 0, s>>>(e.sys, e.st, e.d_params);
-        k_ann_place<2><<<gp, 128, 0, s>>>(e.sys, e.st);
+        k_ann_place<2><<<gp, 128, 0, s>>>(e.sys, e.st, split);
     } else {
         k_ann_decide<1><<<grid_spawns(e, 256, e.occ_insert), 256, 0, s>>>(e.sys, e.st, e.d_params);
-        k_ann_place<1><<<gp, 128, 0, s>>>(e.sys, e.st);
+        k_ann_place<1><<<gp, 128, 0, s>>>(e.sys, e.st, split);
     }
 }
-void launch_merge_stats(Engine &e, cudaStream_t s, int with_core) {
+void launch_merge_stats(Engine &e, cudaStream_t s, int with_core, int split) {
     if (e.sys.L == 2)
-        k_merge_stats<2><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core);
+        k_merge_stats<2><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core,
+                                                                                   split);
     else
-        k_merge_stats<1><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core);
+        k_merge_stats<1><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core,
+                                                                                   split);
 }
 void launch_rdm(Engine &e, cudaStream_t s) {
     if (!e.sys.rdm) return;
@@ -1600,8 +1635,8 @@ void launch_rdm(Engine &e, cudaStream_t s) {
     k_rdm_diag<<<grid_slots(e), 256, use_shared ? shm : 0, s>>>(e.sys, e.st, use_shared);
 }
 
-void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter) {
-    k_final<<<1, 32, 0, s>>>(e.st, out, pos, e.max_stats, e.d_params, advance_iter, e.st.n_core);
+void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter, int split) {
+    k_final<<<1, 32, 0, s>>>(e.st, out, pos, e.max_stats, e.d_params, advance_iter, e.st.n_core, split);
 }
 
 }  // namespace neci
