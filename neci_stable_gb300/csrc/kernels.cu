@@ -1618,13 +1618,18 @@ void launch_ann_insert(Engine &e, cudaStream_t s, int split) {
         k_ann_place<1><<<gp, 128, 0, s>>>(e.sys, e.st, split);
     }
 }
+// Blocks per SM of the merge sweep when it runs beside the placement
+// (split): fewer than the sweep's own, so that the placement's blocks find
+// registers on every SM.
+#ifndef NECI_MERGE_SPLIT_BLOCKS
+#define NECI_MERGE_SPLIT_BLOCKS 2
+#endif
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core, int split) {
+    const int grid = split ? clamp_grid(e.st.max_walkers / 2048 + 1, e.num_sms * NECI_MERGE_SPLIT_BLOCKS) : grid_for(e, 256);
     if (e.sys.L == 2)
-        k_merge_stats<2><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core,
-                                                                                   split);
+        k_merge_stats<2><<<grid, kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core, split);
     else
-        k_merge_stats<1><<<grid_for(e, 256), kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core,
-                                                                                   split);
+        k_merge_stats<1><<<grid, kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core, split);
 }
 void launch_rdm(Engine &e, cudaStream_t s) {
     if (!e.sys.rdm) return;
