@@ -1013,23 +1013,46 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st, int sp
     unsigned long long a_new = 0;
     for (long long pi = blockIdx.x * (long long)blockDim.x + threadIdx.x; pi < nround; pi += stride) {
         const bool want = pi < n;
-        long long ci = 0;
-        if (want) ci = st.place[pi];
+        // the determinant, its signs and flag word (cleared from the sums'
+        // slots) and its hash
+        unsigned long long d[kMaxWords], h = 0;
+        long long ws[2] = {0, 0}, flags = 0;
+        NECI_FOR_WORDS(w, W) d[w] = 0ull;
+        if (want) {
+            const long long ci = st.place[pi];
+            const long long *rec = st.spawn + (long long)st.cand[ci] * R;
+            NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
+            h = st.cand_h[ci];
+            NECI_FOR_RUNS(k, L) {
+                ws[k] = st.rep_q[ci * L + k];
+                st.rep_q[ci * L + k] = 0;
+            }
+            flags = (long long)(((unsigned long long)st.rep_cnt[ci * (L + 1)] << 32) | st.rep_cnt[ci * (L + 1) + L]);
+            st.rep_cnt[ci * (L + 1)] = 0u;
+            st.rep_cnt[ci * (L + 1) + L] = 0u;
+        }
         // Slots for the warp's determinants: the next holes of the free list
         // (one atomic on its cursor), then fresh slots at the end of the list
-        // (one atomic on TotWalkers) when the holes run out.
+        // (one atomic on TotWalkers) when the holes run out.  The matrix
+        // elements are computed while the atomics are in flight.
         const unsigned int ballot = __ballot_sync(0xffffffffu, want);
         const unsigned int nwant = __popc(ballot);
         const unsigned int rank = __popc(ballot & ((1u << lane) - 1u));
+        const int leader = nwant ? __ffs(ballot) - 1 : 0;
         unsigned long long t0 = 0, f0 = 0;
         const unsigned long long nfree = c->n_free;
+        if (nwant && lane == leader) {
+            t0 = atomicAdd(&c->free_taken, (unsigned long long)nwant);
+            const unsigned long long from_free = t0 >= nfree ? 0ull : min(nfree - t0, (unsigned long long)nwant);
+            if (nwant > from_free) f0 = atomicAdd(&c->tot_walkers, (unsigned long long)(nwant - from_free));
+        }
+        double dh = 0.0, odh = 0.0;
+        if (want) {
+            dh = diag_helement(s, d) - s.hii;
+            const int ic = excit_level(s.ilut_ref, d, W);
+            odh = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
+        }
         if (nwant) {
-            const int leader = __ffs(ballot) - 1;
-            if (lane == leader) {
-                t0 = atomicAdd(&c->free_taken, (unsigned long long)nwant);
-                const unsigned long long from_free = t0 >= nfree ? 0ull : min(nfree - t0, (unsigned long long)nwant);
-                if (nwant > from_free) f0 = atomicAdd(&c->tot_walkers, (unsigned long long)(nwant - from_free));
-            }
             t0 = __shfl_sync(0xffffffffu, t0, leader);
             f0 = __shfl_sync(0xffffffffu, f0, leader);
         }
@@ -1037,28 +1060,18 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st, int sp
         const unsigned long long t = t0 + rank;
         const unsigned long long first_fresh = t0 >= nfree ? t0 : nfree;  // the first t that gets a fresh slot
         const long long slot = t < nfree ? (long long)st.free_list[t] : (long long)(f0 + (t - first_fresh));
-        long long ws[2] = {0, 0};
-        NECI_FOR_RUNS(k, L) {
-            ws[k] = st.rep_q[ci * L + k];
-            st.rep_q[ci * L + k] = 0;
-        }
-        const long long flags = (long long)(((unsigned long long)st.rep_cnt[ci * (L + 1)] << 32) |
-                                            st.rep_cnt[ci * (L + 1) + L]);
-        st.rep_cnt[ci * (L + 1)] = 0u;
-        st.rep_cnt[ci * (L + 1) + L] = 0u;
         if (slot + 1 >= st.max_walkers) {
             set_err(c, NECI_GPU_ERR_LIST_FULL);
             continue;
         }
-        const long long *rec = st.spawn + (long long)st.cand[ci] * R;
-        unsigned long long d[kMaxWords];
-        NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
         long long *o = st.dets + slot * R;
         NECI_FOR_WORDS(w, W) o[w] = (long long)d[w];
         NECI_FOR_RUNS(k, L) o[W + k] = ws[k];
         o[W + L] = flags & ~1ll;
+        st.diagH[slot] = dh;
+        st.offdiagH[slot] = odh;
         if (st.n_core > 0) st.core_of_slot[slot] = -1;
-        a_tomb -= hash_insert(st, slot, st.cand_h[ci], c);
+        a_tomb -= hash_insert(st, slot, h, c);
         ++a_new;
         if (split) {
             bool is_ref = true;
@@ -1070,9 +1083,6 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st, int sp
                 if (is_ref) c->noat_hf[k] = v;
             }
         }
-        st.diagH[slot] = diag_helement(s, d) - s.hii;
-        const int ic = excit_level(s.ilut_ref, d, W);
-        st.offdiagH[slot] = (ic >= 1 && ic <= 2) ? offdiag_helement(s, s.ilut_ref, d, ic) : 0.0;
     }
     unsigned long long u[2] = {(unsigned long long)a_tomb, a_new};  // two's complement for -count
     unsigned long long *const du[2] = {&c->n_tomb, &c->n_new};
