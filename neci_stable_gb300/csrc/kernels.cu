@@ -580,7 +580,8 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
 }
 
 // ===========================================================================
-// k_expand: attempt entries of heavily populated parents, one block per parent.
+// k_expand: attempt entries of heavily populated parents, one warp per parent
+// (the whole grid for the few with more than kHugeAttempts).
 // ===========================================================================
 __global__ void k_expand(DevState st) {
     if (halted(st)) return;
@@ -592,13 +593,16 @@ __global__ void k_expand(DevState st) {
              a += (unsigned long long)gridDim.x * blockDim.x)
             st.att[base + a] = head | (a << 34);
     }
-    // the others: a block per parent
+    // the others (33 to 65536 attempts, mostly a few hundred): a warp per parent
     const unsigned long long nb = min(st.ctl->n_big, (unsigned long long)st.max_big);
-    for (unsigned long long b = blockIdx.x; b < nb; b += gridDim.x) {
+    const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
+    const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
+    const unsigned long long lane = threadIdx.x & 31;
+    for (unsigned long long b = warp; b < nb; b += nwarps) {
         const unsigned long long head = st.big[3 * b];
         const unsigned long long n = st.big[3 * b + 1];
         const unsigned long long base = st.big[3 * b + 2];
-        for (unsigned long long a = threadIdx.x; a < n; a += blockDim.x) st.att[base + a] = head | (a << 34);
+        for (unsigned long long a = lane; a < n; a += 32) st.att[base + a] = head | (a << 34);
     }
 }
 
