@@ -1599,8 +1599,9 @@ static void launch_core_g(Engine &e, cudaStream_t s) {
     const int grid = clamp_grid(e.st.n_core_seg * G / 256 + 1, e.num_sms * 8);
     if (e.h_params->precision == NECI_PREC_MIXED) k_core<G, true><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
     else k_core<G, false><<<grid, 256, 0, s>>>(e.sys, e.st, e.d_params);
-    if (e.st.n_core_multi > 0)
-        k_core_sum<<<clamp_grid(e.st.n_core_multi / 256 + 1, e.num_sms), 256, 0, s>>>(e.sys, e.st, e.d_params);
+    // launched whether or not a row has several segments, so that a step's
+    // launches do not depend on the core's row lengths
+    k_core_sum<<<clamp_grid(e.st.n_core_multi / 256 + 1, e.num_sms), 256, 0, s>>>(e.sys, e.st, e.d_params);
 }
 void launch_core(Engine &e, cudaStream_t s) {
     if (e.st.n_core <= 0) return;
