@@ -355,7 +355,9 @@ int32_t neci_gpu_core_nnz(neci_gpu_ctx *ctx, int64_t *nnz);
 
 /* ---- engine variants ------------------------------------------------------
  * Options that choose how a step is computed, never what it computes: the
- * walker lists and estimators are the same bit for bit under every setting.
+ * walker lists and estimators are the same bit for bit under every setting
+ * of the first two, and NECI_OPT_CORE_SEGMENT changes only the order of the
+ * core projection's additions.
  * They have no counterpart in the reference, whose one CPU path has no such
  * choice; the reference routine each variant restates is named below.  A
  * change takes effect from the next step.                                 */
