@@ -854,6 +854,21 @@ static void update_fuse_probe(Engine &e, const neci_gpu_iter_stats &last) {
     }
 }
 
+// The merge sweep's blocks per SM while it runs beside the placement: two
+// where the branch of the new determinants is the longer one (many unique
+// spawned determinants per slot: n = 24, the Hubbard lattice), four, as
+// alone, where the merge sweep is (a large list with few spawns per slot:
+// n = 64), with a margin so that the choice does not flap.
+static void update_merge_blocks(Engine &e, const neci_gpu_iter_stats &last) {
+    if (last.tot_walkers <= 0) return;
+    const double r = (double)last.n_unique / (double)last.tot_walkers;
+    const int want = e.merge_bpsm == 2 ? (r < 0.10 ? 4 : 2) : (r > 0.20 ? 2 : 4);
+    if (want != e.merge_bpsm) {
+        e.merge_bpsm = want;
+        drop_graphs(e);
+    }
+}
+
 static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_gpu_iter_stats *stats,
                      double *device_ms = nullptr) {
     if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
@@ -890,6 +905,7 @@ static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_
             }
         done += batch;
         update_fuse_probe(e, stats[done - 1]);
+        update_merge_blocks(e, stats[done - 1]);
     }
     return NECI_GPU_OK;
 }
@@ -998,7 +1014,10 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         Engine &e = ctxs[c]->e;
         std::memcpy(stats + (size_t)c * n_iter, e.h_stats, sizeof(neci_gpu_iter_stats) * n_iter);
         for (int i = 0; i < n_iter && !first_err; ++i) first_err = e.h_stats[i].err;
-        if (!first_err) update_fuse_probe(e, e.h_stats[n_iter - 1]);
+        if (!first_err) {
+            update_fuse_probe(e, e.h_stats[n_iter - 1]);
+            update_merge_blocks(e, e.h_stats[n_iter - 1]);
+        }
     }
     if (first_err) return fail(first_err, "device reported an error in a batched step");
     return NECI_GPU_OK;

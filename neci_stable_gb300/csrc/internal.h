@@ -51,6 +51,7 @@ struct Engine {
     // blocks per SM (DevState::comp_shift holds the table load setting)
     int spawn_occ = 8;
     int sort_bpsm = 2;
+    int merge_bpsm = 2;  // merge sweep blocks per SM beside the placement (update_merge_blocks)
     int core_seg_lane = kCoreSegmentPerLane;  // NECI_OPT_CORE_SEGMENT
     cudaStream_t stream = nullptr;
     IterParams *d_params = nullptr;

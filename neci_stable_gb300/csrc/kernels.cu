@@ -1634,13 +1634,10 @@ void launch_ann_insert(Engine &e, cudaStream_t s, int split) {
     }
 }
 // Blocks per SM of the merge sweep when it runs beside the placement
-// (split): fewer than the sweep's own, so that the placement's blocks find
-// registers on every SM.
-#ifndef NECI_MERGE_SPLIT_BLOCKS
-#define NECI_MERGE_SPLIT_BLOCKS 2
-#endif
+// (split): e.merge_bpsm, two unless the merge sweep is the longer branch, so
+// that the placement's blocks find registers on every SM.
 void launch_merge_stats(Engine &e, cudaStream_t s, int with_core, int split) {
-    const int grid = split ? clamp_grid(e.st.max_walkers / 2048 + 1, e.num_sms * NECI_MERGE_SPLIT_BLOCKS) : grid_for(e, 256);
+    const int grid = split ? clamp_grid(e.st.max_walkers / 2048 + 1, e.num_sms * e.merge_bpsm) : grid_for(e, 256);
     if (e.sys.L == 2)
         k_merge_stats<2><<<grid, kStageTile, merge_smem_bytes(e), s>>>(e.sys, e.st, e.d_params, with_core, split);
     else
