@@ -449,7 +449,13 @@ __device__ inline long long to_fixed(double x, int *overflow) {
     if (!(fabs(s) < 9.2e18)) { *overflow = 1; return 0; }
     return __double2ll_rn(s);
 }
-__device__ inline double from_fixed(long long q) { return __ll2double_rn(q) * 0x1.0p-32; }
+// q 2^-32 as a double: the conversion rounds once, then the scaling by 2^-32
+// is exact and done on the exponent field (|q| >= 1 keeps it far from the
+// subnormal range), not as an FP64 multiply.
+__device__ inline double from_fixed(long long q) {
+    const double v = __ll2double_rn(q);
+    return q == 0 ? 0.0 : __longlong_as_double(__double_as_longlong(v) - (32ll << 52));
+}
 __device__ inline double word_to_double(long long w) { return __longlong_as_double(w); }
 __device__ inline long long double_to_word(double d) { return __double_as_longlong(d); }
 // |x| and -x on the high word, in integer instructions: materialised as FP64

@@ -403,7 +403,9 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
             // skipped
             const double odh = soffd[threadIdx.x];
             const bool has_odh = abs_bits(odh) != 0;
-            NECI_FOR_RUNS(k, L) if (has_odh) acc_en[k] += odh * C[k];
+            // behind a vote: most warps hold no connection of the reference
+            if (__any_sync(__activemask(), has_odh))
+                NECI_FOR_RUNS(k, L) if (has_odh) acc_en[k] += odh * C[k];
             if (__any_sync(__activemask(), is_ref))
                 if (is_ref) NECI_FOR_RUNS(k, L) acc_hf[k] += C[k];
             const unsigned long long dkey = det_key(d, W, p.seed);
@@ -954,15 +956,15 @@ __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const
                     NECI_FOR_RUNS(k, L)
                         if (!test_bit(flags, init_flag_bit(k))) { a_ab[k] += fabs(ss[k]); ss[k] = 0.0; }
                 bool unocc = true;
-                NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) unocc = false;
+                NECI_FOR_RUNS(k, L) if (abs_bits(ss[k]) >= dbl_bits(kEps12)) unocc = false;
                 if (!unocc) {
                     unsigned long long d[kMaxWords];
                     NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
                     const unsigned long long dkey = det_key(d, W, p.seed);
                     NECI_FOR_RUNS(k, L) {
                         // stochRoundSpawn (Annihilation.F90:1354-1418)
-                        const double a = fabs(ss[k]);
-                        if (a > kEps12 && a < p.occupied_thresh) {
+                        const double a = abs_dbl(ss[k]);
+                        if (abs_bits(a) > dbl_bits(kEps12) && abs_bits(a) < dbl_bits(p.occupied_thresh)) {
                             Stream rng(dkey, p.iter, P_ANN_ROUND, k, 0);
                             const double pRemove =
                                 1.0 - (dbl_bits(p.occupied_thresh) == dbl_bits(1.0) ? a : div_dbl(a, p.occupied_thresh));
@@ -970,7 +972,7 @@ __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const
                             else { a_born[k] += p.occupied_thresh - a; ss[k] = fsign(p.occupied_thresh, ss[k]); }
                         }
                     }
-                    NECI_FOR_RUNS(k, L) if (fabs(ss[k]) >= kEps12) want = true;
+                    NECI_FOR_RUNS(k, L) if (abs_bits(ss[k]) >= dbl_bits(kEps12)) want = true;
                 }
             }
             // the sums are consumed: cleared for the next step, or, for a
@@ -1212,7 +1214,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
         }
         if (!core) {
             NECI_FOR_RUNS(k, L) {
-                const double a = fabs(C[k]);
+                const double a = abs_dbl(C[k]);
                 if (abs_bits(a) > dbl_bits(kEps12) && abs_bits(a) < dbl_bits(p.occupied_thresh)) {
                     unsigned long long d[kMaxWords];
                     NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)sr[w];
