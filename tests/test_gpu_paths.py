@@ -70,6 +70,9 @@ def assert_same_stats(sg, sc, tag):
         np.testing.assert_allclose(getattr(sg, f)[:], getattr(sc, f)[:], rtol=1e-9, atol=1e-7, err_msg=f"{f} {tag}")
     assert (sg.n_attempts, sg.n_spawned, sg.n_new, sg.n_occupied) == (sc.n_attempts, sc.n_spawned, sc.n_new,
                                                                      sc.n_occupied), tag
+    # every slot in use is occupied or a hole (the merge sweep counts the slots
+    # the step began with, the placement and the final kernel the rest)
+    assert sg.n_occupied + sg.holes_in_list == sg.tot_walkers, (tag, sg.n_occupied, sg.holes_in_list, sg.tot_walkers)
 
 
 def step_both(spec, eng, orc, iters, tau, seed, first_iter=1, shift=0.0, check_unique=True):
