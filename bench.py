@@ -184,7 +184,9 @@ def algorithmic_bytes(kernel, st, W, L, nnz=0, fused=True):
     N = st["n_new"]
     slots = st["tot_walkers"]
     if kernel == "sweep":
-        return slots * (R + G) + D * 8 * L + D * 16
+        # rows and diagonal data read, signs written, and each slot's
+        # free-list mark (1 B)
+        return slots * (R + G + 1) + D * 8 * L + D * 16
     if kernel == "spawn":
         # the 8 B attempt entries read (parent rows and tables are gathered
         # from L2); fused: per spawn a hash bucket and the row's det words
@@ -204,16 +206,17 @@ def algorithmic_bytes(kernel, st, W, L, nnz=0, fused=True):
     if kernel == "ann_insert":
         return N * (R + G + 4)
     if kernel == "merge_stats":
-        return slots * (R + 12 * L)
+        # rows, spawn counts and sums, and the free-list mark read
+        return slots * (R + 12 * L + 1)
     # the sort form of the annihilation (NECI_ANN_SORT)
     if kernel == "sort_keys":
         # per record: its determinant words and amplitudes read, key, index
         # and 64-bit hash written
         return S * (8 * (W + L) + 16)
     if kernel == "sort_radix":
-        # 4 passes of 8 bits over (32-bit key, 32-bit index): the count pass
-        # reads the key, the scatter reads and writes key and index
-        return S * 4 * (4 + 16)
+        # 3 passes of 8 bits over (24-bit key in 32 bits, 32-bit index): the
+        # count pass reads the key, the scatter reads and writes key and index
+        return S * 3 * (4 + 16)
     if kernel == "sort_group":
         # per record: key, its neighbour's key and the index read, the record
         # gathered; per unique determinant: the hash probe (bucket and row
