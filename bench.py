@@ -751,10 +751,11 @@ def main():
     sort_ms = sum(v["ms"] for v in sort_stages.values())
     sort_bytes = sum(v["algorithmic_bytes"] for v in sort_stages.values())
     ktm = {k: v for k, v in r["ktimes_mixed"].items() if v[1] > 0}
-    # compaction (5) and rehash (2, idle unless flagged), begin, sweep, expand,
-    # spawn, compress, decide, place, merge, final; the probe unless the spawn
-    # kernel does it; the core projection and the sum of its long rows
-    launches_per_step = 16 + (2 if r["last"]["n_core"] > 0 else 0) + (0 if fused else 1)
+    # rehash (2, idle unless flagged), begin, sweep, expand, spawn, compress,
+    # decide, place, merge, final; the probe unless the spawn kernel does it;
+    # the core projection and the sum of its long rows (a compaction, when a
+    # step leaves more holes than walkers, runs between calls)
+    launches_per_step = 11 + (2 if r["last"]["n_core"] > 0 else 0) + (0 if fused else 1)
     line = {
         "metric": METRIC, "value": updates / dev_s, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 * dev_s / args.steps, "higher_is_better": True,

@@ -157,7 +157,6 @@ void compress_pass(Engine &e) {
 // either order give the same list and the same counts.  With profiling on
 // they run one after the other on the step's stream.
 void step_sequence(Engine &e, neci_gpu_iter_stats *out, int advance) {
-    stage(e, K_COMPACT, [&] { launch_compact(e, e.stream); });
     stage(e, K_REHASH, [&] { launch_rehash(e, e.stream); });
     stage(e, K_BEGIN, [&] { launch_begin(e, e.stream); });
     stage(e, K_SWEEP, [&] { launch_sweep(e, e.stream); });
@@ -869,12 +868,28 @@ static void update_merge_blocks(Engine &e, const neci_gpu_iter_stats &last) {
     }
 }
 
+// Compaction of the walker list runs between calls, before the first step
+// of a call whose last step left more holes than occupied slots (the rule
+// k_final applies to Control::compact; the compaction kernels check that
+// flag and ask for the rebuild of the walker hash, which the next step
+// does).  It is not part of the step graph: holes cost only sweep work, and
+// the five launches would do nothing in almost every step.
+static void update_compact_due(Engine &e, const neci_gpu_iter_stats &last) {
+    e.compact_due = last.tot_walkers > 4ll * kCompactTile && 2 * last.holes_in_list > last.tot_walkers;
+}
+static void compact_if_due(Engine &e, cudaStream_t s) {
+    if (!e.compact_due) return;
+    stage(e, K_COMPACT, [&] { launch_compact(e, s); });
+    e.compact_due = false;
+}
+
 static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_gpu_iter_stats *stats,
                      double *device_ms = nullptr) {
     if (const char *why = not_ready(e)) return fail(NECI_GPU_ERR_INVALID, why);
     if (p->tau <= 0.0 || p->av_mc_excits <= 0.0) return fail(NECI_GPU_ERR_INVALID, "tau and AvMCExcits must be positive");
     copy_params(*e.h_params, *p);
     CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e.stream));
+    compact_if_due(e, e.stream);
     int done = 0;
     if (device_ms) *device_ms = 0.0;
     while (done < n_iter) {
@@ -906,6 +921,8 @@ static int run_steps(Engine &e, const neci_gpu_iter_params *p, int n_iter, neci_
         done += batch;
         update_fuse_probe(e, stats[done - 1]);
         update_merge_blocks(e, stats[done - 1]);
+        update_compact_due(e, stats[done - 1]);
+        if (done < n_iter) compact_if_due(e, e.stream);
     }
     return NECI_GPU_OK;
 }
@@ -993,6 +1010,7 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         Engine &e = ctxs[c]->e;
         CK(cudaMemcpyAsync(e.d_params, e.h_params, sizeof(IterParams), cudaMemcpyHostToDevice, e0.stream));
         CK(cudaMemsetAsync(e.d_stat_pos, 0, sizeof(int), e0.stream));
+        compact_if_due(e, e0.stream);
     }
     CK(cudaEventRecord(e0.ev[0], e0.stream));
     for (int i = 0; i < n_iter; ++i) CK(cudaGraphLaunch(e0.batch_graph, e0.stream));
@@ -1017,6 +1035,7 @@ int32_t neci_gpu_iterate_batch(neci_gpu_ctx **ctxs, int32_t n_ctx, const neci_gp
         if (!first_err) {
             update_fuse_probe(e, e.h_stats[n_iter - 1]);
             update_merge_blocks(e, e.h_stats[n_iter - 1]);
+            update_compact_due(e, e.h_stats[n_iter - 1]);
         }
     }
     if (first_err) return fail(first_err, "device reported an error in a batched step");

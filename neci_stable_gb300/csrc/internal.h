@@ -52,6 +52,7 @@ struct Engine {
     int spawn_occ = 8;
     int sort_bpsm = 2;
     int merge_bpsm = 2;  // merge sweep blocks per SM beside the placement (update_merge_blocks)
+    bool compact_due = false;  // the last step left more holes than occupied slots
     int core_seg_lane = kCoreSegmentPerLane;  // NECI_OPT_CORE_SEGMENT
     cudaStream_t stream = nullptr;
     IterParams *d_params = nullptr;
