@@ -902,6 +902,11 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
 // spread over the lanes of the decisions it would hold every lane of a warp
 // that had one survivor.
 // ===========================================================================
+// The high half of a survivor's flag word that stands for "the flag word of
+// its one record"; a flag word computed from the counts holds initiator bits
+// only, so its high half is never this.
+constexpr uint32_t kOwnFlags = 0xFFFFFFFFu;
+
 // LR: lenof_sign of the instance (1, or 2 for a replica pair).
 template <int LR>
 __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const IterParams *pp) {
@@ -922,27 +927,28 @@ __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const
         long long ci = 0;
         double ss[2] = {0.0, 0.0};
         long long flags = 0;
+        uint32_t nrec = 0;
         if (ri < n) {
             ci = st.reps[ri];
             const uint32_t rb = st.rep_bucket[ri];
             if (rb != kNoBucket) st.spawn_hash[rb] = kEmpty;  // leave the table clean
-            const long long *rec = st.spawn + (long long)st.cand[ci] * R;
             long long q[2] = {0, 0};
             uint32_t cnt[2] = {0, 0};
             NECI_FOR_RUNS(k, L) {
                 q[k] = st.rep_q[ci * L + k];
                 cnt[k] = st.rep_cnt[ci * (L + 1) + k];
             }
-            const uint32_t nrec = st.rep_cnt[ci * (L + 1) + L];
-            // compressed flags (CompressSpawnedList / FindResidualParticle)
-            if (nrec == 1) {
-                flags = rec[W + L];
-            } else if (p.t_trunc_initiator) {
+            nrec = st.rep_cnt[ci * (L + 1) + L];
+            // compressed flags (CompressSpawnedList / FindResidualParticle):
+            // a block of one record keeps that record's flag word, read by
+            // k_ann_place for the survivors only; its initiator bit in a run
+            // with a non-zero amplitude is the one in the run's count, so the
+            // counts decide the abort for every block without the record
+            if (p.t_trunc_initiator)
                 NECI_FOR_RUNS(k, L) {
                     const bool coh = p.t_init_coherent_rule && (cnt[k] & 0x7FFFFFFFu) >= 2u;
                     if (coh || (cnt[k] & 0x80000000u)) flags |= 1ll << init_flag_bit(k);
                 }
-            }
             bool zero = true;
             NECI_FOR_RUNS(k, L) {
                 if (q[k] != 0) zero = false;
@@ -958,6 +964,7 @@ __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const
                 bool unocc = true;
                 NECI_FOR_RUNS(k, L) if (abs_bits(ss[k]) >= dbl_bits(kEps12)) unocc = false;
                 if (!unocc) {
+                    const long long *rec = st.spawn + (long long)st.cand[ci] * R;
                     unsigned long long d[kMaxWords];
                     NECI_FOR_WORDS(w, W) d[w] = (unsigned long long)rec[w];
                     const unsigned long long dkey = det_key(d, W, p.seed);
@@ -978,12 +985,14 @@ __global__ void __launch_bounds__(256) k_ann_decide(DevSys s, DevState st, const
             // the sums are consumed: cleared for the next step, or, for a
             // survivor, replaced by its signs (as double bits) and its flag
             // word (low half in the record count's place, high half in the
-            // first run's count) for k_ann_place, which clears them
+            // first run's count; kOwnFlags there for a block of one record,
+            // whose own flag word k_ann_place reads) for k_ann_place, which
+            // clears them
             NECI_FOR_RUNS(k, L) {
                 st.rep_q[ci * L + k] = want ? double_to_word(ss[k]) : 0ll;
                 st.rep_cnt[ci * (L + 1) + k] = 0u;
             }
-            if (want) st.rep_cnt[ci * (L + 1)] = (uint32_t)((unsigned long long)flags >> 32);
+            if (want) st.rep_cnt[ci * (L + 1)] = nrec == 1 ? kOwnFlags : (uint32_t)((unsigned long long)flags >> 32);
             st.rep_cnt[ci * (L + 1) + L] = want ? (uint32_t)flags : 0u;
         }
         const unsigned long long pos = warp_append1(&c->n_place, want);
@@ -1033,7 +1042,9 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st, int sp
                 ws[k] = st.rep_q[ci * L + k];
                 st.rep_q[ci * L + k] = 0;
             }
-            flags = (long long)(((unsigned long long)st.rep_cnt[ci * (L + 1)] << 32) | st.rep_cnt[ci * (L + 1) + L]);
+            const uint32_t hi = st.rep_cnt[ci * (L + 1)];
+            flags = hi == kOwnFlags ? rec[W + L]
+                                    : (long long)(((unsigned long long)hi << 32) | st.rep_cnt[ci * (L + 1) + L]);
             st.rep_cnt[ci * (L + 1)] = 0u;
             st.rep_cnt[ci * (L + 1) + L] = 0u;
         }
