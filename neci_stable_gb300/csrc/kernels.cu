@@ -870,11 +870,13 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
                 const long long fl = rec[W + L];
                 atomicAdd(&st.rep_cnt[owner * (L + 1) + L], 1u);  // records in the block
                 NECI_FOR_RUNS(k, L) {
+                    // FindResidualParticle ORs a record's initiator bit of a
+                    // run into the block whatever its amplitude in that run
+                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&st.rep_cnt[owner * (L + 1) + k], 0x80000000u);
                     const long long q = rec[W + k];
                     if (q == 0) continue;
                     atomicAdd((unsigned long long *)&st.rep_q[owner * L + k], (unsigned long long)q);
                     atomicAdd(&st.rep_cnt[owner * (L + 1) + k], 1u);
-                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&st.rep_cnt[owner * (L + 1) + k], 0x80000000u);
                 }
             }
         }

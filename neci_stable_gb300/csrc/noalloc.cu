@@ -107,12 +107,14 @@ __global__ void k_na_merge(const long long *spawned, long long n, int W, int L, 
                 const long long fl = rec[W + L];
                 atomicAdd(&sc.cnt[owner * 3 + 2], 1u);
                 for (int k = 0; k < L; ++k) {
+                    // a record's initiator bit of a run counts whatever its
+                    // amplitude there (FindResidualParticle)
+                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&sc.cnt[owner * 3 + k], 0x80000000u);
                     const long long q = na_fixed(rec[W + k], &ovf);
                     if (q == 0) continue;
                     atomicAdd((unsigned long long *)&sc.q[owner * 2 + k], (unsigned long long)q);
                     aq[k] += (unsigned long long)(q < 0 ? -q : q);
                     atomicAdd(&sc.cnt[owner * 3 + k], 1u);
-                    if (test_bit(fl, init_flag_bit(k))) atomicOr(&sc.cnt[owner * 3 + k], 0x80000000u);
                 }
             }
         }

@@ -100,11 +100,13 @@ __device__ inline void group_add(Group &g, const long long *rec, int W, int L) {
     ++g.nrec;
     const long long fl = rec[W + L];
     NECI_FOR_RUNS(k, L) {
+        // a record's initiator bit of a run counts whatever its amplitude
+        // there (FindResidualParticle)
+        if (test_bit(fl, init_flag_bit(k))) g.cnt[k] |= 0x80000000u;
         const long long q = rec[W + k];
         if (q == 0) continue;
         g.q[k] = (long long)((unsigned long long)g.q[k] + (unsigned long long)q);  // two's-complement wrap, as the atomics
         g.cnt[k] += 1u;
-        if (test_bit(fl, init_flag_bit(k))) g.cnt[k] |= 0x80000000u;
     }
 }
 

@@ -131,6 +131,38 @@ def test_sort_annihilate_injected(name, trunc):
     assert sg.n_new == sc.n_new and sg.n_occupied == sc.n_occupied
 
 
+@pytest.mark.parametrize("name", ["hub10", "hub10x2", "mol24"])
+@pytest.mark.parametrize("ann", [capi.ANN_HASH, capi.ANN_SORT])
+def test_annihilate_keeps_one_record_flag_words(name, ann):
+    """A new determinant made of one spawn record keeps that record's whole
+    flag word (FindResidualParticle), other flag bits and the other run's
+    initiator bit included, while the initiator abort reads the bits of the
+    runs that carry an amplitude: bit for bit against the oracle."""
+    spec, eng, orc = pair(name, ann)
+    rng = np.random.default_rng(61)
+    W, L = spec.W, spec.lenof_sign
+    walkers = random_walkers(spec, 2000, rng)
+    eng.upload(walkers)
+    orc.upload(walkers)
+    sp = random_spawns(spec, walkers, 15000, rng)
+    extra = rng.random(sp.shape[0]) < 0.5
+    sp[extra, -1] |= np.int64(1) << 5
+    if L == 2:  # the other run's initiator bit on records of one run
+        cross = rng.random(sp.shape[0]) < 0.3
+        sp[cross, -1] |= np.int64(1) << capi.FLAG_INITIATOR[1]
+    p = capi.default_params(seed=7, iter=5, t_trunc_initiator=1, occupied_thresh=1.0)
+    sg = eng.annihilate(p, sp)
+    sc, rc = orc.annihilate(p, sp)
+    assert rc == 0 and sg.err == 0
+    rg = canonical(eng.download()[0], W)
+    rcpu = canonical(orc.download()[0], W)
+    assert rg.shape == rcpu.shape
+    assert np.array_equal(rg[:, :W + L], rcpu[:, :W + L])
+    assert np.array_equal(rg[:, -1] & ~1, rcpu[:, -1] & ~1)
+    assert np.any((rg[:, -1] >> 5) & 1), "no kept flag word carries the extra bit"
+    assert sg.n_new == sc.n_new and sg.n_occupied == sc.n_occupied
+
+
 def default_flags(eng):
     """Hands the context NECI's default flag rules (tTruncInitiator and
     tInitCoherentRule on), which the compression applies: an annihilation of
