@@ -1098,7 +1098,7 @@ __global__ void __launch_bounds__(128) k_ann_place(DevSys s, DevState st, int sp
             NECI_FOR_RUNS(k, L) {
                 const double v = word_to_double(ws[k]);
                 a_tp[k] += fabs(v);
-                a_norm[k] += v * v;
+                a_norm[k] = fma(v, v, a_norm[k]);  // a statistic: one rounding, one FP64 instruction
                 if (is_ref) c->noat_hf[k] = v;
             }
         }
@@ -1258,7 +1258,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
         occ = false;
         NECI_FOR_RUNS(k, L) {
             a_tp[k] += fabs(C[k]);
-            a_norm[k] += C[k] * C[k];
+            a_norm[k] = fma(C[k], C[k], a_norm[k]);  // a statistic: one rounding, one FP64 instruction
             if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
         }
         if (occ || core) {
