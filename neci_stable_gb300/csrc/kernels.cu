@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
             flags = sr[W + L];
             core = st.n_core > 0 && is_core_flags(flags);
             NECI_FOR_RUNS(k, L) {
-                acc_old[k] += fabs(C[k]);
+                acc_old[k] += abs_dbl(C[k]);
                 if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
             }
             if (core) {
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                 if (s.tau_search && !(dbl_bits(kd) >> 63) && dbl_bits(kd) > dbl_bits(death_max)) death_max = kd;
                 if (gt_pos(fac, 2.0)) set_err(c, NECI_GPU_ERR_UNSTABLE);
                 double idie;
-                if (FAST || p.t_all_real_coeff) idie = fac * fabs(C[k]);
+                if (FAST || p.t_all_real_coeff) idie = fac * abs_dbl(C[k]);
                 else idie = death_integer(fac, C[k], dkey, p.iter, k);
                 id[k] = idie;
                 // fmin(idie, |C|) to the died; idie > |C| (more died than
@@ -1173,7 +1173,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
             NECI_FOR_RUNS(k, L) {
                 const double y = st.core_y[(long long)ci * L + k];
                 a_born[k] += fabs(y);
-                if (prod_negative(C[k], y)) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(y));
+                if (prod_negative(C[k], y)) a_ann[k] += 2.0 * min_abs(C[k], y);
                 C[k] = y + C[k];
             }
             changed = true;
@@ -1203,7 +1203,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
                                          (p.t_init_coherent_rule && (m[k] & 0x7FFFFFFFu) >= 2u);
                     if (!sp_init && !core) { a_ab[k] += fabs(S[k]); S[k] = 0.0; }
                 }
-                if (prod_negative(C[k], S[k])) a_ann[k] += 2.0 * fmin(fabs(C[k]), fabs(S[k]));
+                if (prod_negative(C[k], S[k])) a_ann[k] += 2.0 * min_abs(C[k], S[k]);
             }
             NECI_FOR_RUNS(k, L) C[k] = S[k] + C[k];
             changed = true;
@@ -1257,7 +1257,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
         if (changed) NECI_FOR_RUNS(k, L) r[W + k] = double_to_word(C[k]);
         occ = false;
         NECI_FOR_RUNS(k, L) {
-            a_tp[k] += fabs(C[k]);
+            a_tp[k] += abs_dbl(C[k]);
             a_norm[k] = fma(C[k], C[k], a_norm[k]);  // a statistic: one rounding, one FP64 instruction
             if (abs_bits(C[k]) >= dbl_bits(kEps12)) occ = true;
         }
