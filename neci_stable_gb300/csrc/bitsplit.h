@@ -1,7 +1,7 @@
 // bitsplit.h -- threshold tests and the integer/fraction split of a walker
 // sign done on the IEEE-754 bit pattern, for the per-determinant sweeps.
 //
-// GB300 issues FP64 instructions at 1/64 of the FP32 rate, and the sweeps
+// GB300 runs FP64 instructions at about 1/128 of the FP32 rate, and the sweeps
 // over CurrentDets test |C| against thresholds and split |C| into whole and
 // fractional walkers for every determinant.  For finite doubles of equal
 // sign the order of the values is the order of their bit patterns read as

@@ -459,7 +459,8 @@ __device__ inline double from_fixed(long long q) {
 __device__ inline double word_to_double(long long w) { return __longlong_as_double(w); }
 __device__ inline long long double_to_word(double d) { return __double_as_longlong(d); }
 // |x| and -x on the high word, in integer instructions: materialised as FP64
-// operations they would take a slot of GB300's 1/64-rate FP64 pipe each.
+// operations they would take a slot of GB300's FP64 pipe each (about one lane
+// per clock per SM).
 __device__ inline double abs_dbl(double x) { return __hiloint2double(__double2hiint(x) & 0x7FFFFFFF, __double2loint(x)); }
 // fmin(|a|, |b|) for finite a, b, on the bit patterns.
 __device__ inline double min_abs(double a, double b) { return abs_bits(a) < abs_bits(b) ? abs_dbl(a) : abs_dbl(b); }

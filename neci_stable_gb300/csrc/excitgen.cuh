@@ -7,7 +7,7 @@
 // uniform_index(n) (multiply-high), r < p becomes a threshold test; the
 // sampled distributions and the returned p_gen are those of NECI's routines,
 // with the constant divisions of p_gen hoisted out of the attempt.  GB300
-// executes FP64 at 1/64 of the FP32 rate, so the sampling itself carries no
+// executes FP64 at about 1/128 of the FP32 rate, so the sampling itself carries no
 // FP64 arithmetic.
 #pragma once
 

@@ -290,7 +290,8 @@ __device__ __noinline__ double death_integer(double fac, double c, unsigned long
 
 // LR: lenof_sign of the instance (1, or 2 for a replica pair).  FAST: the
 // instance for real coefficients with AvMCExcits = 1 (sweep_fast).  GB300
-// issues FP64 instructions at 1/64 of the FP32 rate and a predicated one
+// runs FP64 instructions at about one lane per clock per SM (1/128 of the
+// FP32 rate) and a predicated one
 // holds the pipe like an executed one, so the FP64 instructions of paths a
 // warp rarely takes sit behind branches (warp votes) or out of line.
 template <int LR, bool FAST>
@@ -900,7 +901,8 @@ __global__ void __launch_bounds__(256) k_ann_compress(DevSys s, DevState st) {
 // initiator abort, stochRoundSpawn, and appends the survivors to a list.
 // k_ann_place gives each survivor a slot (AddNewHashDet), writes its row and
 // hash bucket and computes H_jj - Hii and <D0|H|D_j>, one determinant per
-// thread: the O(nel^2) diagonal sum runs on GB300's 1/64-rate FP64 pipe, and
+// thread: the O(nel^2) diagonal sum runs on GB300's FP64 pipe (about one lane per
+// clock per SM), and
 // spread over the lanes of the decisions it would hold every lane of a warp
 // that had one survivor.
 // ===========================================================================
