@@ -61,13 +61,27 @@ __device__ inline Real sltcnd_1_r(const DevSys &s, const unsigned long long *d, 
         const Real *jr = (sizeof(Real) == 8 ? (const Real *)s.jrow : (const Real *)s.jrow32) + row;
         const Real *jkr = (sizeof(Real) == 8 ? (const Real *)s.jkrow : (const Real *)s.jkrow32) + row;
         const unsigned long long same = beta(src) ? kBetaBits : kAlphaBits;
+        // The occupied k other than src in increasing order, four loads in
+        // flight at a time and added in that order.
         NECI_FOR_WORDS(w, nwords<NW>(s)) {
             unsigned long long x = d[w];
+            if (((src - 1) >> 6) == w) x &= ~(1ull << ((src - 1) & 63));
             while (x) {
-                const int b = __ffsll((long long)x) - 1;
-                const int o = w * 64 + b + 1;
-                x &= x - 1;
-                if (o != src) hel += __ldg(((same >> b) & 1ull) ? &jkr[spat(o)] : &jr[spat(o)]);
+                Real v[4];
+                bool have[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    have[u] = x != 0ull;
+                    v[u] = 0;
+                    if (have[u]) {
+                        const int b = __ffsll((long long)x) - 1;
+                        x &= x - 1;
+                        v[u] = __ldg(((same >> b) & 1ull) ? &jkr[spat(w * 64 + b + 1)] : &jr[spat(w * 64 + b + 1)]);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (have[u]) hel += v[u];
             }
         }
     }
@@ -284,9 +298,11 @@ __device__ inline void gen_pchb_double(const DevSys &s, const unsigned long long
         if (exch) { const int t = spin0; spin0 = spin1; spin1 = t; }
     }
     // sample_AliasTable_t (aliasSampling.F90:310-331): slot and fraction
-    // from the high and low halves of one 64x(abMax) product
+    // from the high and low halves of one 64x(abMax) product.  An empty
+    // table (no allowed ab) is not tested for first: its slots keep
+    // themselves with probability 0, so the draw ends in the pholes test
+    // below with no child, one dependent load fewer on every double.
     const size_t t = (size_t)(ij - 1) * 3 + (type - 1);
-    if (!__ldg(&s.alias_present[t])) { e.pgen = 0; return; }
     const unsigned long long r = rng.next64();
     const unsigned long long n = (unsigned long long)s.abMax;
     const unsigned long long pos0 = __umul64hi(r, n);

@@ -372,10 +372,14 @@ __global__ void k_pchb_pexch(DevSys s, const double *wsum, double *pexch, unsign
     }
 }
 // Integer thresholds of the alias biases and single-precision probabilities.
-__global__ void k_pchb_derived(long long n, const double *bias, const double *prob, unsigned long long *thr, float *prob32,
-                               double *inv, float *inv32) {
+// The slots of an empty table (no allowed ab, `present` 0) keep themselves
+// (threshold ~0) and have probability 0, so a draw from one reads only its
+// own slot and is rejected by the pholes > 1e-10 test: the attempt makes no
+// child, as the present flag's early exit in the reference order does.
+__global__ void k_pchb_derived(long long n, long long ab_max, const uint8_t *present, const double *bias,
+                               const double *prob, unsigned long long *thr, float *prob32, double *inv, float *inv32) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        thr[i] = prob_thresh(bias[i]);
+        thr[i] = present[i / ab_max] ? prob_thresh(bias[i]) : ~0ull;
         prob32[i] = (float)prob[i];
         const double v = 1.0 / prob[i];
         inv[i] = v;
@@ -473,7 +477,8 @@ int launch_pchb_build(Engine &e) {
                                                (unsigned long long *)e.sys.pexch_thr, (float *)e.sys.pexch32,
                                                (double *)e.sys.pexch_inv, (double *)e.sys.pnoexch_inv,
                                                (float *)e.sys.pexch_inv32, (float *)e.sys.pnoexch_inv32);
-    k_pchb_derived<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, e.sys.alias_bias, e.sys.alias_prob,
+    k_pchb_derived<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, n, e.sys.alias_present, e.sys.alias_bias,
+                                                 e.sys.alias_prob,
                                                  (unsigned long long *)e.sys.alias_thr, (float *)e.sys.alias_prob32,
                                                  (double *)e.sys.alias_inv, (float *)e.sys.alias_inv32);
     k_alias_rec<<<gsz(e), 256, 0, e.stream>>>((long long)ntab * n, n, e.sys.alias_thr, e.sys.alias_prob,
