@@ -84,11 +84,12 @@ def _fcidump64():
 # The configurations: the spec, target walkers, semistochastic core size,
 # and the buffer sizes as multiples of the walker number (slots, spawn records).
 WORKLOADS = {
-    "n24": dict(spec=workload_spec, walkers=TARGET_WALKERS, core=0, slots=3.0, spawns=4.0,
+    "n24": dict(spec=workload_spec, walkers=TARGET_WALKERS, core=0, slots=3.0, spawns=4.0, rescale=True,
+                energy_steps=400,
                 desc="synthetic FCIDUMP n=24 orbitals (48 spin orbitals), 10 electrons, Sz=0, PCHB, initiator "
                      "FCIQMC, real coefficients"),
     "ring10": dict(spec=_ring10, walkers=1e4, core=0, slots=10.0, spawns=100.0, start="single_part", sft_damp=0.1,
-                   tau=0.01,
+                   tau=0.01, energy_steps=400,
                    desc="1D Hubbard ring, 10 sites, 10 electrons, Sz=0, periodic, t=1, U=4, real-space, "
                         "uniform generator"),
     "hub6x6": dict(spec=_square6x6, walkers=1e8, core=10_000, slots=2.0, spawns=2.0, start="single_part",
@@ -260,6 +261,9 @@ def run_gpu(args, rank, world):
     # the target (its overshoot fits the buffers sized for the target) and the
     # list is then scaled to the target: every sign times the same factor, so
     # the shape and the shift carry over (a restart from a rescaled POPSFILE).
+    # With rescale, the population is equilibrated at the target and scaled
+    # back to it afterwards: once the shift varies it holds the population
+    # wherever the growth stopped, which is not the target.
     scale = wl.get("scale_up", 1.0)
     target = args.walkers / scale
     # the conventional tau search runs on the device over the first half of
@@ -280,7 +284,7 @@ def run_gpu(args, rank, world):
         drv.diag_sft = [0.0] * eng.L
     equil = drv.run(args.equil)  # untimed equilibration of the walker distribution
     scale_info = None
-    if scale > 1.0:
+    if scale > 1.0 or wl.get("rescale"):
         st0 = eng.iterate_n(drv.params(), 1)[0]
         drv.iter += 1
         rows, dh, odh = eng.download(max_rows=int(st0.tot_walkers) + 1)
@@ -357,17 +361,40 @@ def run_gpu(args, rank, world):
             p.iter += 1
             e2e_updates += st.tot_parts_old[0]
         e2e_s = time.perf_counter() - t0
+    # ---- energy window (untimed): further cycles of StepsSft steps of each
+    # precision, interleaved on the same population with the shift updated
+    # after every cycle, so that E_proj of the two precisions has error bars
+    # from many blocks
+    drv.iter = p.iter
+    old = st.tot_parts[0]  # the growth of the first cycle is taken from the last e2e step
+    en = {capi.PREC_FP64: list(stats), capi.PREC_MIXED: list(mstats)}
+    n_energy = args.energy_steps if args.energy_steps is not None else wl.get("energy_steps", 60)
+    while len(en[capi.PREC_MIXED]) < args.steps + n_energy:
+        for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+            pc = drv.params()
+            pc.precision = prec
+            sts = eng.iterate_n(pc, drv.calc.steps_sft)
+            drv.iter += drv.calc.steps_sft
+            en[prec].extend(sts)
+            parts = sts[-1].tot_parts[0]
+            drv.diag_sft[0] -= math.log(parts / old) * drv.calc.sft_damp / (drv.calc.tau * drv.calc.steps_sft)
+            old = parts
+    p = drv.params()
     updates = sum(s.tot_parts_old[0] for s in stats)
     bb_updates = sum(s.tot_parts_old[0] for s in bb_stats)
     mixed_updates = sum(s.tot_parts_old[0] for s in mstats)
-    # E_proj of the FP64 and of the mixed-precision steps (blocks of 10 steps)
+    # E_proj of the FP64 and of the mixed-precision steps of the timed region
+    # and the energy window (blocks of 10 steps, reblocked)
     from neci_stable_gb300 import analysis
     proje = {}
-    for name, sts in (("fp64", stats), ("mixed", mstats)):
+    for name, sts in (("fp64", en[capi.PREC_FP64]), ("mixed", en[capi.PREC_MIXED])):
         num = np.array([sum(x.enum_cyc[0] for x in sts[k:k + 10]) for k in range(0, len(sts), 10)])
         den = np.array([sum(x.hf_cyc[0] for x in sts[k:k + 10]) for k in range(0, len(sts), 10)])
         e, err = analysis.projected_energy(num, den, eng.hii) if len(num) >= 2 else (float(num.sum() / den.sum()) + eng.hii, None)
-        proje[name] = {"e_proj": e, "err": err}
+        proje[name] = {"e_proj": e, "err": err, "steps": len(sts)}
+    if proje["fp64"]["err"] and proje["mixed"]["err"]:
+        d = proje["mixed"]["e_proj"] - proje["fp64"]["e_proj"]
+        proje["mixed_minus_fp64"] = {"ha": d, "sigma": abs(d) / math.hypot(proje["fp64"]["err"], proje["mixed"]["err"])}
     # ---- per-kernel timing passes (events around each kernel; not the timed
     # number): FP64, then the mixed-precision step
     def profile(prec, n=3):
@@ -666,6 +693,8 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--equil", type=int, default=600, help="untimed equilibration iterations")
+    ap.add_argument("--energy-steps", type=int, default=None,
+                    help="untimed steps of each precision after the timed region for E_proj (default: the workload's)")
     ap.add_argument("--walkers", type=float, default=None, help="target walker number (default: the workload's)")
     ap.add_argument("--workload", default="n24", choices=sorted(WORKLOADS),
                     help="n24: the headline configuration; ring10, hub6x6, n64: the other single-GPU configurations")
@@ -737,7 +766,7 @@ def main():
     ann = tuple(k for k in ("ann_probe", "ann_compress", "ann_insert") if k in kt)
     ann_ms = sum(kt[k][0] / kt[k][1] for k in ann)
     ann_bytes = sum(algorithmic_bytes(k, r["last"], W, L) for k in ann)
-    # the sort form of the annihilation: per stage (keys, the 4 radix passes,
+    # the sort form of the annihilation: per stage (keys, the 3 radix passes,
     # grouping + walker-hash lookup) and the insertion of new determinants
     kts = {k: v for k, v in r["ktimes_sort"].items() if v[1] > 0}
     sort_stages = {}
@@ -793,8 +822,8 @@ def main():
             "ms_per_step": r["sort_ms"] / args.steps,
             "stages": sort_stages, "ms_per_step_annihilation": sort_ms,
             "annihilation_frac": sort_bytes / (sort_ms / 1e3) / 1e9 / hbm if sort_ms > 0 else None,
-            "note": "NECI_ANN_SORT on the same population: spawns radix-sorted by a 32-bit key of their "
-                    "determinant's hash and reduced as runs; the hash form is the default"},
+            "note": "NECI_ANN_SORT on the same population: spawns radix-sorted (three 8-bit passes) by a "
+                    "24-bit key of their determinant's hash and reduced as runs; the hash form is the default"},
         "proje": r["proje"],
         "mixed_precision": {"value": r["mixed_updates"] / (r["mixed_ms"] / 1000.0), "unit": UNIT,
                             "ms_per_step": r["mixed_ms"] / args.steps,

@@ -314,6 +314,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.slot_bucket, (size_t)st.max_walkers);
     A(st.free_list, (size_t)st.max_walkers + 1);
     A(st.hole_mark, (size_t)st.max_walkers + kStagePad);
+    A(st.dkey, (size_t)st.max_walkers);
     A(st.spawn, (size_t)st.max_spawned * s.R);
     A(st.att, (size_t)st.max_att);
     A(st.big, (size_t)st.max_big * 3);

@@ -184,6 +184,7 @@ struct DevState {
     unsigned long long hash_n;     // buckets (power of two)
     uint32_t *slot_bucket;         // bucket holding each slot
     uint8_t *hole_mark;            // 1: the slot went to this step's free list (k_sweep)
+    unsigned long long *dkey;      // det_key of each slot with spawn attempts this step (k_sweep)
     int32_t *free_list;
     long long max_walkers, max_spawned, max_att;
     long long *spawn;              // spawn records

@@ -410,6 +410,9 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
             if (__any_sync(__activemask(), is_ref))
                 if (is_ref) NECI_FOR_RUNS(k, L) acc_hf[k] += C[k];
             const unsigned long long dkey = det_key(d, W, p.seed);
+            // the key of the spawn attempts' streams, read by k_spawn for
+            // every attempt of this slot instead of hashing the row again
+            st.dkey[j] = dkey;
             NECI_FOR_RUNS(k, L) {
                 // decide_num_to_spawn (fcimc_helper.F90:2160-2174)
                 uint32_t whole;

@@ -355,7 +355,7 @@ void launch_sort_keys(Engine &e, cudaStream_t s) {
     else k_sk_keys<1><<<sk_grid(e, 8), 256, shm, s>>>(e.sys, e.st);
 }
 
-// The four radix passes; returns the buffer index that holds the sorted pairs.
+// The three radix passes; returns the buffer index that holds the sorted pairs.
 int launch_sort_radix(Engine &e, cudaStream_t s) {
     uint32_t *const key[2] = {e.st.sk_key[0], e.st.sk_key[1]};
     uint32_t *const val[2] = {e.st.sk_val[0], e.st.sk_val[1]};

@@ -90,7 +90,16 @@ __device__ inline void load_parent(const DevSys &s, const DevState &st, const It
     const long long flags = r[rwords<RW>(s) + s.L];
     P.core = st.n_core > 0 && is_core_flags(flags);
     P.pinit = p.t_trunc_initiator && test_bit(flags, init_flag_bit(P.run));
-    P.key = det_key(P.d, rwords<RW>(s), p.seed, nwords<NW>(s));
+    // det_key of the row (the words past NW are zero), which the sweep
+    // stored for every slot with attempts
+    P.key = st.dkey[j];
+}
+
+// The stream of an attempt from its entry alone: what the classification of
+// an attempt (single or double) needs, without the parent's row.
+__device__ inline Stream attempt_stream(const DevState &st, const IterParams &p, unsigned long long w0) {
+    const long long j = (long long)(w0 & 0xFFFFFFFFull);
+    return Stream(st.dkey[j], p.iter, P_ATTEMPT, (uint32_t)((w0 >> 32) & 1ull), (uint32_t)(w0 >> 34));
 }
 
 // Block-local tau-search log of k_spawn: per TauClass the largest gamma (as
@@ -404,16 +413,12 @@ __global__ void __launch_bounds__(128, NECI_SPAWN_BLOCKS_PER_SM)
             const bool valid = more && q < nat;
             int cls = 0;
             unsigned long long w0 = 0, r1 = 0;
-            {
-                Parent P;
-                if (valid) {
-                    w0 = st.att[q];
-                    load_parent<NW, RW>(s, st, p, w0, P);
-                    Stream rng(P.key, p.iter, P_ATTEMPT, P.run, P.k);
-                    const unsigned long long r0 = rng.next64();
-                    r1 = rng.next64();
-                    cls = (GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles) ? 1 : 0;
-                }
+            if (valid) {
+                w0 = st.att[q];
+                Stream rng = attempt_stream(st, p, w0);
+                const unsigned long long r0 = rng.next64();
+                r1 = rng.next64();
+                cls = (GEN == NECI_EXGEN_UNIFORM ? !(r0 < s.thr_doubles) : r0 < s.thr_singles) ? 1 : 0;
             }
             const bool queued = valid;
             unsigned int m[2];
