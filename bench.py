@@ -295,7 +295,12 @@ def run_gpu(args, rank, world):
         eng.upload(rows, dh, odh)
         scale_info = {"equilibrated_walkers": st0.tot_parts[0], "factor": factor}
         drv.calc.target_walkers = args.walkers
-        drv.run(100)  # re-equilibration at the target population
+        # re-equilibration at the target population, with the shift damped
+        # strongly enough to stop the population's drift within it
+        damp = drv.calc.sft_damp
+        drv.calc.sft_damp = max(damp, 0.3)
+        drv.run(100)
+        drv.calc.sft_damp = damp
     tau = drv.calc.tau
     tau_info = {"start": tau0, "final": tau, "cycles_searched": len(equil.tau)}
     core_info = None
