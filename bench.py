@@ -48,11 +48,11 @@ BLOOM = 3.0
 # roofline.traffic: kernel -> (bytes per unit, step count that is the unit).
 # The spawn kernel is bound by instruction issue, not by HBM: its issue
 # figures from the same capture are reported beside its HBM roofline.
-NCU_SPAWN_ISSUE = {"issue_active": 0.605, "alu_pipe": 0.544, "fp64_pipe": 0.326, "warps_active": 0.436,
-                   "lanes_per_instruction": 24.4, "dram_bytes_per_attempt": 14.0}
+NCU_SPAWN_ISSUE = {"issue_active": 0.586, "alu_pipe": 0.541, "fp64_pipe": 0.372, "warps_active": 0.451,
+                   "lanes_per_instruction": 25.2, "dram_bytes_per_attempt": 15.8}
 
 NCU_DRAM_BYTES_PER_UNIT = {
-    "spawn": (14.0, "n_attempts"),
+    "spawn": (15.8, "n_attempts"),
     "sweep": (47.2, "tot_walkers"),
     "merge_stats": (38.3, "tot_walkers"),
     "ann_probe": (102.3, "n_spawned"),
