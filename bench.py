@@ -185,9 +185,9 @@ def algorithmic_bytes(kernel, st, W, L, nnz=0, fused=True):
     N = st["n_new"]
     slots = st["tot_walkers"]
     if kernel == "sweep":
-        # rows and diagonal data read, signs written, and each slot's
-        # free-list mark (1 B)
-        return slots * (R + G + 1) + D * 8 * L + D * 16
+        # rows and diagonal data read, signs written, each slot's free-list
+        # mark (1 B), and each occupied slot's stream key (8 B)
+        return slots * (R + G + 1) + D * 8 * L + D * 16 + D * 8
     if kernel == "spawn":
         # the 8 B attempt entries read (parent rows and tables are gathered
         # from L2); fused: per spawn a hash bucket and the row's det words
