@@ -296,7 +296,9 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     st.max_walkers = sys->max_walkers;
     st.max_spawned = sys->max_spawned;
     st.max_att = 2 * sys->max_spawned + 1024;
-    st.max_big = st.max_att / kBigAttempts + 1024;
+    // a parent with n attempts (kBigAttempts < n <= kHugeAttempts) takes
+    // ceil(n / kExpandChunk) entries, at most n / kBigAttempts + n / kExpandChunk
+    st.max_big = st.max_att / kBigAttempts + st.max_att / kExpandChunk + 1024;
     st.hash_n = next_pow2(std::max<unsigned long long>((unsigned long long)sys->n_walker_hashes,
                                                        2ull * (unsigned long long)sys->max_walkers));
     st.spawn_hash_n = next_pow2(2ull * (unsigned long long)sys->max_spawned);

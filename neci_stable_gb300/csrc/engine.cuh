@@ -26,6 +26,7 @@ constexpr int kMaxNel = 64;
 constexpr int kMaxNeigh = 8;
 constexpr int kBigAttempts = 32;  // parents with more attempts are expanded by k_expand
 constexpr int kHugeAttempts = 1 << 16;  // ... and with more than this by the whole grid
+constexpr int kExpandChunk = 512;  // k_expand's work item: at most this many attempts of one parent
 constexpr int kMaxHuge = 4096;
 constexpr int kCompactTile = 1024;        // slots per block of the compaction scans
 constexpr int kProbeLimit = 1 << 16;
@@ -189,7 +190,8 @@ struct DevState {
     long long max_walkers, max_spawned, max_att;
     long long *spawn;              // spawn records
     unsigned long long *att;       // attempts: slot | run << 32 | neg << 33 | attempt << 34
-    unsigned long long *big;       // triples: slot | run << 32 | neg << 33, attempts, first entry
+    unsigned long long *big;       // chunks of at most kExpandChunk attempts of one parent, as triples:
+                                   // slot | run << 32 | neg << 33 | first attempt << 34, attempts, first entry
     unsigned long long *huge;      // the same for parents with more than kHugeAttempts attempts
     long long max_big;
     long long *acc;                // per slot*L fixed-point spawn sums (found determinants)

@@ -546,13 +546,18 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                                 set_err(c, NECI_GPU_ERR_SPAWN_FULL);
                             }
                         } else if (nsp[k] > (unsigned int)kBigAttempts) {
-                            const unsigned long long b = atomicAdd(&c->n_big, 1ull);
-                            if (b < (unsigned long long)st.max_big) {
-                                st.big[3 * b] = head;
-                                st.big[3 * b + 1] = nsp[k];
-                                st.big[3 * b + 2] = q;
-                            } else {
-                                set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+                            // in chunks of kExpandChunk attempts, so that one
+                            // heavy parent does not hold one warp of k_expand
+                            const unsigned int nch = (nsp[k] + kExpandChunk - 1) / kExpandChunk;
+                            // (every entry below max_big is written, so that
+                            // k_expand reads none from an earlier step)
+                            const unsigned long long b = atomicAdd(&c->n_big, (unsigned long long)nch);
+                            if (b + nch > (unsigned long long)st.max_big) set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+                            for (unsigned int ch = 0; ch < nch && b + ch < (unsigned long long)st.max_big; ++ch) {
+                                const unsigned int a0 = ch * kExpandChunk;
+                                st.big[3 * (b + ch)] = head | ((unsigned long long)a0 << 34);
+                                st.big[3 * (b + ch) + 1] = min((unsigned int)kExpandChunk, nsp[k] - a0);
+                                st.big[3 * (b + ch) + 2] = q + a0;
                             }
                         } else {
                             for (unsigned int a = 0; a < nsp[k]; ++a) st.att[q + a] = head | ((unsigned long long)a << 34);
@@ -586,8 +591,9 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
 }
 
 // ===========================================================================
-// k_expand: attempt entries of heavily populated parents, one warp per parent
-// (the whole grid for the few with more than kHugeAttempts).
+// k_expand: attempt entries of heavily populated parents, one warp per chunk
+// of at most kExpandChunk attempts of a parent (the whole grid per parent for
+// the few with more than kHugeAttempts).
 // ===========================================================================
 __global__ void k_expand(DevState st) {
     if (halted(st)) return;
@@ -599,7 +605,8 @@ __global__ void k_expand(DevState st) {
              a += (unsigned long long)gridDim.x * blockDim.x)
             st.att[base + a] = head | (a << 34);
     }
-    // the others (33 to 65536 attempts, mostly a few hundred): a warp per parent
+    // the others (33 to 65536 attempts): a warp per chunk; the chunk's head
+    // carries its first attempt index, so its entry a is head + (a << 34)
     const unsigned long long nb = min(st.ctl->n_big, (unsigned long long)st.max_big);
     const unsigned long long warp = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5;
     const unsigned long long nwarps = ((unsigned long long)gridDim.x * blockDim.x) >> 5;
@@ -608,7 +615,7 @@ __global__ void k_expand(DevState st) {
         const unsigned long long head = st.big[3 * b];
         const unsigned long long n = st.big[3 * b + 1];
         const unsigned long long base = st.big[3 * b + 2];
-        for (unsigned long long a = lane; a < n; a += 32) st.att[base + a] = head | (a << 34);
+        for (unsigned long long a = lane; a < n; a += 32) st.att[base + a] = head + (a << 34);
     }
 }
 
