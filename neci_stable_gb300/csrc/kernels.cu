@@ -314,8 +314,8 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
     __shared__ int stage_ok;
     // the round's appends: per-warp counts of free slots and attempts, and
     // the block's first positions
-    __shared__ unsigned int s_wfree[kStageTile / 32], s_watt[kStageTile / 32];
-    __shared__ unsigned long long s_base_free, s_base_att;
+    __shared__ unsigned int s_wfree[kStageTile / 32], s_watt[kStageTile / 32], s_wbig[kStageTile / 32];
+    __shared__ unsigned long long s_base_free, s_base_att, s_base_big;
     const size_t stage_bytes = (size_t)kStageTile * (R + 2) * 8;
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
@@ -487,47 +487,82 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
         }
         // the signs just written are all zero
         const bool freed = live && occ && !core && out_zero;
-        // The round's two appends, free slots and spawn-attempt entries, with
-        // one atomic per counter for the whole block (both issued before
-        // either result is read): per-warp atomics on these two addresses
-        // serialise in one L2 slice, tens of thousands to millions per step.
-        // One entry per attempt; a parent with more than kBigAttempts attempts
-        // is handed to k_expand, which writes its entries with a whole block.
+        // The round's three appends, free slots, spawn-attempt entries and
+        // k_expand's chunks, with one atomic per counter for the whole block
+        // (all issued before any result is read): per-warp atomics on these
+        // addresses serialise in one L2 slice, tens of thousands to millions
+        // per step.  One entry per attempt; a parent with more than
+        // kBigAttempts attempts is handed to k_expand in chunks of at most
+        // kExpandChunk attempts, each written by a warp there.
         {
             const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
             const bool want = hole || freed;
             if (live) st.hole_mark[j] = want ? 1 : 0;
             const unsigned int mf = __ballot_sync(0xffffffffu, want);
-            unsigned int nat = 0;
-            NECI_FOR_RUNS(k, L) nat += nsp[k];
-            unsigned int incl = nat;  // inclusive scan of the warp's attempts
+            unsigned int nat = 0, nbig = 0;
+            NECI_FOR_RUNS(k, L) {
+                nat += nsp[k];
+                if (nsp[k] > (unsigned int)kBigAttempts && nsp[k] <= (unsigned int)kHugeAttempts)
+                    nbig += (nsp[k] + kExpandChunk - 1) / kExpandChunk;
+            }
+            unsigned int incl = nat, bincl = nbig;  // inclusive scans of the warp's attempts and chunks
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const unsigned int y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= o) incl += y;
+                const unsigned int z = __shfl_up_sync(0xffffffffu, bincl, o);
+                if (lane >= o) {
+                    incl += y;
+                    bincl += z;
+                }
             }
             if (lane == 31) {
                 s_wfree[wid] = __popc(mf);
                 s_watt[wid] = incl;
+                s_wbig[wid] = bincl;
             }
             __syncthreads();
             if (threadIdx.x == 0) {
-                unsigned int tf = 0, ta = 0;
+                unsigned int tf = 0, ta = 0, tb = 0;
                 for (int w = 0; w < kStageTile / 32; ++w) {
                     tf += s_wfree[w];
                     ta += s_watt[w];
+                    tb += s_wbig[w];
                 }
                 s_base_free = tf ? atomicAdd(&c->n_free, (unsigned long long)tf) : 0ull;
                 s_base_att = ta ? atomicAdd(&c->n_att, (unsigned long long)ta) : 0ull;
+                s_base_big = tb ? atomicAdd(&c->n_big, (unsigned long long)tb) : 0ull;
             }
             __syncthreads();
-            unsigned long long bf = s_base_free, ba = s_base_att;
+            unsigned long long bf = s_base_free, ba = s_base_att, bb = s_base_big;
             for (int w = 0; w < wid; ++w) {
                 bf += s_wfree[w];
                 ba += s_watt[w];
+                bb += s_wbig[w];
             }
             if (want) st.free_list[bf + __popc(mf & ((1u << lane) - 1u))] = (int32_t)j;
             const unsigned long long base = ba + incl - nat;
+            // this lane's chunks for k_expand: every entry below max_big is
+            // written (with no attempts where the lane's entries do not fit),
+            // so that k_expand reads none from an earlier step
+            if (nbig) {
+                unsigned long long cb = bb + bincl - nbig;
+                const bool fits = base + nat <= (unsigned long long)st.max_att;
+                if (cb + nbig > (unsigned long long)st.max_big) set_err(c, NECI_GPU_ERR_SPAWN_FULL);
+                unsigned long long q = base;
+                NECI_FOR_RUNS(k, L) {
+                    if (nsp[k] > (unsigned int)kBigAttempts && nsp[k] <= (unsigned int)kHugeAttempts) {
+                        const unsigned long long head = (unsigned long long)j | ((unsigned long long)k << 32) |
+                                                        ((unsigned long long)neg[k] << 33);
+                        for (unsigned int a0 = 0; a0 < nsp[k] && cb < (unsigned long long)st.max_big;
+                             a0 += kExpandChunk, ++cb) {
+                            st.big[3 * cb] = head | ((unsigned long long)a0 << 34);
+                            st.big[3 * cb + 1] = fits ? min((unsigned int)kExpandChunk, nsp[k] - a0) : 0u;
+                            st.big[3 * cb + 2] = q + a0;
+                        }
+                    }
+                    q += nsp[k];
+                }
+            }
             if (nat) {
                 if (base + nat > (unsigned long long)st.max_att) {
                     set_err(c, NECI_GPU_ERR_SPAWN_FULL);
@@ -546,19 +581,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                                 set_err(c, NECI_GPU_ERR_SPAWN_FULL);
                             }
                         } else if (nsp[k] > (unsigned int)kBigAttempts) {
-                            // in chunks of kExpandChunk attempts, so that one
-                            // heavy parent does not hold one warp of k_expand
-                            const unsigned int nch = (nsp[k] + kExpandChunk - 1) / kExpandChunk;
-                            // (every entry below max_big is written, so that
-                            // k_expand reads none from an earlier step)
-                            const unsigned long long b = atomicAdd(&c->n_big, (unsigned long long)nch);
-                            if (b + nch > (unsigned long long)st.max_big) set_err(c, NECI_GPU_ERR_SPAWN_FULL);
-                            for (unsigned int ch = 0; ch < nch && b + ch < (unsigned long long)st.max_big; ++ch) {
-                                const unsigned int a0 = ch * kExpandChunk;
-                                st.big[3 * (b + ch)] = head | ((unsigned long long)a0 << 34);
-                                st.big[3 * (b + ch) + 1] = min((unsigned int)kExpandChunk, nsp[k] - a0);
-                                st.big[3 * (b + ch) + 2] = q + a0;
-                            }
+                            // its chunks for k_expand are written above
                         } else {
                             for (unsigned int a = 0; a < nsp[k]; ++a) st.att[q + a] = head | ((unsigned long long)a << 34);
                         }
