@@ -318,6 +318,20 @@ def test_parent_with_more_than_65536_attempts(ann):
     assert st.n_attempts > 65536
 
 
+# ------------------------------------- parents expanded in several chunks
+@pytest.mark.parametrize("name,pop", [("mol12", 3000.0), ("hub10x2", 2000.0)])
+def test_parents_in_several_expansion_chunks(name, pop):
+    """A parent of a few thousand attempts is handed to the expansion kernel in
+    chunks of 512 (each a warp's work, the chunk's head carrying its first
+    attempt index); with a replica pair both runs' chunks follow each other.
+    The steps stay bit-exact, so every chunk wrote its entries."""
+    spec, eng, orc = pair(name)
+    eng.start_from_reference(initial_part=pop)
+    orc.upload(eng.download()[0])
+    st = step_both(spec, eng, orc, 4, 0.01, seed=83)
+    assert st.n_attempts > 1024
+
+
 # ---------------------------------------------------------- 1e5 walkers
 @pytest.mark.parametrize("name,tau,grow,p_singles", [("mol24", 0.02, 6, 0.5), ("hub6x6", 0.002, 4, None)])
 @pytest.mark.parametrize("ann", [capi.ANN_HASH, capi.ANN_SORT])
