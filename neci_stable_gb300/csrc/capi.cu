@@ -315,7 +315,7 @@ int32_t neci_gpu_init(neci_gpu_ctx **out, const neci_gpu_system *sys, int32_t de
     A(st.hash, (size_t)st.hash_n);
     A(st.slot_bucket, (size_t)st.max_walkers);
     A(st.free_list, (size_t)st.max_walkers + 1);
-    A(st.hole_mark, (size_t)st.max_walkers + kStagePad);
+    A(st.hole_mark, (size_t)st.max_walkers + 16);  // the merge sweep stages it in multiples of 16 slots
     A(st.dkey, (size_t)st.max_walkers);
     A(st.spawn, (size_t)st.max_spawned * s.R);
     A(st.att, (size_t)st.max_att);

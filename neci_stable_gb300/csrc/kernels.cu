@@ -1170,11 +1170,13 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
     unsigned long long a_s[2] = {0, 0}, a_occ = 0, a_holes = 0, a_found = 0, a_tomb = 0;
     // Tiles staged into shared memory by TMA bulk copies as in k_sweep: the
     // rows, the per-slot spawn counts (meta) and the per-slot spawn sums
-    // (acc) of the tile, so that no global load waits in a slot's path.
+    // (acc) of the tile, and in a step (split) the sweep's free-list marks,
+    // so that no global load waits in a slot's path.
     extern __shared__ __align__(16) unsigned char merge_smem[];
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int stage_ok;
-    const size_t stage_bytes = (size_t)kStageTile * (R * 8 + L * 4 + L * 8);
+    // rows, meta, acc and (split) the free-list marks of a tile
+    const size_t stage_bytes = (size_t)kStageTile * (R * 8 + L * 4 + L * 8 + 1);
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
@@ -1188,11 +1190,15 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
         if (rows == 0) return;
         unsigned char *base = merge_smem + (k & 1) * stage_bytes;
         const uint32_t br = (uint32_t)rows * R * 8, bm = (uint32_t)rows * L * 4, ba = (uint32_t)rows * L * 8;
+        // the one-byte marks move in multiples of 16 slots (the array is
+        // allocated 16 slots longer)
+        const uint32_t bh = split ? (uint32_t)((rows + 15) & ~15) : 0u;
         fence_proxy_async_smem();
-        mbar_expect_tx(&bars[k & 1], br + bm + ba);
+        mbar_expect_tx(&bars[k & 1], br + bm + ba + bh);
         bulk_g2s(base, st.dets + tile * kStageTile * R, br, &bars[k & 1]);
         bulk_g2s(base + (size_t)kStageTile * R * 8, st.meta + tile * kStageTile * L, bm, &bars[k & 1]);
         bulk_g2s(base + (size_t)kStageTile * (R * 8 + L * 4), st.acc + tile * kStageTile * L, ba, &bars[k & 1]);
+        if (bh) bulk_g2s(base + (size_t)kStageTile * (R * 8 + L * 12), st.hole_mark + tile * kStageTile, bh, &bars[k & 1]);
     };
     // one slot: its row (global, for writes), staged row, meta and acc
     auto body = [&](long long j, const long long *sr, const uint32_t *sm, const long long *sa) {
@@ -1324,7 +1330,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
             }
         }
         const long long j = tile * kStageTile + threadIdx.x;
-        if (j < n && !(split && st.hole_mark[j]))
+        if (j < n && !(split && sbase[(size_t)kStageTile * (R * 8 + L * 12) + threadIdx.x]))
             body(j, (const long long *)sbase + (size_t)threadIdx.x * R,
                  (const uint32_t *)(sbase + (size_t)kStageTile * R * 8) + (size_t)threadIdx.x * L,
                  (const long long *)(sbase + (size_t)kStageTile * (R * 8 + L * 4)) + (size_t)threadIdx.x * L);
@@ -1594,7 +1600,7 @@ void launch_rehash(Engine &e, cudaStream_t s) {
 
 // Dynamic shared memory of the staged sweeps: two stages of a tile.
 static size_t sweep_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R + 2) * 8; }
-static size_t merge_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R * 8 + e.sys.L * 12); }
+static size_t merge_smem_bytes(const Engine &e) { return 2ull * kStageTile * (e.sys.R * 8 + e.sys.L * 12 + 1); }
 
 int configure_kernels(Engine &e) {
     // The stages and the block reductions' shared arrays pass the default
@@ -1603,7 +1609,7 @@ int configure_kernels(Engine &e) {
     // (kMaxWords det words, two signs, a flag word), never lowered.
     const int rmax = kMaxWords + 2 + 1;
     const int sweep_max = 2 * kStageTile * (rmax + 2) * 8;
-    const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 12);
+    const int merge_max = 2 * kStageTile * (rmax * 8 + 2 * 12 + 1);
     if (cudaFuncSetAttribute(k_sweep<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
         cudaFuncSetAttribute(k_sweep<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
         cudaFuncSetAttribute(k_sweep<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sweep_max) != cudaSuccess ||
