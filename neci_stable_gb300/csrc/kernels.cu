@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
     // processed: rows, diagH and offdiagH of the tile.  Writes go to global.
     extern __shared__ __align__(16) unsigned char sweep_smem[];
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int stage_ok;
+    __shared__ int stage_ok[2];  // by round parity
     // the round's appends: per-warp counts of free slots and attempts, and
     // the block's first positions
     __shared__ unsigned int s_wfree[kStageTile / 32], s_watt[kStageTile / 32], s_wbig[kStageTile / 32];
@@ -336,26 +336,30 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
         bulk_g2s(base + (size_t)kStageTile * R * 8, st.diagH + tile * kStageTile, bd, &bars[k & 1]);
         bulk_g2s(base + (size_t)kStageTile * (R + 1) * 8, st.offdiagH + tile * kStageTile, bd, &bars[k & 1]);
     };
+    // Round kr: wait for tile kr, one barrier, then the copy of tile kr + 1
+    // into the other buffer: every thread has passed the barrier, so none is
+    // still in round kr - 1, the buffer's last reader.  The barrier also
+    // keeps the appends' per-warp counts of round kr - 1 until all have read
+    // them, so a round needs no barrier at its end.
     if (threadIdx.x == 0 && nrounds > 0) issue(0);
     for (long long kr = 0; kr < nrounds; ++kr) {
         const long long tile = blockIdx.x + kr * gridDim.x;
         const unsigned char *sbase = sweep_smem + (kr & 1) * stage_bytes;
-        if (threadIdx.x == 0 && kr + 1 < nrounds) issue(kr + 1);
-        if (stage_rows(tile, n) > 0) {
-            if (threadIdx.x == 0) stage_ok = mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1)) ? 1 : 0;
-            __syncthreads();
-            if (!stage_ok) {
-                // a copy that never completed: report it, give the copies in
-                // flight a last bounded wait, and leave
-                if (threadIdx.x == 0) {
-                    set_err(c, NECI_GPU_ERR_TIMEOUT);
-                    (void)mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1));
-                    if (kr + 1 < nrounds) (void)mbar_wait_bounded(&bars[(kr + 1) & 1], (uint32_t)(((kr + 1) >> 1) & 1));
-                }
-                __syncthreads();
-                return;
+        if (threadIdx.x == 0)
+            stage_ok[kr & 1] =
+                stage_rows(tile, n) > 0 ? (mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1)) ? 1 : 0) : 1;
+        __syncthreads();
+        if (!stage_ok[kr & 1]) {
+            // a copy that never completed: report it, give it a last
+            // bounded wait (it is the only one in flight), and leave
+            if (threadIdx.x == 0) {
+                set_err(c, NECI_GPU_ERR_TIMEOUT);
+                (void)mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1));
             }
+            __syncthreads();
+            return;
         }
+        if (threadIdx.x == 0 && kr + 1 < nrounds) issue(kr + 1);
         const long long j = tile * kStageTile + threadIdx.x;
         bool live = j < n;
         long long *r = st.dets + (live ? j : 0) * R;  // the global row (writes)
@@ -590,7 +594,6 @@ __global__ void __launch_bounds__(256, 4) k_sweep(DevSys s, DevState st, const I
                 }
             }
         }
-        __syncthreads();  // this round's stage is refilled two rounds on
     }
     const double v[12] = {acc_old[0], acc_old[1], acc_hf[0], acc_hf[1], acc_en[0], acc_en[1], acc_died[0],
                           acc_died[1], acc_born[0], acc_born[1], acc_ab[0], acc_ab[1]};
@@ -1174,7 +1177,7 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
     // so that no global load waits in a slot's path.
     extern __shared__ __align__(16) unsigned char merge_smem[];
     __shared__ __align__(8) uint64_t bars[2];
-    __shared__ int stage_ok;
+    __shared__ int stage_ok[2];  // by round parity
     // rows, meta, acc and (split) the free-list marks of a tile
     const size_t stage_bytes = (size_t)kStageTile * (R * 8 + L * 4 + L * 8 + 1);
     if (threadIdx.x == 0) {
@@ -1311,30 +1314,30 @@ __global__ void __launch_bounds__(256, 4) k_merge_stats(DevSys s, DevState st, c
             ++a_holes;
         }
         };
+    // Round kr: wait for tile kr, one barrier, then the copy of tile kr + 1
+    // into the other buffer, which no thread reads any more (as in k_sweep).
     if (threadIdx.x == 0 && nrounds > 0) issue(0);
     for (long long kr = 0; kr < nrounds; ++kr) {
         const long long tile = blockIdx.x + kr * gridDim.x;
         const unsigned char *sbase = merge_smem + (kr & 1) * stage_bytes;
-        if (threadIdx.x == 0 && kr + 1 < nrounds) issue(kr + 1);
-        if (stage_rows(tile, n) > 0) {
-            if (threadIdx.x == 0) stage_ok = mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1)) ? 1 : 0;
-            __syncthreads();
-            if (!stage_ok) {
-                if (threadIdx.x == 0) {
-                    set_err(c, NECI_GPU_ERR_TIMEOUT);
-                    (void)mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1));
-                    if (kr + 1 < nrounds) (void)mbar_wait_bounded(&bars[(kr + 1) & 1], (uint32_t)(((kr + 1) >> 1) & 1));
-                }
-                __syncthreads();
-                return;
+        if (threadIdx.x == 0)
+            stage_ok[kr & 1] =
+                stage_rows(tile, n) > 0 ? (mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1)) ? 1 : 0) : 1;
+        __syncthreads();
+        if (!stage_ok[kr & 1]) {
+            if (threadIdx.x == 0) {
+                set_err(c, NECI_GPU_ERR_TIMEOUT);
+                (void)mbar_wait_bounded(&bars[kr & 1], (uint32_t)((kr >> 1) & 1));  // the only copy in flight
             }
+            __syncthreads();
+            return;
         }
+        if (threadIdx.x == 0 && kr + 1 < nrounds) issue(kr + 1);
         const long long j = tile * kStageTile + threadIdx.x;
         if (j < n && !(split && sbase[(size_t)kStageTile * (R * 8 + L * 12) + threadIdx.x]))
             body(j, (const long long *)sbase + (size_t)threadIdx.x * R,
                  (const uint32_t *)(sbase + (size_t)kStageTile * R * 8) + (size_t)threadIdx.x * L,
                  (const long long *)(sbase + (size_t)kStageTile * (R * 8 + L * 4)) + (size_t)threadIdx.x * L);
-        __syncthreads();  // this round's stage is refilled two rounds on
     }
     double v[12] = {a_born[0], a_born[1], a_ann[0], a_ann[1], a_ab[0], a_ab[1], a_rm[0], a_rm[1],
                     a_tp[0], a_tp[1], a_norm[0], a_norm[1]};
