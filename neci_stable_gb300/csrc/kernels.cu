@@ -1468,14 +1468,29 @@ __global__ void __launch_bounds__(256) k_rdm_core(DevSys s, DevState st) {
 }
 
 // Diagonal terms; per-block sums in shared memory when npair doubles fit.
+// The lanes of a warp hold determinants that share most of their orbitals
+// (those near the reference), so walking their pairs in one order would
+// send all lanes' atomics to the same sum at once; each lane walks the list
+// of electron pairs from its own starting point instead.  (The sums are
+// atomics, whose order is not defined in either case.)
 __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use_shared) {
     if (halted(st)) return;
     extern __shared__ double sh_diag[];
+    // the electron pairs (a, b), b < a, as a | b << 8
+    __shared__ uint16_t pairs[kMaxNel * (kMaxNel - 1) / 2];
     const long long npair = s.npair;
-    if (use_shared) {
-        for (long long k = threadIdx.x; k < npair; k += blockDim.x) sh_diag[k] = 0.0;
-        __syncthreads();
+    const int P = s.nel * (s.nel - 1) / 2;
+    for (int k = threadIdx.x; k < P; k += blockDim.x) {
+        // the largest a with a (a - 1) / 2 <= k, from a float estimate
+        int a = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)k)) * 0.5f);
+        while (a > 1 && a * (a - 1) / 2 > k) --a;
+        while ((a + 1) * a / 2 <= k) ++a;
+        pairs[k] = (uint16_t)(a | ((k - a * (a - 1) / 2) << 8));
     }
+    if (use_shared)
+        for (long long k = threadIdx.x; k < npair; k += blockDim.x) sh_diag[k] = 0.0;
+    __syncthreads();
+    const int start = P > 0 ? (int)((threadIdx.x * 7u) % (unsigned)P) : 0;
     const long long n = (long long)min(st.ctl->tot_walkers, (unsigned long long)st.max_walkers);
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
         const long long *r = st.dets + j * s.R;
@@ -1484,13 +1499,15 @@ __global__ void __launch_bounds__(256) k_rdm_diag(DevSys s, DevState st, int use
         uint8_t nI[kMaxNel];
         unsigned long long d[kMaxWords];
         NECI_FOR_WORDS(w, s.W) d[w] = (unsigned long long)r[w];
-        const int nel = decode(d, s.W, nI);
-        for (int a = 1; a < nel; ++a)
-            for (int b = 0; b < a; ++b) {
-                const long long pq = rdm_pair(nI[b], nI[a]);
-                if (use_shared) atomicAdd(&sh_diag[pq], prod);
-                else atomicAdd(&st.rdm2[pq * npair + pq], prod);
-            }
+        if (decode(d, s.W, nI) != s.nel) continue;  // every row holds nel electrons (checked at upload)
+        int k = start;
+        for (int t = 0; t < P; ++t) {
+            const uint32_t ab = pairs[k];
+            const long long pq = rdm_pair(nI[ab >> 8], nI[ab & 0xFFu]);
+            if (use_shared) atomicAdd(&sh_diag[pq], prod);
+            else atomicAdd(&st.rdm2[pq * npair + pq], prod);
+            if (++k == P) k = 0;
+        }
     }
     if (use_shared) {
         __syncthreads();
@@ -1708,7 +1725,10 @@ void launch_rdm(Engine &e, cudaStream_t s) {
     if (e.st.n_core > 0) k_rdm_core<<<clamp_grid(e.st.n_core_seg / 8 + 1, e.num_sms * 8), 256, 0, s>>>(e.sys, e.st);
     const size_t shm = (size_t)e.sys.npair * sizeof(double);
     const int use_shared = shm <= 48 * 1024 ? 1 : 0;  // the default dynamic shared-memory limit
-    k_rdm_diag<<<grid_slots(e), 256, use_shared ? shm : 0, s>>>(e.sys, e.st, use_shared);
+    // at least 64 slots per thread: every block ends by adding its npair
+    // shared sums to the global 2-RDM, so the blocks are kept few
+    const int grid = clamp_grid(e.st.max_walkers / (256 * 64) + 1, e.num_sms);
+    k_rdm_diag<<<grid, 256, use_shared ? shm : 0, s>>>(e.sys, e.st, use_shared);
 }
 
 void launch_final(Engine &e, cudaStream_t s, neci_gpu_iter_stats *out, int *pos, int advance_iter, int split) {
