@@ -1700,7 +1700,10 @@ void launch_ann_compress(Engine &e, cudaStream_t s) {
     else k_ann_compress<1><<<grid_spawns(e, 256, e.occ_compress), 256, 0, s>>>(e.sys, e.st);
 }
 void launch_ann_insert(Engine &e, cudaStream_t s, int split) {
-    const int gp = clamp_grid(e.st.max_spawned / 128 + 1, e.num_sms * e.occ_place);
+    // new determinants are a small part of the spawns: the placement's grid
+    // (one determinant per thread and round) is sized to a fraction of the
+    // spawn capacity, so that a small instance of a batch launches few blocks
+    const int gp = clamp_grid(e.st.max_spawned / 1024 + 1, e.num_sms * e.occ_place);
     if (e.sys.L == 2) {
         k_ann_decide<2><<<grid_spawns(e, 256, e.occ_insert), 256, 0, s>>>(e.sys, e.st, e.d_params);
         k_ann_place<2><<<gp, 128, 0, s>>>(e.sys, e.st, split);
