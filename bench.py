@@ -42,10 +42,10 @@ N_ORB, N_EL, SEED = 24, 10, 20240601
 TARGET_WALKERS = 1.0e7
 BLOOM = 3.0
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, ncu captures of
-# this workload: profiles/step_kernels_n24_pchb_1e7.md, and for the spawn
-# kernel profiles/spawn_fp64_n24_2e6.md) per unit of work, for
-# roofline.traffic: kernel -> (bytes per unit, step count that is the unit).
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum of the ncu capture
+# of the spawn kernel on this workload, profiles/spawn_fp64_n24_2e6.md) per
+# unit of work, for roofline.traffic when that kernel dominates the step:
+# kernel -> (bytes per unit, step count that is the unit).
 # The spawn kernel is bound by instruction issue, not by HBM: its issue
 # figures from the same capture are reported beside its HBM roofline.
 NCU_SPAWN_ISSUE = {"issue_active": 0.586, "alu_pipe": 0.541, "fp64_pipe": 0.372, "warps_active": 0.451,
@@ -53,9 +53,6 @@ NCU_SPAWN_ISSUE = {"issue_active": 0.586, "alu_pipe": 0.541, "fp64_pipe": 0.372,
 
 NCU_DRAM_BYTES_PER_UNIT = {
     "spawn": (15.8, "n_attempts"),
-    "sweep": (47.2, "tot_walkers"),
-    "merge_stats": (38.3, "tot_walkers"),
-    "ann_probe": (102.3, "n_spawned"),
 }
 
 
